@@ -1,0 +1,242 @@
+"""Host-side mirror of fairSIM's ``SimParam`` / ``SimParam.Dir`` / ``OtfProvider`` (estimate).
+
+Field meanings follow the reference:
+  * ``SimParam.create(bands, dirs, phases, size, micronsPerPxl, otf)``
+    (org/fairsim/sim_algorithm/SimParam.java:118-124);
+  * ``Dir.setPxPy`` stores the highest-band shift divided by (nBands-1), ``px(b) = pX*b``
+    (SimParam.java:536-562);
+  * phases ``2*pi*i/nPhases + phaOff`` (SimParam.java:463-477);
+  * modulations clamped to [0.3, 1.1] by ``getModulations`` (SimParam.java:598-607);
+  * ``OtfProvider.fromEstimate(na, lambda, a)`` with cutoff ``1000/(lambda/na/2)`` cycles/micron
+    (OtfProvider.java:96-127), attenuation defaults 0.99 / 1.2 (OtfProvider.java:64).
+
+These are plain parameter records: every computation on them runs in the native library.
+"""
+from __future__ import annotations
+
+import copy
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+
+class OtfProvider:
+    """``OtfProvider.fromEstimate`` parameters (S/OtfProvider.java:96-127)."""
+
+    def __init__(self, na: float, em_wavelength: float, a: float):
+        if a < 0 or a > 1 or na < 0.3 or na > 2.2 or em_wavelength < 300 or em_wavelength > 1500:
+            raise ValueError("unphysical input parameters")
+        self.na = float(na)
+        self.emWavelength = float(em_wavelength)
+        self.a = float(a)
+        self.attStrength = 0.99
+        self.attFWHM = 1.2
+        self.useAttenuation = False
+
+    @staticmethod
+    def fromEstimate(na: float, em_wavelength: float, a: float) -> "OtfProvider":
+        return OtfProvider(na, em_wavelength, a)
+
+    def getCutoff(self) -> float:
+        return 1000.0 / (self.emWavelength / self.na / 2.0)
+
+    def setAttenuation(self, strength: float, fwhm: float) -> None:
+        self.attStrength = float(strength)
+        self.attFWHM = float(fwhm)
+
+    def switchAttenuation(self, on: bool) -> None:
+        self.useAttenuation = bool(on)
+
+    def isAttenuate(self) -> bool:
+        return self.useAttenuation
+
+    def duplicate(self) -> "OtfProvider":
+        return copy.deepcopy(self)
+
+
+@dataclass
+class Dir:
+    nrBands: int
+    nrPhases: int
+    pX: float = 0.0
+    pY: float = 0.0
+    phaOff: float = 0.0
+    phases: Optional[List[float]] = None  # individual phases (None = equidistant)
+    modul: List[float] = field(default_factory=list)
+
+    def __post_init__(self):
+        if self.nrBands < 2:
+            raise ValueError("bands < 2, not useful")
+        if self.nrPhases < 2 * self.nrBands - 1:
+            raise ValueError("not enough phases for bands")
+        if not self.modul:
+            self.modul = [1.0] * self.nrBands
+
+    def setPxPy(self, x: float, y: float) -> None:
+        self.pX = x / (self.nrBands - 1)
+        self.pY = y / (self.nrBands - 1)
+
+    def px(self, band: int) -> float:
+        return self.pX * band
+
+    def py(self, band: int) -> float:
+        return self.pY * band
+
+    def setPhaOff(self, p: float) -> None:
+        self.phaOff = float(p)
+
+    def getPhaOff(self) -> float:
+        return self.phaOff
+
+    def setPhases(self, pha, reset: bool) -> None:
+        if len(pha) != self.nrPhases:
+            raise ValueError("Length mismatch")
+        if reset:
+            self.phaOff = 0.0
+        self.phases = [float(p) for p in pha]
+
+    def getPhases(self) -> List[float]:
+        base = self.phases or [(2 * math.pi / self.nrPhases) * i for i in range(self.nrPhases)]
+        return [b + self.phaOff for b in base]
+
+    def setModulation(self, b: int, m: float) -> bool:
+        self.modul[b] = float(m)
+        return 0.3 < m < 1.1
+
+    def getModulations(self) -> List[float]:
+        return [min(max(m, 0.3), 1.1) for m in self.modul]
+
+    def nrComp(self) -> int:
+        return 2 * self.nrBands - 1
+
+
+class SimParam:
+    """2D subset of ``SimParam`` (S/SimParam.java:31-615)."""
+
+    def __init__(self, bands: int, dirs: int, phases: int, size: int, microns_per_pxl: float, otf: OtfProvider):
+        if dirs < 1:
+            raise ValueError("dirs < 1, not useful")
+        self.nrDirs = int(dirs)
+        self.nrBands = int(bands)
+        self.nrPhases = int(phases)
+        self.directions = [Dir(bands, phases) for _ in range(dirs)]
+        self.imgSize = int(size)
+        self.micronsPerPixel = float(microns_per_pxl)
+        self._otf = otf
+        self.wienerFilterParameter = 0.05
+        self.apoCutOff = 2.0
+        self.apoBend = 0.9  # runReconstruction's fixed bend (SimAlgorithm.java:277)
+
+    @staticmethod
+    def create(bands, dirs, phases, size, microns_per_pxl, otf) -> "SimParam":
+        return SimParam(bands, dirs, phases, size, microns_per_pxl, otf)
+
+    def dir(self, i: int) -> Dir:
+        return self.directions[i]
+
+    def nrDir(self) -> int:
+        return self.nrDirs
+
+    def nrBand(self) -> int:
+        return self.nrBands
+
+    def otf(self) -> OtfProvider:
+        return self._otf
+
+    def pxlSizeCyclesMicron(self) -> float:
+        return 1.0 / (self.imgSize * self.micronsPerPixel)
+
+    def setPxlSize(self, size: int, microns: Optional[float] = None) -> "SimParam":
+        self.imgSize = int(size)
+        if microns is not None:
+            self.micronsPerPixel = float(microns)
+        return self
+
+    def setWienerFilter(self, w: float) -> "SimParam":
+        self.wienerFilterParameter = float(w)
+        return self
+
+    def getWienerFilter(self) -> float:
+        return self.wienerFilterParameter
+
+    def setApoCutoff(self, a: float) -> "SimParam":
+        self.apoCutOff = float(a)
+        return self
+
+    def getApoCutoff(self) -> float:
+        return self.apoCutOff
+
+    def vectorWidth(self) -> int:
+        return self.imgSize
+
+    def vectorHeight(self) -> int:
+        return self.imgSize
+
+    def duplicate(self) -> "SimParam":
+        return copy.deepcopy(self)
+
+    # flat views used by the native bindings (and by the oracle's ctypes struct)
+    @property
+    def w(self):
+        return self.imgSize
+
+    @property
+    def na(self):
+        return self._otf.na
+
+    @property
+    def emWavelength(self):
+        return self._otf.emWavelength
+
+    @property
+    def otfA(self):
+        return self._otf.a
+
+    @property
+    def useAttenuation(self):
+        return self._otf.useAttenuation
+
+    @property
+    def attStrength(self):
+        return self._otf.attStrength
+
+    @property
+    def attFWHM(self):
+        return self._otf.attFWHM
+
+    @property
+    def wiener(self):
+        return self.wienerFilterParameter
+
+    @property
+    def apoCutoff(self):
+        return self.apoCutOff
+
+    @property
+    def pX(self):
+        return [d.pX for d in self.directions]
+
+    @property
+    def pY(self):
+        return [d.pY for d in self.directions]
+
+    @property
+    def phaOff(self):
+        return [d.phaOff for d in self.directions]
+
+    @property
+    def modulations(self):
+        return [list(d.modul) for d in self.directions]
+
+    @property
+    def phases(self):
+        if all(d.phases is None for d in self.directions):
+            return None
+        return [d.phases or [(2 * math.pi / d.nrPhases) * i for i in range(d.nrPhases)] for d in self.directions]
+
+    def set_from(self, vals: dict) -> None:
+        for d in range(self.nrDirs):
+            self.directions[d].pX = vals["pX"][d]
+            self.directions[d].pY = vals["pY"][d]
+            self.directions[d].phaOff = vals["phaOff"][d]
+            self.directions[d].modul = list(vals["modulations"][d])

@@ -1,0 +1,121 @@
+"""Known-answer tests that pin the CPU restatement (the oracle) of fairSIM's Java path.
+
+The reference has no test suite and no golden data, so these tests pin each building
+block against mathematics it must satisfy, following the reference's own self-checks
+(org/fairsim/linalg/MTool.java:80-92, org/fairsim/linalg/MatrixComplex.java:307-327)."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+
+@pytest.mark.parametrize("n", [64, 96, 128, 384])
+@pytest.mark.parametrize("dtype,tol", [(np.float32, 2e-6), (np.float64, 1e-13)])
+def test_fft2d_matches_numpy(oracle, n, dtype, tol):
+    rng = np.random.default_rng(n)
+    z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    f = oracle.fft2d(z, inverse=False, dtype=dtype)
+    assert rel_l2(f, np.fft.fft2(z)) < tol
+    g = oracle.fft2d(z, inverse=True, dtype=dtype)  # JTransforms complexInverse(scale=true)
+    assert rel_l2(g, np.fft.ifft2(z)) < tol
+
+
+def test_fft2d_non_square(oracle):
+    rng = np.random.default_rng(3)
+    z = rng.standard_normal((48, 80)) + 1j * rng.standard_normal((48, 80))
+    assert rel_l2(oracle.fft2d(z, dtype=np.float64), np.fft.fft2(z)) < 1e-13
+
+
+def test_fsin_error_bound(oracle):
+    # MTool.fsin documents 5.4e-9 max error; the reference's main() scans +-6 pi in 0.01 steps
+    worst = 0.0
+    for r in np.arange(-6 * math.pi, 6 * math.pi, 0.01):
+        worst = max(worst, abs(oracle.fsin(r) - math.sin(r)), abs(oracle.fcos(r) - math.cos(r)))
+    assert worst <= 5.5e-9
+
+
+def test_matrix_inverse_identity(oracle):
+    rng = np.random.default_rng(7)
+    for n in (3, 5):
+        M = rng.uniform(-1, 1, (n, n)) + 1j * rng.uniform(-1, 1, (n, n))
+        inv = oracle.matrix_inverse(M)
+        assert np.abs(inv @ M - np.eye(n)).max() < 1e-10
+    A = rng.uniform(-1, 1, (5, 3)) + 1j * rng.uniform(-1, 1, (5, 3))
+    pinv = oracle.matrix_inverse(A, pseudo=True)
+    assert np.abs(pinv - np.linalg.pinv(A)).max() < 1e-10
+
+
+@pytest.mark.parametrize("n_pha,bands", [(3, 2), (5, 2), (5, 3)])
+def test_band_separation_recovers_bands(oracle, fs, n_pha, bands):
+    n = 32
+    rng = np.random.default_rng(11)
+    nc = 2 * bands - 1
+    truth = rng.standard_normal((nc, n, n)) + 1j * rng.standard_normal((nc, n, n))
+    phases = [2 * math.pi * p / n_pha + 0.3 for p in range(n_pha)]
+    mod = [1.0] + [0.7] * (bands - 1)
+    fac = [mod[0]] + [0.5 * m for m in mod[1:]]
+    mixed = []
+    for p in range(n_pha):
+        img = fac[0] * truth[0]
+        for j in range(bands - 1):
+            ph = phases[p] * (j + 1)
+            img = img + fac[j + 1] * np.exp(1j * ph) * truth[2 * j + 1] + fac[j + 1] * np.exp(-1j * ph) * truth[2 * j + 2]
+        mixed.append(img)
+    otf = fs.OtfProvider.fromEstimate(1.4, 525, 1.0)
+    sp = fs.SimParam.create(bands, 1, n_pha, n, 0.08, otf)
+    sp.dir(0).setPhaOff(0.3)
+    for b in range(1, bands):
+        sp.dir(0).setModulation(b, 0.7)
+    sep = oracle.separate_bands(sp, 0, np.array(mixed), dtype=np.float64)
+    assert rel_l2(sep, truth) < 1e-10
+
+
+def test_integer_fourier_shift_is_roll(oracle):
+    n = 64
+    rng = np.random.default_rng(5)
+    z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    # SimUtils.fourierShift(v, kx, ky): ifft, times exp(i 2pi (kx x - ky y)/N), fft
+    real = np.fft.ifft2(z)
+    real = oracle.fourier_shift(real, 5.0, -(-3.0), dtype=np.float64)
+    shifted = np.fft.fft2(real)
+    assert rel_l2(shifted, np.roll(np.roll(z, 5, axis=1), 3, axis=0)) < 1e-12
+
+
+def test_paste_freq_layout(oracle):
+    z = np.arange(16, dtype=np.float64).reshape(4, 4) + 0j
+    out = oracle.paste_freq(z, 8, 8, dtype=np.float64)
+    # x<wi/2 stays, x>=wi/2 moves by wo/2 (org/fairsim/linalg/BasicVectors.java:275-283)
+    assert out[0, 0] == 0 and out[0, 1] == 1 and out[0, 6] == 2 and out[0, 7] == 3
+    assert out[6, 0] == 8 and out[7, 7] == 15 and out[2, 2] == 0
+    off = oracle.paste_freq(z, 8, 8, 1, -1, dtype=np.float64)
+    assert off[7, 1] == 0 and off[0, 2] == 5
+
+
+def test_otf_lookup_is_floor_indexed(oracle, fs):
+    # getOtfVal returns vals[floor(pos)] (S/OtfProvider.java:208-219)
+    n = 64
+    otf = fs.OtfProvider.fromEstimate(1.4, 525, 0.3)
+    sp = fs.SimParam.create(2, 1, 3, n, 0.08, otf)
+    v = oracle.otf_vector(sp, np.zeros((n, n), complex), 0, 0, which=0, dtype=np.float64)
+    cut = 1000 / (525 / 1.4 / 2)
+    cpm = 1 / (n * 0.08)
+    step = cut / 512
+    for x in (1, 3, 7, 11):
+        pos = x * cpm / step
+        d = math.floor(pos) / 512
+        ideal = (2 / math.pi) * (math.acos(d) - d * math.sqrt(1 - d * d)) * 0.3 ** d
+        assert abs(v[0, x].real - ideal) < 1e-12
+
+
+def test_estimation_recovers_seeded_k0(oracle, fs):
+    n = 256
+    raw, truth = fs.synth.make_dataset(n=n, seed=4)
+    sp = fs.synth.sim_param_for(truth, n, known=False)
+    spec = oracle.prepare_raw(sp, raw)
+    est, peaks, coarse = oracle.estimate(sp, spec, 1, 0.6)
+    for d in range(3):
+        assert abs(est["pX"][d] - truth["pxpy"][d][0]) < 0.1
+        assert abs(est["pY"][d] - truth["pxpy"][d][1]) < 0.1
+        assert abs(est["modulations"][d][1] - truth["modulation"]) < 0.15
