@@ -1,0 +1,360 @@
+// Parameter estimation on the device: Correlation.commonRegion / locatePeak / fitPeak /
+// getPeak and SimAlgorithm.estimateParameters (S/Correlation.java:43-288,
+// S/SimAlgorithm.java:37-159; the live refit of LM/ReconstructionRunner.java:642-746).
+//
+// The 10x10 sub-pixel grid of fitPeak is evaluated in two passes instead of 100 shifted
+// vector copies: the shift phase ramp is separable, so
+//   corr(xi, yi) = sum_y ty[yi](y) * sum_x tx[xi](x) * b1(x,y) * conj(b0(x,y)),
+// first 10 row sums per image row (one block per row), then the 100 column sums.
+// Both passes accumulate in FP64 in a fixed order (deterministic).
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "estimate.cuh"
+#include "filters.cuh"
+#include "otf.cuh"
+#include "runtime.cuh"
+#include "sim_host.h"
+#include "vec_ops.cuh"
+
+namespace fsim {
+
+// ---- commonRegion as a gather (Correlation.java:227-288) --------------------------------
+__global__ void k_common_region(float2* __restrict__ b0, float2* __restrict__ b1, int w, int h,
+                                const OtfTable* __restrict__ t, double kx, double ky, double dist, double wl, int divide) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= w) return;
+  const double xh = freq_x(x, w), yh = freq_y(y, h);
+  float w0 = 0.f, w1 = 0.f, t0 = 0.f, t1 = 0.f;
+  if (!otf_at(*t, xh, yh, 0, 0, false, &w0)) w0 = 0.f;
+  w1 = w0;  // single-band OTF: weight1 == weight0
+  if (!otf_at(*t, xh, yh, kx, ky, false, &t0)) t0 = 0.f;
+  if (!otf_at(*t, xh, yh, -kx, -ky, false, &t1)) t1 = 0.f;
+  const size_t i = (size_t)y * w + x;
+  float2 v0 = b0[i], v1 = b1[i];
+  // |OTF| of (val, 0) computed as (float)sqrt((double)val*val) == |val|
+  if (fabsf(w0) < wl || fabsf(t0) < wl) {
+    v0 = make_float2(0.f, 0.f);
+  } else if (divide) {
+    float r = __fdiv_rn(w0, __fmul_rn(w0, w0));  // Cplx.Float.reciproc, real part
+    v0 = make_float2(__fmul_rn(v0.x, r), __fmul_rn(v0.y, r));
+  }
+  if (fabsf(w1) < wl || fabsf(t1) < wl) {
+    v1 = make_float2(0.f, 0.f);
+  } else if (divide) {
+    float r = __fdiv_rn(w1, __fmul_rn(w1, w1));
+    v1 = make_float2(__fmul_rn(v1.x, r), __fmul_rn(v1.y, r));
+  }
+  const double mx = sqrt(kx * kx + ky * ky);
+  auto cut = [&](int xx, int yy) {
+    long long a = (xx < w / 2) ? (long long)xx * xx : (long long)(xx - w) * (xx - w);
+    long long b = (yy < h / 2) ? (long long)yy * yy : (long long)(yy - h) * (yy - h);
+    double ratio = sqrt((double)(a + b)) / mx;
+    return (ratio < dist) || (ratio > (1 - dist));
+  };
+  if (cut(x, y)) v0 = make_float2(0.f, 0.f);
+  // band1 is zeroed at ((x-(int)kx+w)%w, (y+(int)ky+h)%h) for every cut (x,y)
+  const int ikx = (int)kx, iky = (int)ky;
+  const int xs = ((x + ikx) % w + w) % w, ys = ((y - iky) % h + h) % h;
+  if (cut(xs, ys)) v1 = make_float2(0.f, 0.f);
+  b0[i] = v0;
+  b1[i] = v1;
+}
+
+// ---- locatePeak: argmax |v| outside kMin, first in y-major scan order --------------------
+__global__ void k_peak_partial(const float2* __restrict__ v, int w, int h, double kmin, float* pmag, int* pidx) {
+  float best = -1.f;
+  int bi = 0x7fffffff;
+  const int n = w * h;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int x = i % w, y = i / w;
+    long long a = (x < w / 2) ? (long long)x * x : (long long)(x - w) * (x - w);
+    long long b = (y < h / 2) ? (long long)y * y : (long long)(y - h) * (y - h);
+    double rad = sqrt((double)(a + b));
+    if (rad > kmin) {
+      float2 z = v[i];
+      float m = (float)sqrt((double)z.x * z.x + (double)z.y * z.y);  // Cplx.Float.abs()
+      if (m > best || (m == best && i < bi)) {
+        best = m;
+        bi = i;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    float m2 = __shfl_down_sync(0xffffffffu, best, o);
+    int i2 = __shfl_down_sync(0xffffffffu, bi, o);
+    if (m2 > best || (m2 == best && i2 < bi)) {
+      best = m2;
+      bi = i2;
+    }
+  }
+  __shared__ float sm[32];
+  __shared__ int si[32];
+  if (threadIdx.x % 32 == 0) {
+    sm[threadIdx.x / 32] = best;
+    si[threadIdx.x / 32] = bi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x / 32); k++)
+      if (sm[k] > best || (sm[k] == best && si[k] < bi)) {
+        best = sm[k];
+        bi = si[k];
+      }
+    pmag[blockIdx.x] = best;
+    pidx[blockIdx.x] = bi;
+  }
+}
+
+// ---- correlation grid ---------------------------------------------------------------------
+// ramp tables: tx[j][x] = exp(+2 pi i * kxj * x / N), ty[j][y] = exp(+2 pi i * kyj * y / N)
+// (fourierShift(xpos, -ypos) => ky_j = -ypos_j), phases reduced modulo one turn in double.
+__global__ void k_ramp_table(float2* __restrict__ tab, const double* __restrict__ k, int nk, int N) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (x >= N || j >= nk) return;
+  double f = k[j] * (double)x / (double)N;
+  f -= floor(f);
+  double s, c;
+  sincospi(2.0 * f, &s, &c);
+  tab[(size_t)j * N + x] = make_float2((float)c, (float)s);
+}
+
+// pass 1: Q[j][y] = sum_x b1(x,y) conj(b0(x,y)) tx[j][x], one block per row
+template <int NK>
+__global__ void k_corr_rows(const float2* __restrict__ b0, const float2* __restrict__ b1, const float2* __restrict__ tx,
+                            int N, double2* __restrict__ Q) {
+  const int y = blockIdx.x;
+  double2 acc[NK];
+#pragma unroll
+  for (int j = 0; j < NK; j++) acc[j] = make_double2(0, 0);
+  for (int x = threadIdx.x; x < N; x += blockDim.x) {
+    size_t i = (size_t)y * N + x;
+    float2 p = cmulc(b1[i], b0[i]);  // b1 * conj(b0)
+#pragma unroll
+    for (int j = 0; j < NK; j++) {
+      float2 r = cmul(p, tx[(size_t)j * N + x]);
+      acc[j].x += r.x;
+      acc[j].y += r.y;
+    }
+  }
+  __shared__ double2 red[NK][32];
+#pragma unroll
+  for (int j = 0; j < NK; j++) {
+    double a = acc[j].x, b = acc[j].y;
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (threadIdx.x % 32 == 0) red[j][threadIdx.x / 32] = make_double2(a, b);
+  }
+  __syncthreads();
+  if (threadIdx.x < NK) {
+    double a = 0, b = 0;
+    for (int k = 0; k < (int)(blockDim.x / 32); k++) {
+      a += red[threadIdx.x][k].x;
+      b += red[threadIdx.x][k].y;
+    }
+    Q[(size_t)threadIdx.x * N + y] = make_double2(a, b);
+  }
+}
+
+// pass 2: corr[jy][jx] = sum_y Q[jx][y] * ty[jy][y], one warp per output
+__global__ void k_corr_cols(const double2* __restrict__ Q, const float2* __restrict__ ty, int N, int nkx, int nky,
+                            double scal, double2* __restrict__ out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
+  if (warp >= nkx * nky) return;
+  const int jx = warp % nkx, jy = warp / nkx;
+  double a = 0, b = 0;
+  for (int y = lane; y < N; y += 32) {
+    double2 q = Q[(size_t)jx * N + y];
+    float2 t = ty[(size_t)jy * N + y];
+    a += q.x * t.x - q.y * t.y;
+    b += q.x * t.y + q.y * t.x;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) out[warp] = make_double2(a * scal, b * scal);  // Cplx.mult(sum, (scal,0))
+}
+
+// ---- host side ------------------------------------------------------------------------------
+int common_region_device(float2* b0, float2* b1, int w, int h, const OtfTable* t, double kx, double ky, double dist,
+                         double wl, bool divide, cudaStream_t st) {
+  dim3 g(div_up(w, 128), h);
+  k_common_region<<<g, 128, 0, st>>>(b0, b1, w, h, t, kx, ky, dist, wl, divide ? 1 : 0);
+  FSIM_CHECK_LAUNCH();
+  return FSIM_OK;
+}
+
+int locate_peak_device(const float2* v, int w, int h, double kmin, EstScratch& s, cudaStream_t st, double out4[4]) {
+  const int blocks = 128;
+  k_peak_partial<<<blocks, 256, 0, st>>>(v, w, h, kmin, s.pmag, s.pidx);
+  FSIM_CHECK_LAUNCH();
+  std::vector<float> m(blocks);
+  std::vector<int> idx(blocks);
+  FSIM_CUDA(cudaMemcpyAsync(m.data(), s.pmag, sizeof(float) * blocks, cudaMemcpyDeviceToHost, st));
+  FSIM_CUDA(cudaMemcpyAsync(idx.data(), s.pidx, sizeof(int) * blocks, cudaMemcpyDeviceToHost, st));
+  FSIM_CUDA(cudaStreamSynchronize(st));
+  float best = -1.f;
+  int bi = 0x7fffffff;
+  for (int b = 0; b < blocks; b++)
+    if (m[b] > best || (m[b] == best && idx[b] < bi)) {
+      best = m[b];
+      bi = idx[b];
+    }
+  double xPos = -0., yPos = -1, phase = 0;
+  double max = -1;
+  if (bi != 0x7fffffff && best >= 0) {
+    xPos = bi % w;
+    yPos = bi / w;
+    max = best;
+    float2 z;
+    FSIM_CUDA(cudaMemcpyAsync(&z, v + bi, sizeof(float2), cudaMemcpyDeviceToHost, st));
+    FSIM_CUDA(cudaStreamSynchronize(st));
+    phase = (double)(float)std::atan2((double)z.y, (double)z.x);  // Cplx.Float.phase()
+  }
+  if (xPos > w / 2) xPos = xPos - w;
+  if (yPos > h / 2)
+    yPos = h - yPos;
+  else
+    yPos *= -1;
+  out4[0] = xPos;
+  out4[1] = yPos;
+  out4[2] = max;
+  out4[3] = phase;
+  return FSIM_OK;
+}
+
+int EstScratch::alloc(int N, cudaStream_t st) {
+  if (n == N && b0) return FSIM_OK;
+  free(st);
+  n = N;
+  size_t img = (size_t)N * N * sizeof(float2);
+  FSIM_CUDA(cudaMallocAsync(&b0, img, st));
+  FSIM_CUDA(cudaMallocAsync(&b1, img, st));
+  FSIM_CUDA(cudaMallocAsync(&tx, sizeof(float2) * 10 * N, st));
+  FSIM_CUDA(cudaMallocAsync(&ty, sizeof(float2) * 10 * N, st));
+  FSIM_CUDA(cudaMallocAsync(&Q, sizeof(double2) * 10 * N, st));
+  FSIM_CUDA(cudaMallocAsync(&corr, sizeof(double2) * 100, st));
+  FSIM_CUDA(cudaMallocAsync(&kbuf, sizeof(double) * 20, st));
+  FSIM_CUDA(cudaMallocAsync(&pmag, sizeof(float) * 256, st));
+  FSIM_CUDA(cudaMallocAsync(&pidx, sizeof(int) * 256, st));
+  return FSIM_OK;
+}
+void EstScratch::free(cudaStream_t st) {
+  void* ps[] = {b0, b1, tx, ty, Q, corr, kbuf, pmag, pidx};
+  for (void* p : ps)
+    if (p) cudaFreeAsync(p, st);
+  b0 = b1 = nullptr;
+  tx = ty = nullptr;
+  Q = corr = nullptr;
+  kbuf = nullptr;
+  pmag = nullptr;
+  pidx = nullptr;
+  n = 0;
+}
+
+// Evaluates corr(xi, yi) for kx grid kxs[nx] and ky grid kys[ny] (before the fourierShift
+// sign flip of ky) on real-space b0/b1 already prepared; out[yi*nx + xi].
+int corr_grid_device(const float2* b0, const float2* b1, int N, const double* kxs, int nx, const double* kys, int ny,
+                     double scal, EstScratch& s, cudaStream_t st, std::vector<std::complex<double>>& out) {
+  double k[20];
+  for (int i = 0; i < nx; i++) k[i] = kxs[i];
+  for (int i = 0; i < ny; i++) k[10 + i] = -kys[i];
+  FSIM_CUDA(cudaMemcpyAsync(s.kbuf, k, sizeof(double) * 20, cudaMemcpyHostToDevice, st));
+  k_ramp_table<<<dim3(div_up(N, 128), nx), 128, 0, st>>>(s.tx, s.kbuf, nx, N);
+  k_ramp_table<<<dim3(div_up(N, 128), ny), 128, 0, st>>>(s.ty, s.kbuf + 10, ny, N);
+  if (nx == 10)
+    k_corr_rows<10><<<N, 256, 0, st>>>(b0, b1, s.tx, N, s.Q);
+  else
+    k_corr_rows<1><<<N, 256, 0, st>>>(b0, b1, s.tx, N, s.Q);
+  int warps = nx * ny;
+  k_corr_cols<<<div_up(warps * 32, 256), 256, 0, st>>>(s.Q, s.ty, N, nx, ny, scal, s.corr);
+  FSIM_CHECK_LAUNCH();
+  std::vector<double2> h(nx * ny);
+  FSIM_CUDA(cudaMemcpyAsync(h.data(), s.corr, sizeof(double2) * nx * ny, cudaMemcpyDeviceToHost, st));
+  FSIM_CUDA(cudaStreamSynchronize(st));
+  out.resize(nx * ny);
+  for (int i = 0; i < nx * ny; i++) out[i] = std::complex<double>(h[i].x, h[i].y);
+  return FSIM_OK;
+}
+
+// norm2 of a device vector in FP64 (float squares), synchronous
+int norm2_device(const float2* v, size_t n, double* out, cudaStream_t st);
+
+// Correlation.fitPeak (Correlation.java:43-136) on device spectra band0/band1 (w x w).
+int fit_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
+                    double search, EstScratch& s, cudaStream_t st, double out4[4], double* grid_out) {
+  double resPhase = 0, resMag = 0;
+  const size_t img = (size_t)N * N * sizeof(float2);
+  for (int iter = 0; iter < 3; iter++) {
+    FSIM_CUDA(cudaMemcpyAsync(s.b0, band0, img, cudaMemcpyDeviceToDevice, st));
+    FSIM_CUDA(cudaMemcpyAsync(s.b1, band1, img, cudaMemcpyDeviceToDevice, st));
+    int rc = common_region_device(s.b0, s.b1, N, N, t, kx, ky, 0.15, wl, true, st);
+    if (rc) return rc;
+    rc = fft2d_device(s.b0, N, N, true, st);
+    if (rc) return rc;
+    rc = fft2d_device(s.b1, N, N, true, st);
+    if (rc) return rc;
+    double n2 = 0;
+    rc = norm2_device(s.b0, (size_t)N * N, &n2, st);
+    if (rc) return rc;
+    const double scal = 1. / n2;
+    double kxs[10], kys[10];
+    for (int i = 0; i < 10; i++) {
+      kxs[i] = kx + ((i - 4.5) / 4.5) * search;
+      kys[i] = ky + ((i - 4.5) / 4.5) * search;
+    }
+    std::vector<std::complex<double>> corr;
+    rc = corr_grid_device(s.b0, s.b1, N, kxs, 10, kys, 10, scal, s, st, corr);
+    if (rc) return rc;
+    double max = 0, newKx = 0, newKy = 0;
+    for (int yi = 0; yi < 10; yi++)
+      for (int xi = 0; xi < 10; xi++) {
+        std::complex<double> c = corr[yi * 10 + xi];
+        double hv = std::hypot(c.real(), c.imag());
+        if (grid_out) {
+          grid_out[(iter * 100 + yi * 10 + xi) * 2] = c.real();
+          grid_out[(iter * 100 + yi * 10 + xi) * 2 + 1] = c.imag();
+        }
+        if (hv > max) {
+          max = hv;
+          newKx = kxs[xi];
+          newKy = kys[yi];
+          resPhase = std::atan2(c.imag(), c.real());
+          resMag = hv;
+        }
+      }
+    kx = newKx;
+    ky = newKy;
+    search /= 5;
+  }
+  out4[0] = kx;
+  out4[1] = ky;
+  out4[2] = resPhase;
+  out4[3] = resMag;
+  return FSIM_OK;
+}
+
+// Correlation.getPeak (Correlation.java:183-209)
+int get_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
+                    EstScratch& s, cudaStream_t st, std::complex<double>* out) {
+  const size_t img = (size_t)N * N * sizeof(float2);
+  FSIM_CUDA(cudaMemcpyAsync(s.b0, band0, img, cudaMemcpyDeviceToDevice, st));
+  FSIM_CUDA(cudaMemcpyAsync(s.b1, band1, img, cudaMemcpyDeviceToDevice, st));
+  int rc = common_region_device(s.b0, s.b1, N, N, t, kx, ky, 0.15, wl, true, st);
+  if (rc) return rc;
+  if ((rc = fft2d_device(s.b0, N, N, true, st))) return rc;
+  if ((rc = fft2d_device(s.b1, N, N, true, st))) return rc;
+  double n2 = 0;
+  if ((rc = norm2_device(s.b0, (size_t)N * N, &n2, st))) return rc;
+  std::vector<std::complex<double>> c;
+  rc = corr_grid_device(s.b0, s.b1, N, &kx, 1, &ky, 1, 1. / n2, s, st, c);
+  if (rc) return rc;
+  *out = c[0];
+  return FSIM_OK;
+}
+
+}  // namespace fsim

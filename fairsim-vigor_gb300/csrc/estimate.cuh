@@ -1,0 +1,39 @@
+// Internal interface of the device parameter estimation (estimate.cu, algo.cu).
+#pragma once
+
+#include <complex>
+#include <vector>
+
+#include "common.cuh"
+#include "otf.cuh"
+
+namespace fsim {
+
+// Device scratch of one estimation (allocated stream-ordered; reused across calls).
+struct EstScratch {
+  int n = 0;
+  float2 *b0 = nullptr, *b1 = nullptr, *tx = nullptr, *ty = nullptr;
+  double2 *Q = nullptr, *corr = nullptr;
+  double* kbuf = nullptr;
+  float* pmag = nullptr;
+  int* pidx = nullptr;
+  int alloc(int N, cudaStream_t st);
+  void free(cudaStream_t st);
+};
+
+int common_region_device(float2* b0, float2* b1, int w, int h, const OtfTable* t, double kx, double ky, double dist,
+                         double wl, bool divide, cudaStream_t st);
+int locate_peak_device(const float2* v, int w, int h, double kmin, EstScratch& s, cudaStream_t st, double out4[4]);
+int corr_grid_device(const float2* b0, const float2* b1, int N, const double* kxs, int nx, const double* kys, int ny,
+                     double scal, EstScratch& s, cudaStream_t st, std::vector<std::complex<double>>& out);
+int fit_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
+                    double search, EstScratch& s, cudaStream_t st, double out4[4], double* grid_out);
+int get_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
+                    EstScratch& s, cudaStream_t st, std::complex<double>* out);
+
+// SimAlgorithm.estimateParameters (live=false) or ParameterRefitThread.doRefit (live=true)
+// on device spectra spec[a*nP + p] (N x N complex); updates p's shifts/phases/modulations.
+int estimate_core(fsim_sim_param* p, const float2* const* spec, int fit_band, double fit_exclude, bool live,
+                  double* peaks_out, cudaStream_t st);
+
+}  // namespace fsim

@@ -1,0 +1,155 @@
+// 2D complex FFT (the replacement of the reference's cufftExecC2C path,
+// accel/cuda_cplx.cu:475-514) built from the Stockham line FFT of fft_line.cuh:
+//   pass 1: rows   - G rows per block, each row by T threads, coalesced row loads;
+//   pass 2: columns - C adjacent columns per block interleaved in shared memory so that
+//           every global access moves C*8 contiguous bytes (64 B for C = 8).
+// Each pass reads and writes the array once (16 bytes per complex element per pass).
+#include "common.cuh"
+#include "fft_line.cuh"
+#include "runtime.cuh"
+#include "vec_ops.cuh"
+
+namespace fsim {
+
+template <int L>
+struct LinePlan {
+  static constexpr int E = (L % 3 == 0) ? 12 : 16;
+  static constexpr int T = L / E;
+  static constexpr int G = T >= 256 ? 1 : 256 / T;  // rows per block in the row pass
+  static constexpr int C = L <= 1024 ? 8 : (L <= 3072 ? 4 : 2);  // columns per block, column pass
+};
+
+template <int L, bool INV>
+__global__ void __launch_bounds__(256) k_fft_rows(float2* __restrict__ data, int nrows, size_t item_stride, float scale) {
+  using P = LinePlan<L>;
+  constexpr int T = P::T, E = P::E, G = P::G, SL = smem_line_elems(L, 1);
+  extern __shared__ float2 sm[];
+  const int g = threadIdx.x / T, t = threadIdx.x % T;
+  const int row = blockIdx.x * G + g;
+  float2* s = sm + g * SL;
+  float2* base = data + blockIdx.y * item_stride + (size_t)row * L;
+  if (row < nrows) {
+#pragma unroll
+    for (int i = 0; i < E; i++) s[sidx(t + i * T)] = base[t + i * T];
+  }
+  __syncthreads();
+  line_fft<L, T, 1, INV>(s, t);
+  if (row < nrows) {
+#pragma unroll
+    for (int i = 0; i < E; i++) base[t + i * T] = cscale(s[sidx(t + i * T)], scale);
+  }
+}
+
+template <int L, bool INV>
+__global__ void k_fft_cols(float2* __restrict__ data, int ncols, size_t item_stride, float scale) {
+  using P = LinePlan<L>;
+  constexpr int T = P::T, E = P::E, C = P::C;
+  extern __shared__ float2 s[];
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int x = blockIdx.x * C + c;
+  float2* base = data + blockIdx.y * item_stride;
+#pragma unroll
+  for (int i = 0; i < E; i++) {
+    int k = t + i * T;
+    s[sidx(k * C + c)] = (x < ncols) ? base[(size_t)k * ncols + x] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  line_fft<L, T, C, INV>(s, threadIdx.x);
+  if (x < ncols) {
+#pragma unroll
+    for (int i = 0; i < E; i++) {
+      int k = t + i * T;
+      base[(size_t)k * ncols + x] = cscale(s[sidx(k * C + c)], scale);
+    }
+  }
+}
+
+template <int L, bool INV>
+static int launch_rows(float2* d, int nrows, int batch, size_t stride, float scale, cudaStream_t st) {
+  using P = LinePlan<L>;
+  size_t smem = sizeof(float2) * (size_t)P::G * smem_line_elems(L, 1);
+  static bool attr = false;
+  if (!attr) {
+    FSIM_CUDA(cudaFuncSetAttribute(k_fft_rows<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  dim3 grid(div_up(nrows, P::G), batch);
+  k_fft_rows<L, INV><<<grid, P::G * P::T, smem, st>>>(d, nrows, stride, scale);
+  FSIM_CHECK_LAUNCH();
+  return FSIM_OK;
+}
+
+template <int L, bool INV>
+static int launch_cols(float2* d, int ncols, int batch, size_t stride, float scale, cudaStream_t st) {
+  using P = LinePlan<L>;
+  size_t smem = sizeof(float2) * (size_t)smem_line_elems(L, P::C);
+  static bool attr = false;
+  if (!attr) {
+    FSIM_CUDA(cudaFuncSetAttribute(k_fft_cols<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  dim3 grid(div_up(ncols, P::C), batch);
+  k_fft_cols<L, INV><<<grid, P::C * P::T, smem, st>>>(d, ncols, stride, scale);
+  FSIM_CHECK_LAUNCH();
+  return FSIM_OK;
+}
+
+#define FSIM_FFT_LENGTHS(X) \
+  X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(1536) X(2048) X(3072) X(4096)
+
+static bool len_ok(int L) {
+  switch (L) {
+#define CASE(n) case n:
+    FSIM_FFT_LENGTHS(CASE)
+#undef CASE
+    return true;
+    default:
+      return false;
+  }
+}
+
+bool fft2d_supported(int w, int h) { return len_ok(w) && len_ok(h); }
+
+static int rows_dispatch(int L, bool inv, float2* d, int nrows, int batch, size_t stride, float scale, cudaStream_t st) {
+  switch (L) {
+#define CASE(n)                                                                          \
+  case n:                                                                                \
+    return inv ? launch_rows<n, true>(d, nrows, batch, stride, scale, st)               \
+               : launch_rows<n, false>(d, nrows, batch, stride, scale, st);
+    FSIM_FFT_LENGTHS(CASE)
+#undef CASE
+  }
+  set_error("unsupported FFT length %d", L);
+  return FSIM_EINVAL;
+}
+static int cols_dispatch(int L, bool inv, float2* d, int ncols, int batch, size_t stride, float scale, cudaStream_t st) {
+  switch (L) {
+#define CASE(n)                                                                          \
+  case n:                                                                                \
+    return inv ? launch_cols<n, true>(d, ncols, batch, stride, scale, st)               \
+               : launch_cols<n, false>(d, ncols, batch, stride, scale, st);
+    FSIM_FFT_LENGTHS(CASE)
+#undef CASE
+  }
+  set_error("unsupported FFT length %d", L);
+  return FSIM_EINVAL;
+}
+
+int fft2d_device(float2* data, int w, int h, bool inverse, cudaStream_t stream, int batch) {
+  FSIM_REQUIRE(fft2d_supported(w, h), FSIM_EINVAL,
+               "fft2d: unsupported size %d x %d (lengths 2^k in 32..4096 and 3*2^k in 48..3072)", w, h);
+  size_t stride = (size_t)w * h;
+  int rc = rows_dispatch(w, inverse, data, h, batch, stride, 1.f, stream);
+  if (rc) return rc;
+  float scale = inverse ? (float)(1.0 / ((double)w * (double)h)) : 1.f;
+  return cols_dispatch(h, inverse, data, w, batch, stride, scale, stream);
+}
+
+}  // namespace fsim
+
+extern "C" int fsim_vec_fft2d(fsim_vec* v, int inverse) {
+  int rc = fsim::ensure_init();
+  if (rc) return rc;
+  FSIM_REQUIRE(v && v->d && v->cplx, FSIM_EINVAL, "fft2d: complex vector required");
+  return fsim::fft2d_device(reinterpret_cast<float2*>(v->d), v->w, v->h, inverse != 0, fsim::ctx().stream, 1);
+}

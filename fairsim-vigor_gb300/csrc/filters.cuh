@@ -1,0 +1,33 @@
+// Internal interface of the filter builders (filters.cu).
+#pragma once
+
+#include "common.cuh"
+#include "otf.cuh"
+
+namespace fsim {
+
+struct ShiftSet {  // per-direction band-1 shifts
+  int n_dirs, n_bands;
+  double px[FSIM_MAX_DIRS], py[FSIM_MAX_DIRS];
+};
+ShiftSet shift_set(const fsim_sim_param* p);
+
+constexpr int SEP_MAX_OUT = 2 * FSIM_MAX_BANDS - 1;
+struct SepArgs {
+  int n_in, n_out;
+  const float2* in[FSIM_MAX_PHASES];
+  float2* out[SEP_MAX_OUT];
+  float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
+};
+
+// Stream-ordered upload of a SimParam's OTF table into the shared staging buffer.
+int upload_otf_table(const fsim_sim_param* p, OtfTable** dev, cudaStream_t st);
+int wiener_denominator_device(float* out, const fsim_sim_param* p, double wiener, const OtfTable* t, bool reciprocal,
+                              cudaStream_t st);
+int apo_device(float* out, int cplx, int W, int H, double vec_cpm, double cutoff_abs, double bend, cudaStream_t st);
+int att_device(float* out, int w, int h, double vec_cpm, double str, double fwhm, double kx, double ky, cudaStream_t st);
+int otf_vector_device(float2* v, int w, int h, const OtfTable* t, double kx, double ky, bool att, bool write,
+                      cudaStream_t st);
+int separate_device(const SepArgs& a, size_t n, cudaStream_t st);
+
+}  // namespace fsim

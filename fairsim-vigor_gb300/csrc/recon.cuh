@@ -1,0 +1,64 @@
+// Internal interface of the fused reconstruction (recon.cu, live.cu, plan.cu).
+#pragma once
+
+#include "common.cuh"
+#include "otf.cuh"
+
+namespace fsim {
+
+// One dataset in a batched launch (device-resident table, read by every pass).
+struct JobDesc {
+  const void* raw;    // nA*nP frames of N*N (f32 or u16)
+  float* out;         // W*W reconstruction
+  float* widefield;   // N*N (live path), nullable
+  int input_u16, nA, nP, nC, nWin;
+  float bgr;
+  const float* damp;    // N*N border fade, nullable
+  const float2* coef;   // [a][c][p] separation coefficients
+  const float2* ramps;  // [a][c] {x ramp[W], y ramp[W]}  (offline) / {x ramp[N], y ramp[N]} (live)
+  const int* win;       // [a][c] {Xs, Ys} window origins (offline) / {xInt, yInt} paste offsets (live)
+  const float* masks;   // [a][c] OTF masks (offline) / N*N conj-OTF vector (live)
+  const float* wa;      // Wiener x apodization, quad layout [X/4][Y][X%4]
+  float2* I;            // workspace: intermediate after the row pass
+  float2* O;            // workspace: W*W after the column pass
+};
+
+struct Plan {
+  fsim_sim_param prm{};
+  int path = FSIM_PATH_OFFLINE;
+  int input_type = FSIM_INPUT_F32;
+  int fade_px = 0;
+  double bgr = 0;
+  int nwin = 0;
+  void* dev = nullptr;
+  size_t dev_bytes = 0;
+  size_t filter_bytes = 0;
+  float2* d_coef = nullptr;
+  float2* d_ramps = nullptr;
+  int* d_win = nullptr;
+  OtfTable* d_otf = nullptr;
+  float* d_damp = nullptr;
+  float* d_masks = nullptr;
+  float* d_wa = nullptr;
+  // host-call convenience buffers (fsim_recon_host)
+  void* h_ws = nullptr;
+  size_t h_ws_bytes = 0;
+  void* h_io = nullptr;
+  size_t h_io_bytes = 0;
+  JobDesc* h_job = nullptr;
+  JobDesc* d_job = nullptr;
+
+  int build(cudaStream_t st);       // offline tables
+  int build_live(cudaStream_t st);  // live tables
+  size_t workspace_bytes() const;
+  size_t workspace_bytes_live() const;
+  void fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws) const;
+  void fill_job_live(JobDesc& j, const void* raw, float* out, float* wf, char* ws) const;
+};
+
+bool offline_size_supported(int n);
+bool live_size_supported(int n);
+int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);
+int launch_live_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);
+
+}  // namespace fsim

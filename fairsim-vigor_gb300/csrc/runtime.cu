@@ -1,0 +1,127 @@
+// Library runtime: error state, device/stream context, FFT twiddle tables.
+#include <cmath>
+#include <cstdarg>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "fft_line.cuh"
+#include "runtime.cuh"
+
+namespace fsim {
+
+static thread_local char g_errbuf[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_errbuf, sizeof(g_errbuf), fmt, ap);
+  va_end(ap);
+}
+const char* last_error() { return g_errbuf; }
+
+static std::mutex g_mu;
+static Ctx g_ctx;
+
+Ctx& ctx() { return g_ctx; }
+
+void fill_twiddle_host(float2* h) {
+  auto fill = [&](int L) {
+    int off = tw_offset(L);
+    for (int m = 0; m < L; m++) {
+      double a = -2.0 * M_PI * (double)m / (double)L;
+      h[off + m] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+  };
+  for (int L = 16; L <= 8192; L *= 2) fill(L);
+  for (int L = 48; L <= 6144; L *= 2) fill(L);
+}
+
+static std::vector<tw_upload_fn>& uploaders() {
+  static std::vector<tw_upload_fn> v;
+  return v;
+}
+int register_twiddle_uploader(tw_upload_fn f) {
+  uploaders().push_back(f);
+  return (int)uploaders().size();
+}
+static int upload_all_twiddles() {
+  for (auto f : uploaders())
+    if (f() != 0) {
+      set_error("uploading FFT twiddle tables failed");
+      return FSIM_ECUDA;
+    }
+  return FSIM_OK;
+}
+
+int ensure_init() {
+  std::lock_guard<std::mutex> g(g_mu);
+  if (g_ctx.ready) return FSIM_OK;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    set_error("no CUDA device: %s", cudaGetErrorString(e));
+    return FSIM_ENODEV;
+  }
+  if (g_ctx.device < 0) g_ctx.device = 0;
+  FSIM_CUDA(cudaSetDevice(g_ctx.device));
+  int rc = upload_all_twiddles();
+  if (rc) return rc;
+  if (!g_ctx.stream) {
+    FSIM_CUDA(cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking));
+    g_ctx.own_stream = true;
+  }
+  FSIM_CUDA(cudaMalloc(&g_ctx.red, sizeof(double) * RED_SLOTS));
+  FSIM_CUDA(cudaMallocHost(&g_ctx.red_host, sizeof(double) * RED_SLOTS));
+  cudaDeviceProp prop;
+  FSIM_CUDA(cudaGetDeviceProperties(&prop, g_ctx.device));
+  g_ctx.num_sms = prop.multiProcessorCount;
+  g_ctx.ready = true;
+  return FSIM_OK;
+}
+
+int select_device(int device) {
+  std::lock_guard<std::mutex> g(g_mu);
+  if (g_ctx.ready && g_ctx.device != device) {
+    set_error("fsim_init: library already initialised on device %d", g_ctx.device);
+    return FSIM_EINVAL;
+  }
+  g_ctx.device = device;
+  return FSIM_OK;
+}
+
+}  // namespace fsim
+
+extern "C" {
+
+const char* fsim_last_error(void) { return fsim::last_error(); }
+
+int fsim_init(int device) {
+  int rc = fsim::select_device(device);
+  if (rc) return rc;
+  return fsim::ensure_init();
+}
+
+int fsim_sync(void) {
+  int rc = fsim::ensure_init();
+  if (rc) return rc;
+  FSIM_CUDA(cudaDeviceSynchronize());
+  return FSIM_OK;
+}
+
+int fsim_version(void) { return 10000; }
+
+int fsim_set_stream(void* stream) {
+  int rc = fsim::ensure_init();
+  if (rc) return rc;
+  fsim::Ctx& c = fsim::ctx();
+  if (stream) {
+    c.stream = (cudaStream_t)stream;
+  } else {
+    FSIM_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    c.own_stream = true;
+  }
+  return FSIM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,451 @@
+// Served form: the GB300 counterpart of ReconstructionRunner
+// (LM/ReconstructionRunner.java:140-593, 599-748, 753-829).
+//
+// * Admission: a stack is admitted into one of a fixed set of slots (pinned host staging
+//   + device raw/output buffers). The slot count is bounded by max_inflight and by the
+//   HBM budget; a full server returns FSIM_EBUSY instead of dropping frames silently
+//   (the reference counts misses when its queue is full, :140-150).
+// * Continuous batching: a worker thread takes every pending stack (up to max_batch) and
+//   launches one fused batch (H2D, reconstruction, D2H) on the next of `streams` CUDA
+//   streams; stacks arriving while batches run are taken by the next launch, so batches
+//   overlap on the device. Completion is signalled by a host callback on the stream.
+// * Refit: every refit_every stacks of a channel, ParameterRefitThread.doRefit runs on the
+//   device (estimate_core, live mode) on a side stream and thread, then the channel's
+//   inactive plan is rebuilt and swapped in (double-buffered filters, so batches in
+//   flight keep reading the tables they were launched with).
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+#include "estimate.cuh"
+#include "recon.cuh"
+#include "runtime.cuh"
+#include "sim_host.h"
+
+namespace fsim {
+int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStream_t st, JobDesc* host_table,
+                bool upload_table);
+size_t plan_ws(const Plan* p);
+}  // namespace fsim
+
+using namespace fsim;
+using clk = std::chrono::steady_clock;
+
+static double now_ms() {
+  return std::chrono::duration<double, std::milli>(clk::now().time_since_epoch()).count();
+}
+
+struct fsim_server {
+  struct Channel {
+    fsim_sim_param prm{};
+    Plan* plans[2] = {nullptr, nullptr};
+    int active = 0;
+    cudaEvent_t last_use[2] = {nullptr, nullptr};
+    uint64_t count = 0;
+    bool refit_busy = false;
+    void* d_refit_raw = nullptr;
+    size_t raw_bytes = 0;
+  };
+  enum { FREE = 0, FILLING, PENDING, RUNNING, DONE };
+  struct Slot {
+    void* h_raw = nullptr;
+    void* d_raw = nullptr;
+    float* h_out = nullptr;
+    float* d_out = nullptr;
+    int state = FREE;
+    uint64_t ticket = 0;
+    int channel = 0;
+    double t_submit = 0, t_done = 0;
+  };
+  struct Done {
+    fsim_server* s;
+    std::vector<int> slots;
+  };
+
+  fsim_serve_config cfg{};
+  std::vector<Channel> ch;
+  std::vector<Slot> slots;
+  std::vector<int> free_list;
+  std::deque<int> pending;
+  std::map<uint64_t, int> by_ticket;
+  uint64_t next_ticket = 1;
+  std::vector<cudaStream_t> streams;
+  std::vector<void*> ws;
+  std::vector<JobDesc*> tables;
+  std::vector<cudaEvent_t> table_ev;
+  size_t ws_bytes = 0;
+  int rr = 0;
+  cudaStream_t refit_stream = nullptr;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done, cv_refit;
+  std::thread worker, refitter;
+  std::deque<int> refit_queue;
+  bool stop = false;
+  // stats
+  std::vector<double> lat;
+  uint64_t submitted = 0, completed = 0, rejected = 0, refits = 0;
+  double t_first = 0, t_last = 0;
+};
+
+static void CUDART_CB on_batch_done(void* arg) {
+  auto* d = static_cast<fsim_server::Done*>(arg);
+  fsim_server* s = d->s;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    double t = now_ms();
+    for (int i : d->slots) {
+      auto& sl = s->slots[i];
+      sl.state = fsim_server::DONE;
+      sl.t_done = t;
+      s->lat.push_back(t - sl.t_submit);
+      s->completed++;
+      s->t_last = t;
+    }
+  }
+  s->cv_done.notify_all();
+  delete d;
+}
+
+static void worker_loop(fsim_server* s) {
+  cudaSetDevice(ctx().device);
+  for (;;) {
+    std::vector<int> batch;
+    int si;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty(); });
+      if (s->stop && s->pending.empty()) return;
+      while (!s->pending.empty() && (int)batch.size() < s->cfg.max_batch) {
+        int i = s->pending.front();
+        s->pending.pop_front();
+        s->slots[i].state = fsim_server::RUNNING;
+        batch.push_back(i);
+      }
+      si = s->rr;
+      s->rr = (s->rr + 1) % (int)s->streams.size();
+    }
+    cudaStream_t st = s->streams[si];
+    // the job table of this stream is rewritten only after its previous upload ran
+    cudaEventSynchronize(s->table_ev[si]);
+    std::vector<fsim_job> jobs(batch.size());
+    std::vector<int> used_plan(batch.size());
+    std::vector<int> refit_now;
+    {
+      std::lock_guard<std::mutex> g(s->mu);
+      for (size_t k = 0; k < batch.size(); k++) {
+        auto& sl = s->slots[batch[k]];
+        auto& c = s->ch[sl.channel];
+        used_plan[k] = c.active;
+        jobs[k] = fsim_job{reinterpret_cast<const fsim_plan*>(c.plans[c.active]), sl.d_raw, sl.d_out, nullptr};
+        c.count++;
+        if (s->cfg.refit_every > 0 && c.count % s->cfg.refit_every == 0 && !c.refit_busy) {
+          c.refit_busy = true;
+          refit_now.push_back(batch[k]);
+        }
+      }
+    }
+    for (int i : batch) {
+      auto& sl = s->slots[i];
+      cudaMemcpyAsync(sl.d_raw, sl.h_raw, s->ch[sl.channel].raw_bytes, cudaMemcpyHostToDevice, st);
+    }
+    int rc = recon_batch(jobs.data(), (int)jobs.size(), s->ws[si], s->ws_bytes, st, s->tables[si], true);
+    cudaEventRecord(s->table_ev[si], st);
+    for (size_t k = 0; k < batch.size(); k++) {
+      auto& sl = s->slots[batch[k]];
+      auto& c = s->ch[sl.channel];
+      const size_t W = 2 * (size_t)c.prm.w;
+      cudaMemcpyAsync(sl.h_out, sl.d_out, W * W * sizeof(float), cudaMemcpyDeviceToHost, st);
+      cudaEventRecord(c.last_use[used_plan[k]], st);
+    }
+    // the newest stack of a channel due for a refit is copied for the refit thread
+    for (int i : refit_now) {
+      auto& sl = s->slots[i];
+      auto& c = s->ch[sl.channel];
+      cudaMemcpyAsync(c.d_refit_raw, sl.d_raw, c.raw_bytes, cudaMemcpyDeviceToDevice, st);
+    }
+    if (!refit_now.empty()) {
+      cudaStreamSynchronize(st);
+      std::lock_guard<std::mutex> g(s->mu);
+      for (int i : refit_now) s->refit_queue.push_back(s->slots[i].channel);
+      s->cv_refit.notify_all();
+    }
+    if (rc != FSIM_OK) {
+      std::lock_guard<std::mutex> g(s->mu);
+      for (int i : batch) s->slots[i].state = fsim_server::DONE;  // waiter sees the error
+      s->cv_done.notify_all();
+      continue;
+    }
+    auto* d = new fsim_server::Done{s, batch};
+    cudaLaunchHostFunc(st, on_batch_done, d);
+  }
+}
+
+static void refit_loop(fsim_server* s) {
+  cudaSetDevice(ctx().device);
+  for (;;) {
+    int c;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv_refit.wait(lk, [&] { return s->stop || !s->refit_queue.empty(); });
+      if (s->stop) return;
+      c = s->refit_queue.front();
+      s->refit_queue.pop_front();
+    }
+    auto& chn = s->ch[c];
+    fsim_sim_param p = chn.prm;
+    const int N = p.w, frames = p.nr_dirs * p.nr_phases;
+    const size_t n = (size_t)N * N;
+    cudaStream_t st = s->refit_stream;
+    int rc = FSIM_OK;
+    // ParameterRefitThread.doRefit on the device: damp, FFT, estimate (live mode)
+    float2* spec = nullptr;
+    if (cudaMallocAsync(&spec, sizeof(float2) * n * frames, st) != cudaSuccess) rc = FSIM_EOOM;
+    if (!rc) {
+      extern int refit_spectra(const fsim_sim_param* p, const void* raw, int input_u16, int fade, float2* spec,
+                               cudaStream_t st);
+      rc = refit_spectra(&p, chn.d_refit_raw, s->cfg.input_type == FSIM_INPUT_U16, s->cfg.fade_px, spec, st);
+    }
+    if (!rc) {
+      std::vector<const float2*> ptrs(frames);
+      for (int i = 0; i < frames; i++) ptrs[i] = spec + i * n;
+      rc = estimate_core(&p, ptrs.data(), 1, .8, true, nullptr, st);
+    }
+    if (spec) cudaFreeAsync(spec, st);
+    if (!rc) {
+      const int spare = 1 - chn.active;
+      cudaEventSynchronize(chn.last_use[spare]);  // no batch in flight reads the spare tables
+      chn.plans[spare]->prm = p;
+      rc = chn.plans[spare]->build_live(st);
+      if (!rc) {
+        std::lock_guard<std::mutex> g(s->mu);
+        chn.prm = p;
+        chn.active = spare;
+        s->refits++;
+      }
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    chn.refit_busy = false;
+  }
+}
+
+// damp + forward FFT of a raw stack on the device (shared with the estimation entry points)
+namespace fsim {
+std::vector<float> fade_vector(int w, int h, int px);
+int fft2d_device(float2* data, int w, int h, bool inverse, cudaStream_t stream, int batch);
+int raw_to_cplx_device(float2* y, const void* raw, int input_u16, const float* damp, size_t n, size_t frames,
+                       cudaStream_t st);
+}  // namespace fsim
+int refit_spectra(const fsim_sim_param* p, const void* raw, int input_u16, int fade, float2* spec, cudaStream_t st) {
+  const int N = p->w, frames = p->nr_dirs * p->nr_phases;
+  const size_t n = (size_t)N * N;
+  float* damp = nullptr;
+  if (fade > 0) {
+    std::vector<float> h = fade_vector(N, N, fade);
+    FSIM_CUDA(cudaMallocAsync(&damp, sizeof(float) * n, st));
+    FSIM_CUDA(cudaMemcpyAsync(damp, h.data(), sizeof(float) * n, cudaMemcpyHostToDevice, st));
+    FSIM_CUDA(cudaStreamSynchronize(st));
+  }
+  int rc = raw_to_cplx_device(spec, raw, input_u16, damp, n, frames, st);
+  if (!rc) rc = fft2d_device(spec, N, N, false, st, frames);
+  if (damp) cudaFreeAsync(damp, st);
+  return rc;
+}
+
+extern "C" {
+
+int fsim_serve_open(fsim_server** out, const fsim_serve_config* cfg, const fsim_sim_param* channels, int n_channels) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  FSIM_REQUIRE(out && cfg && channels && n_channels > 0, FSIM_EINVAL, "serve_open: bad arguments");
+  FSIM_REQUIRE(cfg->max_batch > 0 && cfg->max_inflight > 0 && cfg->streams > 0, FSIM_EINVAL,
+               "serve_open: max_batch, max_inflight and streams must be positive");
+  auto* s = new fsim_server();
+  s->cfg = *cfg;
+  s->ch.resize(n_channels);
+  size_t max_raw = 0, max_out = 0, max_ws = 0;
+  const int in_sz = cfg->input_type == FSIM_INPUT_U16 ? 2 : 4;
+  for (int c = 0; c < n_channels; c++) {
+    auto& chn = s->ch[c];
+    chn.prm = channels[c];
+    for (int k = 0; k < 2; k++) {
+      fsim_plan* pl = nullptr;
+      rc = fsim_plan_create(&pl, &channels[c], FSIM_PATH_LIVE, cfg->input_type, cfg->fade_px, 0.0);
+      if (rc) {
+        fsim_serve_close(s);
+        return rc;
+      }
+      chn.plans[k] = reinterpret_cast<Plan*>(pl);
+      cudaEventCreateWithFlags(&chn.last_use[k], cudaEventDisableTiming);
+    }
+    const size_t N = channels[c].w;
+    chn.raw_bytes = N * N * channels[c].nr_dirs * channels[c].nr_phases * in_sz;
+    FSIM_CUDA(cudaMalloc(&chn.d_refit_raw, chn.raw_bytes));
+    max_raw = std::max(max_raw, chn.raw_bytes);
+    max_out = std::max(max_out, 4 * N * N * sizeof(float));
+    max_ws = std::max(max_ws, (plan_ws(chn.plans[0]) + 255) & ~(size_t)255);
+  }
+  s->ws_bytes = ((sizeof(JobDesc) * cfg->max_batch + 255) & ~(size_t)255) + max_ws * cfg->max_batch;
+  // admission bound: slots fit the HBM budget after the per-stream workspaces
+  size_t per_slot = max_raw + max_out;
+  size_t ws_total = s->ws_bytes * cfg->streams;
+  int nslots = cfg->max_inflight;
+  if (cfg->hbm_budget_bytes > 0) {
+    FSIM_REQUIRE(cfg->hbm_budget_bytes > ws_total + per_slot, FSIM_EOOM,
+                 "serve_open: HBM budget %zu below workspace %zu + one slot %zu", cfg->hbm_budget_bytes, ws_total,
+                 per_slot);
+    nslots = std::min<size_t>(nslots, (cfg->hbm_budget_bytes - ws_total) / per_slot);
+  }
+  s->slots.resize(nslots);
+  for (int i = 0; i < nslots; i++) {
+    auto& sl = s->slots[i];
+    FSIM_CUDA(cudaMallocHost(&sl.h_raw, max_raw));
+    FSIM_CUDA(cudaMallocHost(&sl.h_out, max_out));
+    FSIM_CUDA(cudaMalloc(&sl.d_raw, max_raw));
+    FSIM_CUDA(cudaMalloc(&sl.d_out, max_out));
+    s->free_list.push_back(nslots - 1 - i);
+  }
+  s->streams.resize(cfg->streams);
+  s->ws.resize(cfg->streams);
+  s->tables.resize(cfg->streams);
+  s->table_ev.resize(cfg->streams);
+  for (int k = 0; k < cfg->streams; k++) {
+    FSIM_CUDA(cudaStreamCreateWithFlags(&s->streams[k], cudaStreamNonBlocking));
+    FSIM_CUDA(cudaMalloc(&s->ws[k], s->ws_bytes));
+    FSIM_CUDA(cudaMallocHost(&s->tables[k], sizeof(JobDesc) * cfg->max_batch));
+    FSIM_CUDA(cudaEventCreateWithFlags(&s->table_ev[k], cudaEventDisableTiming));
+  }
+  FSIM_CUDA(cudaStreamCreateWithFlags(&s->refit_stream, cudaStreamNonBlocking));
+  FSIM_CUDA(cudaDeviceSynchronize());
+  s->worker = std::thread(worker_loop, s);
+  s->refitter = std::thread(refit_loop, s);
+  *out = s;
+  return FSIM_OK;
+}
+
+int fsim_serve_submit(fsim_server* s, int channel, const void* raw_host, uint64_t* ticket) {
+  FSIM_REQUIRE(s && raw_host && ticket, FSIM_EINVAL, "serve_submit: bad arguments");
+  FSIM_REQUIRE(channel >= 0 && channel < (int)s->ch.size(), FSIM_EINVAL, "serve_submit: no channel %d", channel);
+  int i;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->free_list.empty()) {
+      s->rejected++;
+      set_error("serve_submit: no free slot (%zu in flight)", s->slots.size());
+      return FSIM_EBUSY;
+    }
+    i = s->free_list.back();
+    s->free_list.pop_back();
+    auto& sl = s->slots[i];
+    sl.state = fsim_server::FILLING;
+    sl.channel = channel;
+    sl.ticket = s->next_ticket++;
+    sl.t_submit = now_ms();
+    if (s->submitted == 0) s->t_first = sl.t_submit;
+    s->submitted++;
+    s->by_ticket[sl.ticket] = i;
+    *ticket = sl.ticket;
+  }
+  std::memcpy(s->slots[i].h_raw, raw_host, s->ch[channel].raw_bytes);
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->slots[i].state = fsim_server::PENDING;
+    s->pending.push_back(i);
+  }
+  s->cv_work.notify_one();
+  return FSIM_OK;
+}
+
+int fsim_serve_wait(fsim_server* s, uint64_t ticket, float* out_host, int timeout_ms, double* latency_ms) {
+  FSIM_REQUIRE(s && out_host, FSIM_EINVAL, "serve_wait: bad arguments");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->by_ticket.find(ticket);
+  FSIM_REQUIRE(it != s->by_ticket.end(), FSIM_ENOTFOUND, "serve_wait: unknown ticket %llu", (unsigned long long)ticket);
+  const int i = it->second;
+  auto& sl = s->slots[i];
+  if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return sl.state == fsim_server::DONE; })) {
+    set_error("serve_wait: ticket %llu not done after %d ms", (unsigned long long)ticket, timeout_ms);
+    return FSIM_ETIMEOUT;
+  }
+  const size_t W = 2 * (size_t)s->ch[sl.channel].prm.w;
+  std::memcpy(out_host, sl.h_out, W * W * sizeof(float));
+  if (latency_ms) *latency_ms = sl.t_done - sl.t_submit;
+  sl.state = fsim_server::FREE;
+  s->by_ticket.erase(it);
+  s->free_list.push_back(i);
+  return FSIM_OK;
+}
+
+int fsim_serve_stats_get(fsim_server* s, fsim_serve_stats* out) {
+  FSIM_REQUIRE(s && out, FSIM_EINVAL, "serve_stats: bad arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  std::memset(out, 0, sizeof(*out));
+  out->submitted = s->submitted;
+  out->completed = s->completed;
+  out->rejected = s->rejected;
+  out->refits = s->refits;
+  if (!s->lat.empty()) {
+    std::vector<double> v = s->lat;
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double q) { return v[std::min(v.size() - 1, (size_t)(q * (v.size() - 1) + 0.5))]; };
+    out->p50_ms = pct(0.50);
+    out->p99_ms = pct(0.99);
+    double sum = 0;
+    for (double x : v) sum += x;
+    out->mean_ms = sum / v.size();
+    out->max_ms = v.back();
+  }
+  out->wall_s = (s->t_last - s->t_first) / 1000.0;
+  out->recon_per_s = out->wall_s > 0 ? s->completed / out->wall_s : 0;
+  return FSIM_OK;
+}
+
+int fsim_serve_params(fsim_server* s, int channel, fsim_sim_param* out) {
+  FSIM_REQUIRE(s && out && channel >= 0 && channel < (int)s->ch.size(), FSIM_EINVAL, "serve_params: bad arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  *out = s->ch[channel].prm;
+  return FSIM_OK;
+}
+
+int fsim_serve_close(fsim_server* s) {
+  if (!s) return FSIM_OK;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  s->cv_refit.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  if (s->refitter.joinable()) s->refitter.join();
+  cudaDeviceSynchronize();
+  for (auto& sl : s->slots) {
+    if (sl.h_raw) cudaFreeHost(sl.h_raw);
+    if (sl.h_out) cudaFreeHost(sl.h_out);
+    if (sl.d_raw) cudaFree(sl.d_raw);
+    if (sl.d_out) cudaFree(sl.d_out);
+  }
+  for (size_t k = 0; k < s->streams.size(); k++) {
+    if (s->ws[k]) cudaFree(s->ws[k]);
+    if (s->tables[k]) cudaFreeHost(s->tables[k]);
+    if (s->table_ev[k]) cudaEventDestroy(s->table_ev[k]);
+    if (s->streams[k]) cudaStreamDestroy(s->streams[k]);
+  }
+  for (auto& c : s->ch) {
+    for (int k = 0; k < 2; k++) {
+      if (c.plans[k]) fsim_plan_destroy(reinterpret_cast<fsim_plan*>(c.plans[k]));
+      if (c.last_use[k]) cudaEventDestroy(c.last_use[k]);
+    }
+    if (c.d_refit_raw) cudaFree(c.d_refit_raw);
+  }
+  if (s->refit_stream) cudaStreamDestroy(s->refit_stream);
+  delete s;
+  return FSIM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,205 @@
+"""ctypes binding of ``lib/libfairsim_gb300.so`` (the C ABI declared in include/fairsim_gb300.h).
+
+The library is the product: every call here runs native code. There is no Python or CPU
+fallback; a missing library or a failing CUDA call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libfairsim_gb300.so")
+HEADER = os.path.join(_HERE, "..", "include", "fairsim_gb300.h")
+
+FSIM_OK, FSIM_EINVAL, FSIM_EOOM, FSIM_ECUDA, FSIM_ETIMEOUT, FSIM_EBUSY, FSIM_ENOTFOUND, FSIM_ENODEV = 0, -1, -2, -3, -4, -5, -6, -7
+PATH_OFFLINE, PATH_LIVE = 0, 1
+INPUT_F32, INPUT_U16 = 0, 1
+MAXD, MAXB, MAXP = 8, 4, 16
+
+
+class FsimError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("fsim error %d: %s" % (code, msg))
+        self.code = code
+
+
+class SimParamC(C.Structure):
+    _fields_ = [
+        ("w", C.c_int32),
+        ("nr_dirs", C.c_int32),
+        ("nr_bands", C.c_int32),
+        ("nr_phases", C.c_int32),
+        ("microns_per_pixel", C.c_double),
+        ("na", C.c_double),
+        ("em_wavelength", C.c_double),
+        ("otf_a", C.c_double),
+        ("use_attenuation", C.c_int32),
+        ("att_strength", C.c_double),
+        ("att_fwhm", C.c_double),
+        ("wiener", C.c_double),
+        ("apo_cutoff", C.c_double),
+        ("apo_bend", C.c_double),
+        ("px", C.c_double * MAXD),
+        ("py", C.c_double * MAXD),
+        ("pha_off", C.c_double * MAXD),
+        ("modulation", (C.c_double * MAXB) * MAXD),
+        ("has_phases", C.c_int32),
+        ("phases", (C.c_double * MAXP) * MAXD),
+    ]
+
+
+class Job(C.Structure):
+    _fields_ = [("plan", C.c_void_p), ("raw", C.c_void_p), ("out", C.c_void_p), ("widefield", C.c_void_p)]
+
+
+class ServeConfig(C.Structure):
+    _fields_ = [
+        ("max_batch", C.c_int32),
+        ("max_inflight", C.c_int32),
+        ("streams", C.c_int32),
+        ("refit_every", C.c_int32),
+        ("input_type", C.c_int32),
+        ("fade_px", C.c_int32),
+        ("hbm_budget_bytes", C.c_size_t),
+    ]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_uint64),
+        ("completed", C.c_uint64),
+        ("rejected", C.c_uint64),
+        ("refits", C.c_uint64),
+        ("p50_ms", C.c_double),
+        ("p99_ms", C.c_double),
+        ("mean_ms", C.c_double),
+        ("max_ms", C.c_double),
+        ("recon_per_s", C.c_double),
+        ("wall_s", C.c_double),
+    ]
+
+
+def to_c_param(p) -> SimParamC:
+    """SimParam mirror (or dict) -> the C record."""
+    g = (lambda k: p[k]) if isinstance(p, dict) else (lambda k: getattr(p, k))
+    c = SimParamC()
+    c.w = g("w")
+    c.nr_dirs, c.nr_bands, c.nr_phases = g("nrDirs"), g("nrBands"), g("nrPhases")
+    c.microns_per_pixel = g("micronsPerPixel")
+    c.na, c.em_wavelength, c.otf_a = g("na"), g("emWavelength"), g("otfA")
+    c.use_attenuation = int(g("useAttenuation"))
+    c.att_strength, c.att_fwhm = g("attStrength"), g("attFWHM")
+    c.wiener, c.apo_cutoff, c.apo_bend = g("wiener"), g("apoCutoff"), g("apoBend")
+    for d in range(c.nr_dirs):
+        c.px[d], c.py[d], c.pha_off[d] = g("pX")[d], g("pY")[d], g("phaOff")[d]
+        for b in range(c.nr_bands):
+            c.modulation[d][b] = g("modulations")[d][b]
+    ph = g("phases")
+    if ph is not None:
+        c.has_phases = 1
+        for d in range(c.nr_dirs):
+            for i in range(c.nr_phases):
+                c.phases[d][i] = ph[d][i]
+    return c
+
+
+def from_c_param(c: SimParamC) -> dict:
+    n = c.nr_dirs
+    return dict(pX=[c.px[d] for d in range(n)], pY=[c.py[d] for d in range(n)],
+                phaOff=[c.pha_off[d] for d in range(n)],
+                modulations=[[c.modulation[d][b] for b in range(c.nr_bands)] for d in range(n)])
+
+
+_lib = None
+VP, I32, F32, F64, PTR = C.c_void_p, C.c_int, C.c_float, C.c_double, C.c_void_p
+_SIGS = {
+    "fsim_last_error": (C.c_char_p, []),
+    "fsim_init": (I32, [I32]),
+    "fsim_sync": (I32, []),
+    "fsim_version": (I32, []),
+    "fsim_set_stream": (I32, [VP]),
+    "fsim_vec_create": (I32, [C.POINTER(VP), I32, I32, I32]),
+    "fsim_vec_destroy": (I32, [VP]),
+    "fsim_vec_info": (I32, [VP, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32), C.POINTER(VP)]),
+    "fsim_vec_upload": (I32, [VP, VP]),
+    "fsim_vec_download": (I32, [VP, VP]),
+    "fsim_vec_upload_u16": (I32, [VP, VP]),
+    "fsim_vec_zero": (I32, [VP]),
+    "fsim_vec_add": (I32, [VP, VP]),
+    "fsim_vec_addconst": (I32, [VP, F32, F32]),
+    "fsim_vec_axpy": (I32, [VP, F32, F32, VP]),
+    "fsim_vec_times": (I32, [VP, VP, I32]),
+    "fsim_vec_scal": (I32, [VP, F32, F32]),
+    "fsim_vec_copy": (I32, [VP, VP]),
+    "fsim_vec_reciproc": (I32, [VP]),
+    "fsim_vec_norm2": (I32, [VP, C.POINTER(F64)]),
+    "fsim_vec_sum": (I32, [VP, C.POINTER(F64), C.POINTER(F64)]),
+    "fsim_vec_dot": (I32, [VP, VP, C.POINTER(F64), C.POINTER(F64)]),
+    "fsim_vec_fft2d": (I32, [VP, I32]),
+    "fsim_vec_fourier_shift": (I32, [VP, F64, F64]),
+    "fsim_vec_paste_freq": (I32, [VP, VP, I32, I32]),
+    "fsim_otf_to_vector": (I32, [VP, VP, I32, F64, F64, I32, I32]),
+    "fsim_apo_vector": (I32, [VP, VP, F64, F64]),
+    "fsim_attenuation_vector": (I32, [VP, VP, F64, F64, F64, F64]),
+    "fsim_mask_otf": (I32, [VP, VP, F64, F64]),
+    "fsim_wiener_denominator": (I32, [VP, VP, F64]),
+    "fsim_separate_bands": (I32, [VP, I32, VP, I32, VP, I32, VP]),
+    "fsim_common_region": (I32, [VP, VP, VP, F64, F64, F64, F64, I32]),
+    "fsim_locate_peak": (I32, [VP, F64, VP]),
+    "fsim_fit_peak": (I32, [VP, VP, VP, F64, F64, F64, F64, VP, VP]),
+    "fsim_get_peak": (I32, [VP, VP, VP, F64, F64, F64, VP]),
+    "fsim_run_reconstruction": (I32, [VP, VP, VP, I32, I32]),
+    "fsim_estimate_parameters": (I32, [VP, VP, I32, F64, VP]),
+    "fsim_plan_create": (I32, [C.POINTER(VP), VP, I32, I32, I32, F64]),
+    "fsim_plan_update": (I32, [VP, VP]),
+    "fsim_plan_destroy": (I32, [VP]),
+    "fsim_plan_workspace_bytes": (C.c_size_t, [VP]),
+    "fsim_plan_filter_bytes": (C.c_size_t, [VP]),
+    "fsim_plan_info": (I32, [VP, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
+    "fsim_recon_batch": (I32, [VP, I32, VP, C.c_size_t, VP]),
+    "fsim_recon_host": (I32, [VP, VP, VP]),
+    "fsim_estimate_raw": (I32, [VP, VP, I32, I32, I32, F64, VP]),
+    "fsim_live_refit": (I32, [VP, VP, VP]),
+    "fsim_serve_open": (I32, [C.POINTER(VP), VP, VP, I32]),
+    "fsim_serve_submit": (I32, [VP, I32, VP, C.POINTER(C.c_uint64)]),
+    "fsim_serve_wait": (I32, [VP, C.c_uint64, VP, I32, C.POINTER(F64)]),
+    "fsim_serve_stats_get": (I32, [VP, VP]),
+    "fsim_serve_params": (I32, [VP, I32, VP]),
+    "fsim_serve_close": (I32, [VP]),
+}
+
+
+def header_functions():
+    """Names of every function the public header declares."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(fsim_[a-z0-9_]+)\s*\(", txt)))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("native library missing: %s (run __graft_entry__.build())" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != FSIM_OK:
+        msg = lib().fsim_last_error()
+        raise FsimError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def init(device=0):
+    return check(lib().fsim_init(device))

@@ -1,0 +1,151 @@
+"""Fused, batched reconstruction plans (C ABI: fsim_plan_* / fsim_recon_batch) and the
+served form (fsim_serve_*), which replaces ``ReconstructionRunner``
+(org/fairsim/livemode/ReconstructionRunner.java:140-593) with continuous batching.
+
+A plan holds one parameter set's resident filters (separation coefficients, shift ramps,
+OTF masks, Wiener x apodization, border damping). ``PATH_OFFLINE`` reproduces
+``SimAlgorithm.runReconstruction`` with the GUI's input preparation (background clip,
+``fadeBorderCos``, FFT); ``PATH_LIVE`` reproduces the live ``ReconstructionThread``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import native as N
+
+
+class ReconPlan:
+    def __init__(self, sp, path=N.PATH_OFFLINE, input_type=N.INPUT_F32, fade_px=10, bgr=0.0):
+        N.init()
+        self.sp = sp
+        self.path, self.input_type = path, input_type
+        h = C.c_void_p()
+        self._c = N.to_c_param(sp)
+        N.check(N.lib().fsim_plan_create(C.byref(h), C.byref(self._c), int(path), int(input_type), int(fade_px), float(bgr)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def w(self):
+        return self.sp.w
+
+    def update(self, sp):
+        self.sp = sp
+        self._c = N.to_c_param(sp)
+        N.check(N.lib().fsim_plan_update(self._h, C.byref(self._c)))
+
+    def workspace_bytes(self) -> int:
+        return int(N.lib().fsim_plan_workspace_bytes(self._h))
+
+    def filter_bytes(self) -> int:
+        return int(N.lib().fsim_plan_filter_bytes(self._h))
+
+    def raw_dtype(self):
+        return np.uint16 if self.input_type == N.INPUT_U16 else np.float32
+
+    def reconstruct_host(self, raw) -> np.ndarray:
+        """Host buffers in and out: H2D copy, fused reconstruction, D2H copy."""
+        raw = np.ascontiguousarray(raw, dtype=self.raw_dtype())
+        n = self.sp.w
+        if raw.size != self.sp.nrDirs * self.sp.nrPhases * n * n:
+            raise ValueError("raw stack size mismatch")
+        out = np.empty((2 * n, 2 * n), dtype=np.float32)
+        N.check(N.lib().fsim_recon_host(self._h, raw.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().fsim_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_workspace_bytes(plans) -> int:
+    # the library keeps one internal job descriptor (< 256 bytes) per job at the head
+    job_table = (len(plans) * 256 + 255) // 256 * 256
+    return job_table + sum((p.workspace_bytes() + 255) // 256 * 256 for p in plans)
+
+
+def recon_batch(jobs, workspace_ptr: int, workspace_bytes: int, stream_ptr: int = 0):
+    """jobs: iterable of (plan, raw_device_ptr, out_device_ptr[, widefield_device_ptr])."""
+    jobs = list(jobs)
+    arr = (N.Job * len(jobs))()
+    for i, j in enumerate(jobs):
+        arr[i].plan = j[0].handle
+        arr[i].raw = j[1]
+        arr[i].out = j[2]
+        arr[i].widefield = j[3] if len(j) > 3 else None
+    N.check(N.lib().fsim_recon_batch(arr, len(jobs), C.c_void_p(workspace_ptr), C.c_size_t(workspace_bytes),
+                                     C.c_void_p(stream_ptr) if stream_ptr else None))
+
+
+class Server:
+    """Continuous-batching live reconstruction over several channels (fsim_serve_*)."""
+
+    def __init__(self, channel_params, max_batch=16, max_inflight=64, streams=3, refit_every=50,
+                 input_type=N.INPUT_U16, fade_px=10, hbm_budget_bytes=8 << 30):
+        N.init()
+        cfg = N.ServeConfig(max_batch, max_inflight, streams, refit_every, input_type, fade_px, hbm_budget_bytes)
+        self.params = list(channel_params)
+        arr = (N.SimParamC * len(self.params))()
+        for i, p in enumerate(self.params):
+            arr[i] = N.to_c_param(p)
+        h = C.c_void_p()
+        N.check(N.lib().fsim_serve_open(C.byref(h), C.byref(cfg), arr, len(self.params)))
+        self._h = h
+        self.input_type = input_type
+
+    def submit(self, channel: int, raw) -> int:
+        raw = np.ascontiguousarray(raw, dtype=np.uint16 if self.input_type == N.INPUT_U16 else np.float32)
+        t = C.c_uint64()
+        N.check(N.lib().fsim_serve_submit(self._h, int(channel), raw.ctypes.data_as(C.c_void_p), C.byref(t)))
+        return t.value
+
+    def try_submit(self, channel: int, raw):
+        raw = np.ascontiguousarray(raw, dtype=np.uint16 if self.input_type == N.INPUT_U16 else np.float32)
+        t = C.c_uint64()
+        rc = N.lib().fsim_serve_submit(self._h, int(channel), raw.ctypes.data_as(C.c_void_p), C.byref(t))
+        if rc == N.FSIM_EBUSY:
+            return None
+        N.check(rc)
+        return t.value
+
+    def wait(self, ticket: int, out=None, timeout_ms=10000):
+        n = None
+        lat = C.c_double()
+        if out is None:
+            raise ValueError("out buffer required")
+        N.check(N.lib().fsim_serve_wait(self._h, C.c_uint64(ticket), out.ctypes.data_as(C.c_void_p), int(timeout_ms),
+                                        C.byref(lat)))
+        return lat.value
+
+    def stats(self) -> dict:
+        s = N.ServeStats()
+        N.check(N.lib().fsim_serve_stats_get(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in N.ServeStats._fields_}
+
+    def channel_params(self, ch: int) -> dict:
+        c = N.SimParamC()
+        N.check(N.lib().fsim_serve_params(self._h, int(ch), C.byref(c)))
+        return N.from_c_param(c)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.check(N.lib().fsim_serve_close(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

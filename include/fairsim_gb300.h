@@ -1,0 +1,199 @@
+/*
+ * fairsim_gb300.h — C ABI of the GB300-native (sm_103a) fairSIM 2D SIM reconstruction path.
+ *
+ * This is the drop-in boundary. It replaces, one for one, the JNI natives that the
+ * reference's accel backend binds, and it adds the fused entry points the reference
+ * lacks. Reference paths are relative to the fairSIM project root.
+ *
+ *   accel vector natives  org/fairsim/accel/AccelVectorReal.java:218-247,330-333
+ *                         org/fairsim/accel/AccelVectorCplx.java:296-331,483-492
+ *   FFT plan native       org/fairsim/accel/FFTProvider.java:105
+ *   factory natives       org/fairsim/accel/AccelVectorFactory.java:139-146
+ *   SIM algorithm         org/fairsim/sim_algorithm/SimAlgorithm.java:37 (estimateParameters),
+ *                         :268 (runReconstruction); WienerFilter.java:115; OtfProvider.java:331-559
+ *   live serving loop     org/fairsim/livemode/ReconstructionRunner.java:415-593
+ *
+ * Conventions: every function returns an int32 status (FSIM_OK == 0, negative on error;
+ * fsim_last_error() gives a message for the calling thread). Vectors are row-major
+ * (x + w*y); complex vectors are interleaved float32 (re, im), as in
+ * org/fairsim/linalg/Vec2d.java:23-24. Frequency coordinates follow
+ * org/fairsim/sim_algorithm/OtfProvider.java:345-346 (y flipped).
+ * "stream" arguments are cudaStream_t values passed as void* (NULL = the library stream).
+ */
+#ifndef FAIRSIM_GB300_H
+#define FAIRSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the JNI shim maps them to the reference's exception types) ---- */
+#define FSIM_OK 0
+#define FSIM_EINVAL (-1)   /* bad argument: RuntimeException / IndexOutOfBounds in Java */
+#define FSIM_EOOM (-2)     /* allocation failed: OutOfMemoryError (AccelVectorCplx.java:51-54) */
+#define FSIM_ECUDA (-3)    /* CUDA runtime error: cudaRE's RuntimeException (accel/cuda_common.h:33-63) */
+#define FSIM_ETIMEOUT (-4) /* a bounded wait expired */
+#define FSIM_EBUSY (-5)    /* admission refused: no slot / HBM budget, retry later */
+#define FSIM_ENOTFOUND (-6)
+#define FSIM_ENODEV (-7)   /* no CUDA device / library not initialised */
+
+#define FSIM_MAX_DIRS 8
+#define FSIM_MAX_BANDS 4
+#define FSIM_MAX_PHASES 16
+
+/* ---- library ------------------------------------------------------------------- */
+const char* fsim_last_error(void);
+int fsim_init(int device);               /* select device, upload FFT twiddle tables */
+int fsim_sync(void);                     /* AccelVectorFactory.nativeSync (cudaDeviceSynchronize) */
+int fsim_version(void);
+int fsim_set_stream(void* stream);       /* stream used by the vector API (NULL = own stream) */
+
+/* ---- SimParam (+ OtfProvider.fromEstimate) as a flat record ------------------------
+ * org/fairsim/sim_algorithm/SimParam.java:31-615, OtfProvider.java:96-127.
+ * px/py: Dir.pX/pY (band-1 shift; setPxPy divides the highest-band shift by nBands-1),
+ * modulation[d][b]: raw Dir.modul (clamped to [0.3,1.1] where the reference clamps). */
+typedef struct fsim_sim_param {
+  int32_t w; /* raw image width == height */
+  int32_t nr_dirs, nr_bands, nr_phases;
+  double microns_per_pixel;
+  double na, em_wavelength, otf_a;
+  int32_t use_attenuation;
+  double att_strength, att_fwhm;
+  double wiener, apo_cutoff, apo_bend;
+  double px[FSIM_MAX_DIRS], py[FSIM_MAX_DIRS], pha_off[FSIM_MAX_DIRS];
+  double modulation[FSIM_MAX_DIRS][FSIM_MAX_BANDS];
+  int32_t has_phases;
+  double phases[FSIM_MAX_DIRS][FSIM_MAX_PHASES];
+} fsim_sim_param;
+
+/* ---- Vector API: device vectors (AccelVectorReal/Cplx[2d]) ---------------------------- */
+typedef struct fsim_vec fsim_vec;
+/* AccelVector*.alloc / dealloc (AccelVectorCplx.java:305,308; AccelVectorReal.java:226,229) */
+int fsim_vec_create(fsim_vec** out, int w, int h, int is_complex);
+int fsim_vec_destroy(fsim_vec* v);
+int fsim_vec_info(const fsim_vec* v, int* w, int* h, int* is_complex, void** device_ptr);
+/* copyBuffer (AccelVectorCplx.java:311): host <-> device, n floats of the vector */
+int fsim_vec_upload(fsim_vec* v, const float* host);
+int fsim_vec_download(const fsim_vec* v, float* host);
+/* nativeCOPYSHORT (AccelVectorCplx.java:483, AccelVectorReal.java:330): unsigned 16-bit pixels */
+int fsim_vec_upload_u16(fsim_vec* v, const uint16_t* host);
+/* elementwise ops (AccelVectorCplx.java:314-331, AccelVectorReal.java:235-247) */
+int fsim_vec_zero(fsim_vec* y);
+int fsim_vec_add(fsim_vec* y, const fsim_vec* x);
+int fsim_vec_addconst(fsim_vec* y, float re, float im);
+int fsim_vec_axpy(fsim_vec* y, float re, float im, const fsim_vec* x); /* y += a*x */
+int fsim_vec_times(fsim_vec* y, const fsim_vec* x, int conj);         /* y = x .* y (x real or complex) */
+int fsim_vec_scal(fsim_vec* y, float re, float im);
+int fsim_vec_copy(fsim_vec* y, const fsim_vec* x); /* real->cplx (im 0), cplx->real (real part), same */
+int fsim_vec_reciproc(fsim_vec* y);
+int fsim_vec_norm2(const fsim_vec* x, double* out);                     /* nativeREDUCE(sqr=true) */
+int fsim_vec_sum(const fsim_vec* x, double* re, double* im);            /* sumElements */
+int fsim_vec_dot(const fsim_vec* x, const fsim_vec* y, double* re, double* im); /* <conj(x), y> */
+/* nativeFFT (AccelVectorCplx.java:489): 2D C2C in place; inverse scaled 1/(w*h) */
+int fsim_vec_fft2d(fsim_vec* v, int inverse);
+/* nativeFourierShift (AccelVectorCplx.java:490): v *= exp(i 2pi (kx x + ky y)/N), square N */
+int fsim_vec_fourier_shift(fsim_vec* v, double kx, double ky);
+/* nativePasteFreq (AccelVectorCplx.java:491): zero out, place in's spectrum with offset */
+int fsim_vec_paste_freq(fsim_vec* out, const fsim_vec* in, int x_off, int y_off);
+
+/* ---- SIM building blocks on device vectors --------------------------------------- */
+/* OtfProvider.otfToVector (OtfProvider.java:331-373): write != 0 writes OTF, else v *= conj(OTF) */
+int fsim_otf_to_vector(fsim_vec* v, const fsim_sim_param* p, int band, double kx, double ky,
+                       int use_att, int write);
+int fsim_apo_vector(fsim_vec* v, const fsim_sim_param* p, double bend, double cutoff);        /* :437-492 */
+int fsim_attenuation_vector(fsim_vec* v, const fsim_sim_param* p, double str, double fwhm,
+                            double kx, double ky);                                            /* :503-529 */
+int fsim_mask_otf(fsim_vec* v, const fsim_sim_param* p, double kx, double ky);                /* :538-559 */
+/* WienerFilter.getDenominator (WienerFilter.java:88-122): out is real 2w x 2w */
+int fsim_wiener_denominator(fsim_vec* out, const fsim_sim_param* p, double wiener);
+/* BandSeparation.separateBands (BandSeparation.java:131-165), phases of band 1, fac nullable */
+int fsim_separate_bands(fsim_vec* const* in, int n_in, fsim_vec* const* out, int n_out,
+                        const double* phases, int bands, const double* fac);
+/* Correlation (Correlation.java:43-288) */
+int fsim_common_region(fsim_vec* b0, fsim_vec* b1, const fsim_sim_param* p, double kx, double ky,
+                       double dist, double weight_limit, int divide);
+int fsim_locate_peak(const fsim_vec* v, double k_min, double out4[4]);
+int fsim_fit_peak(const fsim_vec* band0, const fsim_vec* band1, const fsim_sim_param* p, double kx,
+                  double ky, double weight_limit, double search, double out4[4], double* grid_out);
+int fsim_get_peak(const fsim_vec* band0, const fsim_vec* band1, const fsim_sim_param* p, double kx,
+                  double ky, double weight_limit, double out2[2]);
+
+/* ---- SimAlgorithm-compatible entries (SimAlgorithm.java:37, :268) -------------------
+ * in_fft: nr_dirs*nr_phases complex w x w spectra (angle-major). The op-by-op variant
+ * chains the vector kernels exactly like the reference's Java on an accel factory
+ * (the "plain GPU form"). */
+int fsim_run_reconstruction(const fsim_sim_param* p, fsim_vec* const* in_fft, fsim_vec* out_real,
+                            int otf_before_shift, int clip_scale);
+int fsim_estimate_parameters(fsim_sim_param* p, fsim_vec* const* in_fft, int fit_band,
+                             double fit_exclude, double* peaks_out /* nr_dirs*4, nullable */);
+
+/* ---- fused batched reconstruction (new; no reference counterpart) --------------------- */
+#define FSIM_PATH_OFFLINE 0 /* runReconstruction: OTF after a 2w-grid shift, apo bend p->apo_bend */
+#define FSIM_PATH_LIVE 1    /* ReconstructionThread: damp, OTF before a w-grid fast shift, apo bend 1 */
+#define FSIM_INPUT_F32 0
+#define FSIM_INPUT_U16 1
+typedef struct fsim_plan fsim_plan;
+/* Builds the resident per-channel filters (OTF masks, Wiener x apodization, damping,
+ * separation coefficients, shift tables) for one parameter set. fade_px: border fade
+ * (SimUtils.fadeBorderCos) applied to raw frames, 0 = off; bgr: background subtracted and
+ * clipped at 0 (SimUtils.subtractBackground) when != 0 (offline path). */
+int fsim_plan_create(fsim_plan** out, const fsim_sim_param* p, int path, int input_type, int fade_px,
+                     double bgr);
+int fsim_plan_update(fsim_plan* plan, const fsim_sim_param* p); /* new shifts/phases/modulation */
+int fsim_plan_destroy(fsim_plan* plan);
+size_t fsim_plan_workspace_bytes(const fsim_plan* plan);      /* per dataset */
+size_t fsim_plan_filter_bytes(const fsim_plan* plan);         /* resident filters */
+int fsim_plan_info(const fsim_plan* plan, int* w, int* path, int* input_type);
+
+typedef struct fsim_job {
+  const fsim_plan* plan;
+  const void* raw;  /* device: nr_dirs*nr_phases frames, w*w each, f32 or u16 (plan input type) */
+  float* out;       /* device: 2w x 2w float32 reconstruction (real part, CLIPSCALE.NONE) */
+  float* widefield; /* device, nullable: w x w mean of the damped raw frames (live path) */
+} fsim_job;
+/* Reconstruct n_jobs datasets (mixed sizes and plans allowed) with one set of launches per
+ * size class. workspace: device memory of at least the sum of fsim_plan_workspace_bytes. */
+int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t workspace_bytes,
+                     void* stream);
+/* Host-buffer convenience: H2D copy of raw, reconstruction, D2H copy of out. */
+int fsim_recon_host(fsim_plan* plan, const void* raw_host, float* out_host);
+/* Parameter fit on device raw frames (fade + FFT + SimAlgorithm.estimateParameters). */
+int fsim_estimate_raw(fsim_sim_param* p, const void* raw_device, int input_type, int fade_px,
+                      int fit_band, double fit_exclude, double* peaks_out);
+/* ParameterRefitThread.doRefit (ReconstructionRunner.java:642-746) on u16 device frames. */
+int fsim_live_refit(fsim_sim_param* p, const uint16_t* raw_device, double* peaks_out);
+
+/* ---- served form: continuous batching over channels (replaces ReconstructionRunner) --- */
+typedef struct fsim_server fsim_server;
+typedef struct fsim_serve_config {
+  int32_t max_batch;        /* stacks per launch */
+  int32_t max_inflight;     /* admitted stacks not yet returned (slots) */
+  int32_t streams;          /* concurrent batch streams */
+  int32_t refit_every;      /* re-fit a channel's parameters every N stacks (0 = never) */
+  int32_t input_type;       /* FSIM_INPUT_U16 or FSIM_INPUT_F32 */
+  int32_t fade_px;
+  size_t hbm_budget_bytes;  /* admission bound on device memory for in-flight stacks */
+} fsim_serve_config;
+typedef struct fsim_serve_stats {
+  uint64_t submitted, completed, rejected, refits;
+  double p50_ms, p99_ms, mean_ms, max_ms;
+  double recon_per_s;
+  double wall_s;
+} fsim_serve_stats;
+int fsim_serve_open(fsim_server** out, const fsim_serve_config* cfg, const fsim_sim_param* channels,
+                    int n_channels);
+/* Copies the raw stack (host) into a staging slot; FSIM_EBUSY when no slot is free. */
+int fsim_serve_submit(fsim_server* s, int channel, const void* raw_host, uint64_t* ticket);
+/* Waits up to timeout_ms for the ticket; copies the 2w x 2w result to out_host. */
+int fsim_serve_wait(fsim_server* s, uint64_t ticket, float* out_host, int timeout_ms, double* latency_ms);
+int fsim_serve_stats_get(fsim_server* s, fsim_serve_stats* out);
+int fsim_serve_params(fsim_server* s, int channel, fsim_sim_param* out);
+int fsim_serve_close(fsim_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FAIRSIM_GB300_H */

@@ -1,0 +1,215 @@
+"""GPU parity of the Vector API kernels (the replacements of the reference's JNI vector
+natives, org/fairsim/accel/AccelVectorCplx.java:296-331) and of the SIM building blocks,
+called through the C ABI and checked against the oracle (float instantiation = the
+reference's semantics) or numpy. This follows the reference's own agreement harness
+(org/fairsim/accel/TestAccel.java:399-443), with thresholds."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def V(fs):
+    fs.native.init(0)
+    return fs.vectors
+
+
+def cvec(V, z):
+    v = V.Vec2dCplx(z.shape[1], z.shape[0])
+    v.setData(z.astype(np.complex64))
+    return v
+
+
+def rvec(V, a):
+    v = V.Vec2dReal(a.shape[1], a.shape[0])
+    v.setData(a.astype(np.float32))
+    return v
+
+
+@pytest.mark.parametrize("w,h", [(64, 64), (96, 96), (128, 256), (384, 384), (512, 512), (768, 768),
+                                 (1024, 1024), (2048, 2048), (1536, 1536), (4096, 4096)])
+def test_fft2d_vs_numpy(V, w, h):
+    rng = np.random.default_rng(w + h)
+    z = (rng.standard_normal((h, w)) + 1j * rng.standard_normal((h, w))).astype(np.complex64)
+    v = cvec(V, z)
+    v.fft2d(False)
+    assert rel_l2(v.vectorData(), np.fft.fft2(z.astype(np.complex128))) < 3e-6
+    v.fft2d(True)
+    assert rel_l2(v.vectorData(), z) < 3e-6
+
+
+def test_elementwise_ops(V):
+    rng = np.random.default_rng(1)
+    n = 96
+    a = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    b = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    r = rng.standard_normal((n, n)).astype(np.float32)
+    va, vb, vr = cvec(V, a), cvec(V, b), rvec(V, r)
+    va.axpy(0.5 - 0.25j, vb)
+    c = np.complex64(0.5 - 0.25j)
+    exp = a.copy()
+    exp.real = a.real + (np.float32(c.real) * b.real - np.float32(c.imag) * b.imag)
+    exp.imag = a.imag + (np.float32(c.imag) * b.real + np.float32(c.real) * b.imag)
+    assert np.array_equal(va.vectorData(), exp)  # AbstractVectorCplx.axpy rounding, bit-exact
+    va.setData(a)
+    va.timesConj(vb)
+    assert rel_l2(va.vectorData(), a * np.conj(b)) < 1e-7
+    va.setData(a)
+    va.times(vr)
+    assert np.array_equal(va.vectorData(), a * r)
+    va.setData(a)
+    assert abs(va.norm2() - float(np.sum(a.real.astype(np.float32) ** 2 + a.imag.astype(np.float32) ** 2, dtype=np.float64))) < 1e-9 * va.norm2()
+    s = va.sumElements()
+    assert abs(s - complex(np.sum(a.astype(np.complex128)))) < 1e-9 * abs(s) + 1e-9
+    d = va.dot(vb)
+    assert abs(d - complex(np.vdot(a.astype(np.complex128), b.astype(np.complex128)))) < 1e-5 * abs(d)
+    vr2 = V.Vec2dReal(n, n)
+    vr2.copy(va)
+    assert np.array_equal(vr2.vectorData(), a.real)
+    va.scal(2.0)
+    assert np.array_equal(va.vectorData(), a * np.float32(2))
+
+
+def test_set_from_16bit_pixels(V):
+    rng = np.random.default_rng(2)
+    u = rng.integers(0, 65535, (64, 64), dtype=np.uint16)
+    v = V.Vec2dCplx(64, 64)
+    v.setFrom16bitPixels(u)
+    assert np.array_equal(v.vectorData(), u.astype(np.float32).astype(np.complex64))
+
+
+@pytest.mark.parametrize("wi,wo,xo,yo", [(64, 128, 0, 0), (64, 128, 5, -7), (48, 96, -3, 2), (64, 64, 3, 1)])
+def test_paste_freq_vs_oracle(V, oracle, wi, wo, xo, yo):
+    rng = np.random.default_rng(wi + wo)
+    z = (rng.standard_normal((wi, wi)) + 1j * rng.standard_normal((wi, wi))).astype(np.complex64)
+    vin, vout = cvec(V, z), V.Vec2dCplx(wo, wo)
+    vout.pasteFreq(vin, xo, yo)
+    assert np.array_equal(vout.vectorData(), oracle.paste_freq(z, wo, wo, xo, yo).astype(np.complex64))
+
+
+@pytest.mark.parametrize("n,kx,ky", [(512, 185.7, -6.7), (1024, -100.9, 155.9), (384, 12.3, 44.1), (1024, 0.37, -0.81)])
+def test_fourier_shift_vs_oracle(V, oracle, n, kx, ky):
+    rng = np.random.default_rng(n)
+    z = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    v = cvec(V, z)
+    v.fourierShift(kx, ky)
+    got = v.vectorData()
+    f64 = oracle.fourier_shift(z.astype(np.complex128), kx, ky, dtype=np.float64)
+    f32 = oracle.fourier_shift(z, kx, ky, dtype=np.float32)
+    # phase reduced exactly before sin/cos: close to FP64; the reference's float phase is within 1e-4
+    assert rel_l2(got, f64) < 2e-7
+    assert rel_l2(got, f32) < 1e-4
+
+
+def test_otf_vectors_vs_oracle(V, oracle, fs):
+    n = 256
+    otf = fs.OtfProvider.fromEstimate(1.4, 525, 0.4)
+    otf.setAttenuation(0.95, 1.4)
+    otf.switchAttenuation(True)
+    sp = fs.SimParam.create(2, 3, 3, n, 0.08, otf)
+    A = fs.algorithm.OtfVectors
+    for (kx, ky, which, write, att) in [(0, 0, 0, True, False), (37.2, -81.6, 0, True, False),
+                                        (12.5, 9.25, 1, True, True)]:
+        v = V.Vec2dCplx(n, n)
+        A.otfToVector(sp, v, 0, kx, ky, att, write)
+        exp = oracle.otf_vector(sp, np.zeros((n, n), complex), kx, ky, which=which)
+        assert np.array_equal(v.vectorData(), exp.astype(np.complex64))
+    rng = np.random.default_rng(3)
+    z = (rng.standard_normal((2 * n, 2 * n)) + 1j * rng.standard_normal((2 * n, 2 * n))).astype(np.complex64)
+    v = cvec(V, z)
+    A.applyOtf(sp, v, 0, 100.5, -40.25)
+    assert np.array_equal(v.vectorData(), oracle.otf_vector(sp, z, 100.5, -40.25, which=2).astype(np.complex64))
+    ra = V.Vec2dReal(2 * n, 2 * n)
+    A.writeApoVector(sp, ra, 0.9, 2.0)
+    assert rel_l2(ra.vectorData(), oracle.apo_vector(sp, 2 * n, 2 * n, 0.9, 2.0)) < 1e-7
+    rt = V.Vec2dReal(n, n)
+    cut = otf.getCutoff()
+    A.writeAttenuationVector(sp, rt, 0.99, 0.15 * cut, 0, 0)
+    assert rel_l2(rt.vectorData(), oracle.attenuation_vector(sp, n, n, 0.99, 0.15 * cut)) < 1e-7
+
+
+def test_wiener_denominator_vs_oracle(V, oracle, fs):
+    n = 256
+    raw, truth = fs.synth.make_dataset(n=n, seed=3)
+    sp = fs.synth.sim_param_for(truth, n)
+    for att in (False, True):
+        sp.otf().switchAttenuation(att)
+        wd = fs.algorithm.WienerFilter(sp).getDenominator(sp.getWienerFilter())
+        exp = oracle.wiener_denominator(sp)
+        assert rel_l2(wd.vectorData(), exp) < 1e-7
+
+
+def test_separate_bands_vs_oracle(V, oracle, fs):
+    n = 128
+    raw, truth = fs.synth.make_dataset(n=n, seed=5)
+    sp = fs.synth.sim_param_for(truth, n)
+    spec = oracle.prepare_raw(sp, raw)
+    inv = [cvec(V, spec[p]) for p in range(3)]
+    out = [V.Vec2dCplx(n, n) for _ in range(3)]
+    d = sp.dir(0)
+    fs.algorithm.BandSeparation.separateBands(inv, out, d.getPhases(), 2, d.getModulations())
+    exp = oracle.separate_bands(sp, 0, spec[:3])
+    for i in range(3):
+        assert np.array_equal(out[i].vectorData(), exp[i].astype(np.complex64))
+
+
+def test_correlation_fit_vs_oracle(V, oracle, fs):
+    n = 256
+    raw, truth = fs.synth.make_dataset(n=n, seed=6)
+    sp = fs.synth.sim_param_for(truth, n, known=False)
+    spec = oracle.prepare_raw(sp, raw)
+    sep = oracle.separate_bands(sp, 0, spec[:3])  # phases 0, 2pi/3.. with modulation 1 -> fac .5
+    k = truth["pxpy"][0]
+    # commonRegion
+    g0, g1 = cvec(V, sep[0]), cvec(V, sep[1])
+    fs.algorithm.Correlation.commonRegion(g0, g1, 0, 1, sp, -k[0], -k[1], 0.15, 0.05, True)
+    e0, e1 = oracle.common_region(sp, sep[0], sep[1], -k[0], -k[1])
+    assert np.array_equal(g0.vectorData(), e0.astype(np.complex64))
+    assert np.array_equal(g1.vectorData(), e1.astype(np.complex64))
+    # fitPeak: the grid maxima and therefore the fitted k must agree
+    b0, b1 = cvec(V, sep[0]), cvec(V, sep[1])
+    start = (-round(k[0]), -round(k[1]))
+    grid = np.zeros((3, 10, 10, 2))
+    got = fs.algorithm.Correlation.fitPeak(b0, b1, 0, 1, sp, start[0], start[1], 0.05, 2.5, grid)
+    exp, egrid = oracle.fit_peak(sp, sep[0], sep[1], start[0], start[1])
+    assert abs(got[0] - exp[0]) < 1e-9 and abs(got[1] - exp[1]) < 1e-9
+    gg = grid[..., 0] + 1j * grid[..., 1]
+    assert rel_l2(gg, egrid) < 1e-4
+    assert abs(got[3] - exp[3]) < 1e-4 * abs(exp[3])
+    p = fs.algorithm.Correlation.getPeak(b0, b1, 0, 1, sp, exp[0], exp[1], 0.05)
+    ep = oracle.get_peak(sp, sep[0], sep[1], exp[0], exp[1])
+    assert abs(p - ep) < 1e-4 * abs(ep)
+
+
+@pytest.mark.parametrize("n", [256, 512])
+def test_estimate_parameters_vs_oracle(V, oracle, fs, n):
+    raw, truth = fs.synth.make_dataset(n=n, seed=8)
+    sp = fs.synth.sim_param_for(truth, n, known=False)
+    spec = oracle.prepare_raw(sp, raw)
+    est, epeaks, _ = oracle.estimate(sp, spec, 1, 0.6)
+    inFFT = [[cvec(V, spec[a * 3 + p]) for p in range(3)] for a in range(3)]
+    gpeaks = fs.algorithm.SimAlgorithm.estimateParameters(sp, inFFT, 1, 0.6)
+    for d in range(3):
+        # same fitted k0 (the grid search picks the same point) and the same pixel
+        assert abs(sp.dir(d).pX - est["pX"][d]) < 1e-9 and abs(sp.dir(d).pY - est["pY"][d]) < 1e-9
+        assert round(sp.dir(d).pX) == round(truth["pxpy"][d][0]) and round(sp.dir(d).pY) == round(truth["pxpy"][d][1])
+        assert abs(sp.dir(d).phaOff - est["phaOff"][d]) < 1e-4
+        assert abs(sp.dir(d).modul[1] - est["modulations"][d][1]) < 1e-4
+
+
+@pytest.mark.parametrize("n", [128, 512])
+def test_run_reconstruction_op_by_op_vs_oracle(V, oracle, fs, n):
+    raw, truth = fs.synth.make_dataset(n=n, seed=9)
+    sp = fs.synth.sim_param_for(truth, n)
+    spec = oracle.prepare_raw(sp, raw)
+    exp32 = oracle.recon(sp, spec)
+    exp64 = oracle.recon(sp, spec.astype(np.complex128), dtype=np.float64)
+    inFFT = [[cvec(V, spec[a * 3 + p]) for p in range(3)] for a in range(3)]
+    out = fs.algorithm.SimAlgorithm.runReconstruction(sp, inFFT, False, 0).vectorData()
+    assert rel_l2(out, exp32) < 1e-4   # vs the reference's float semantics
+    assert rel_l2(out, exp64) < 1e-5   # vs the FP64 oracle
