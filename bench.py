@@ -1,0 +1,418 @@
+"""Benchmark of the fused, batched 2D SIM reconstruction on GB300.
+
+Workload (one "step"): a batch of B independent 512x512 datasets, 3 angles x 3 phases
+(float32 raw, seeded synthetic), reconstructed to 1024x1024 with known parameters,
+Wiener 0.05, apodization cutoff 2.0 (SimAlgorithm.runReconstruction semantics with the
+GUI's input preparation: fadeBorderCos(10), FFT). The raw batch (B * 9 MiB) is larger
+than L2, so no flush is needed between steps.
+
+  value      recon/s with inputs resident in HBM, device-timed (CUDA events on the launch stream)
+  e2e        recon/s through the C ABI with host buffers (pinned H2D + batch + D2H every step)
+  roofline   the dominant pass's algorithmic bytes / its event-timed duration vs measured HBM peak
+  cpu_baseline  the oracle (CPU restatement of the reference's Java path), all host threads
+  plain_gpu  the op-by-op device path (fsim_run_reconstruction, one dataset at a time)
+  serve      live served form: Poisson arrivals, 3 channels, p50/p99 latency
+
+`--impl reference` times the reference path's CPU implementation (the oracle port; the Java
+reference cannot run here) on the same workload and prints the same JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SIM recon/s at 512² 3×3 batched+served vs plain GPU; p50/p99 live latency"
+N = 512
+NA, NP, NB = 3, 3, 2
+WORKLOAD = "offline 2D SIM reconstruction, 512x512 x (3 angles x 3 phases) f32 -> 1024x1024, known params, wiener 0.05, apo cutoff 2.0, fade 10"
+
+
+def load_package():
+    import __graft_entry__ as g
+
+    return g.load_package()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_datasets(fs, n_distinct, seed0=1000):
+    out = []
+    for i in range(n_distinct):
+        raw, truth = fs.synth.make_dataset(n=N, seed=seed0 + i)
+        sp = fs.synth.sim_param_for(truth, N)
+        out.append((raw, sp))
+    return out
+
+
+def cpu_recon_rate(fs, datasets, min_seconds=10.0, max_recons=40):
+    """Oracle (CPU restatement of the reference Java path) with every host thread."""
+    from oracle import refcpu
+
+    cores = os.cpu_count() or 1
+    refcpu.set_threads(cores)
+    raw, sp = datasets[0]
+    refcpu.recon_raw(sp, raw, fade=10)  # warm-up (thread pool, plans)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_recons and (time.perf_counter() - t0 < min_seconds or n < 2):
+        raw, sp = datasets[n % len(datasets)]
+        refcpu.recon_raw(sp, raw, fade=10)
+        n += 1
+    dt = time.perf_counter() - t0
+    return n / dt, cores, n, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    fs = load_package()
+    from oracle import refcpu
+
+    refcpu.build()
+    ds = make_datasets(fs, 2)
+    cores = os.cpu_count() or 1
+    refcpu.set_threads(cores)
+    for i in range(args.warmup):
+        raw, sp = ds[i % len(ds)]
+        refcpu.recon_raw(sp, raw, fade=10)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        raw, sp = ds[i % len(ds)]
+        refcpu.recon_raw(sp, raw, fade=10)
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "recon/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "batch": 1, "n": N,
+                   "note": "each step is one dataset of the batched workload (bounded CPU sample)"},
+        "cpu_baseline": {"value": v, "unit": "recon/s", "cores": cores, "kind": "port",
+                         "sample": "%d reconstructions of 512x512 3x3 -> 1024x1024 (oracle, C++ restatement of the "
+                                   "reference Java path; the Java reference and its JTransforms jar cannot run here)"
+                                   % args.steps},
+        "e2e": {"value": v, "unit": "recon/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--distinct", type=int, default=16)
+    ap.add_argument("--no-extras", action="store_true", help="skip plain-GPU, serve and CPU legs")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    fs = load_package()
+    N_ = fs.native
+    N_.init(local)
+
+    B = args.batch
+    datasets = make_datasets(fs, args.distinct, seed0=1000 + 97 * rank)
+    plans = [fs.plan.ReconPlan(sp, path=N_.PATH_OFFLINE, input_type=N_.INPUT_F32, fade_px=10) for _, sp in datasets]
+    job_plans = [plans[i % len(plans)] for i in range(B)]
+    raw_host = torch.empty((B, NA * NP, N, N), dtype=torch.float32).pin_memory()
+    for i in range(B):
+        raw_host[i].copy_(torch.from_numpy(datasets[i % len(datasets)][0]))
+    raw_dev = raw_host.cuda()
+    out_dev = torch.empty((B, 2 * N, 2 * N), dtype=torch.float32, device="cuda")
+    out_host = torch.empty((B, 2 * N, 2 * N), dtype=torch.float32).pin_memory()
+    ws_bytes = fs.plan.batch_workspace_bytes(job_plans)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    sp_ = stream.cuda_stream
+    jobs = [(job_plans[i], raw_dev[i].data_ptr(), out_dev[i].data_ptr()) for i in range(B)]
+
+    def step():
+        fs.plan.recon_batch(jobs, ws.data_ptr(), ws_bytes, sp_)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(fn, k):
+        with torch.cuda.stream(stream):
+            barrier()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(k):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            barrier()
+            ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # ---- resident (device) throughput ----
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = timed(step, args.steps)
+    clk = clocks.stop()
+    value = B * args.steps * world / (ms / 1000.0)
+    launches_per_step = 3  # one size class: passes A, B, C
+
+    # ---- end to end through the C ABI with host buffers ----
+    def e2e_step():
+        raw_dev.copy_(raw_host, non_blocking=True)
+        fs.plan.recon_batch(jobs, ws.data_ptr(), ws_bytes, sp_)
+        out_host.copy_(out_dev, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            e2e_step()
+    e2e_ms = timed(lambda: None, 0)  # sync
+    e2e_steps = max(3, args.steps // 2)
+    with torch.cuda.stream(stream):
+        e2e_ms = timed(e2e_step, e2e_steps)
+    e2e_value = B * e2e_steps * world / (e2e_ms / 1000.0)
+    h2d = B * NA * NP * N * N * 4
+    d2h = B * 4 * N * N * 4
+
+    # ---- per-pass timing of the dominant kernel (CUDA events between passes) ----
+    import ctypes as C
+
+    N_.check(N_.lib().fsim_profile_enable(1))
+    pass_ms = []
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            step()
+            arr = (C.c_float * 8)()
+            n = C.c_int()
+            N_.check(N_.lib().fsim_profile_read(arr, 8, C.byref(n)))
+            pass_ms.append([arr[i] for i in range(n.value)])
+    N_.check(N_.lib().fsim_profile_enable(0))
+    pm = np.median(np.array(pass_ms), axis=0)
+    nwin = int(np.ceil((2 * np.ceil(1000 / (525 / 1.4 / 2) / (1 / (N * 0.08))) + 6) / 4) * 4 + 4)
+    nwin = min(nwin, 2 * N)
+    W = 2 * N
+    bytes_a = NA * NP * N * N * 4 + NA * (2 * NB - 1) * nwin * N * 8
+    bytes_b = NA * (2 * NB - 1) * nwin * N * 8 + NA * (2 * NB - 1) * nwin * nwin * 4 + W * W * 4 + W * W * 8
+    bytes_c = W * W * 8 + W * W * 4
+    algo = [bytes_a, bytes_b, bytes_c]
+    names = ["k_pass_a<512>", "k_pass_b<512>", "k_pass_c<512>"]
+    dom = int(np.argmax(pm))
+    peak, peak_kind = peaks()
+    achieved = algo[dom] * B / (pm[dom] / 1000.0) / 1e9
+    passes = {names[i]: {"ms": float(pm[i]), "algorithmic_MB_per_dataset": algo[i] / 1e6,
+                         "GB_per_s": algo[i] * B / (pm[i] / 1000.0) / 1e9} for i in range(len(pm))}
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            tr = json.load(f)
+            traffic = tr.get(names[dom])
+    except Exception:
+        pass
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        # plain GPU form: one dataset at a time through the op-by-op vector path
+        V = fs.vectors
+        raw, sp = datasets[0]
+        from oracle import refcpu  # input preparation reference only for shapes
+
+        spec_vecs = [[V.Vec2dCplx(N, N) for _ in range(NP)] for _ in range(NA)]
+        fade = V.Vec2dReal(N, N)
+        fade.setData(np.ones((N, N), np.float32))
+        host_raw = [raw[i] for i in range(NA * NP)]
+
+        def plain():
+            for a in range(NA):
+                for p in range(NP):
+                    v = spec_vecs[a][p]
+                    v.setData(host_raw[a * NP + p].astype(np.complex64))
+                    v.times(fade)
+                    v.fft2d(False)
+            out = fs.algorithm.SimAlgorithm.runReconstruction(sp, spec_vecs, False, 0)
+            out.vectorData()
+
+        plain()
+        t0 = time.perf_counter()
+        k = 5
+        for _ in range(k):
+            plain()
+        plain_rate = k / (time.perf_counter() - t0)
+        extras["plain_gpu"] = {"value": plain_rate, "unit": "recon/s",
+                               "note": "op-by-op device vector path, one dataset at a time, host buffers"}
+        extras["speedup_batched_vs_plain"] = value / plain_rate
+        extras["speedup_e2e_vs_plain"] = e2e_value / plain_rate
+        # served form: Poisson arrivals, 3 channels x 100 stacks/s at 512^2 u16, 10% at 1024^2
+        extras["serve"] = serve_leg(fs, seconds=3.0)
+        # CPU baseline (oracle) on a bounded sample
+        rate, cores, n, dt = cpu_recon_rate(fs, datasets)
+        extras["cpu_baseline"] = {"value": rate, "unit": "recon/s", "cores": cores, "kind": "port",
+                                  "sample": "%d reconstructions of one 512x512 3x3 dataset in %.1f s (oracle: C++ "
+                                            "restatement of the reference Java path, %d threads)" % (n, dt, cores)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "recon/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded: 2000 lognormal points + 40 filaments, cos patterns m=0.8, |k0|=0.85 cutoff, "
+                    "500 photons + N(0,2)); %d distinct datasets tiled to the batch" % args.distinct,
+            "config": {"workload": WORKLOAD, "batch": B, "n": N, "out": 2 * N, "path": "offline (runReconstruction)",
+                       "l2": "inputs larger than L2 (%.0f MiB raw per step)" % (h2d / 2 ** 20),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": "recon/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": algo[dom] * B},
+            "passes": passes,
+            "e2e_fraction_of_hbm": (18874368 * value) / (peak * 1e9),
+            "clocks": clk,
+            "gpu_launches": launches_per_step * args.steps,
+        }
+        if "cpu_baseline" in extras:
+            line["cpu_baseline"] = extras.pop("cpu_baseline")
+        line.update(extras)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def serve_leg(fs, seconds=3.0, rate_per_channel=100.0, seed=5):
+    """Poisson arrivals from 3 channels at 512^2 (u16) plus their 1024^2 stacks (10%)."""
+    N_ = fs.native
+    rng = np.random.default_rng(seed)
+    chans, stacks = [], []
+    for ch, lam in enumerate([488.0, 525.0, 600.0]):
+        for n in (512, 1024):
+            raw, truth = fs.synth.make_dataset(n=n, seed=200 + 10 * ch + n // 512, em_wavelength=lam, as_u16=True)
+            chans.append(fs.synth.sim_param_for(truth, n))
+            stacks.append(raw)
+    srv = fs.plan.Server(chans, max_batch=16, max_inflight=96, streams=3, refit_every=50,
+                         input_type=N_.INPUT_U16, fade_px=10)
+    outs = {n: np.empty((2 * n, 2 * n), np.float32) for n in (512, 1024)}
+    # arrival schedule
+    events = []
+    for ch in range(3):
+        t = 0.0
+        while t < seconds:
+            t += rng.exponential(1.0 / rate_per_channel)
+            big = rng.random() < 0.1
+            events.append((t, 2 * ch + (1 if big else 0)))
+    events.sort()
+    tickets = []
+    t0 = time.perf_counter()
+    rejected = 0
+    for t, c in events:
+        while time.perf_counter() - t0 < t:
+            time.sleep(0.0002)
+        tk = srv.try_submit(c, stacks[c])
+        if tk is None:
+            rejected += 1
+            continue
+        tickets.append((tk, c))
+        # collect finished results opportunistically to free slots
+        while len(tickets) > 64:
+            tk0, c0 = tickets.pop(0)
+            srv.wait(tk0, outs[chans[c0].w])
+    for tk, c in tickets:
+        srv.wait(tk, outs[chans[c].w])
+    st = srv.stats()
+    srv.close()
+    return {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+            "recon_per_s": st["completed"] / max(1e-9, time.perf_counter() - t0), "completed": st["completed"],
+            "rejected": st["rejected"], "refits": st["refits"],
+            "arrivals": "Poisson, 3 channels x %.0f stacks/s, 10%% at 1024^2, u16, %.1f s" % (rate_per_channel, seconds)}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

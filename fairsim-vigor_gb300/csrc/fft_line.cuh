@@ -168,10 +168,9 @@ __host__ __device__ constexpr bool plan_ok(int L, int T) {
 }
 
 // ---- one Stockham stage ---------------------------------------------------------
-template <int L, int T, int C, int R, int NS, bool INV>
-__device__ __forceinline__ void fft_stage(float2* s, int c, int t) {
+template <int L, int T, int C, int R, int NS, bool INV, int TS>
+__device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2* tw) {
   constexpr int E = L / T, NB = E / R, LR = L / R;
-  const float2* tw = g_tw + tw_offset(L);
   float2 v[NB][R];
 #pragma unroll
   for (int b = 0; b < NB; b++) {
@@ -187,7 +186,7 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t) {
     if constexpr (NS > 1) {
 #pragma unroll
       for (int r = 1; r < R; r++) {
-        float2 w = tw[r * k * (L / (NS * R))];
+        float2 w = tw[r * k * (L / (NS * R)) * TS];
         if (INV) w.y = -w.y;
         v[b][r] = cmul(v[b][r], w);
       }
@@ -200,23 +199,37 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t) {
   __syncthreads();
 }
 
-template <int L, int T, int C, bool INV, int NS>
-__device__ __forceinline__ void fft_stages(float2* s, int c, int t) {
+template <int L, int T, int C, bool INV, int NS, int TS>
+__device__ __forceinline__ void fft_stages(float2* s, int c, int t, const float2* tw) {
   if constexpr (NS < L) {
     constexpr int R = pick_radix(L / NS, L / T);
     static_assert((L / NS) % R == 0 && (L / T) % R == 0, "bad radix plan");
-    fft_stage<L, T, C, R, NS, INV>(s, c, t);
-    fft_stages<L, T, C, INV, NS * R>(s, c, t);
+    fft_stage<L, T, C, R, NS, INV, TS>(s, c, t, tw);
+    fft_stages<L, T, C, INV, NS * R, TS>(s, c, t, tw);
   }
 }
 
 // Transform C interleaved lines of length L in place in shared memory `s`.
 // Called by exactly C*T threads (the whole block): it contains __syncthreads.
+// Twiddles come from the accurate global table by default, or from a copy of the
+// length-LT table in shared memory (tw_smem, LT a multiple of L) when the caller staged one.
 template <int L, int T, int C, bool INV>
 __device__ __forceinline__ void line_fft(float2* s, int lt) {
   static_assert(supported_len(L), "unsupported FFT length");
   static_assert(plan_ok(L, T), "L/T must be divisible by every radix");
-  fft_stages<L, T, C, INV, 1>(s, lt % C, lt / C);
+  fft_stages<L, T, C, INV, 1, 1>(s, lt % C, lt / C, g_tw + tw_offset(L));
+}
+template <int L, int T, int C, bool INV, int LT>
+__device__ __forceinline__ void line_fft_tw(float2* s, int lt, const float2* tw_smem) {
+  static_assert(supported_len(L) && LT % L == 0, "unsupported FFT length / table");
+  static_assert(plan_ok(L, T), "L/T must be divisible by every radix");
+  fft_stages<L, T, C, INV, 1, LT / L>(s, lt % C, lt / C, tw_smem);
+}
+// Stage the exp(-2 pi i m / LT) table into shared memory (all threads of the block).
+template <int LT>
+__device__ __forceinline__ void stage_twiddles(float2* tw_smem, int tid, int nthreads) {
+  const float2* g = g_tw + tw_offset(LT);
+  for (int i = tid; i < LT; i += nthreads) tw_smem[i] = g[i];
 }
 
 }  // namespace fsim

@@ -386,10 +386,19 @@ static int launch_live(const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t 
     FSIM_CUDA(cudaFuncSetAttribute(k_live_d<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_d));
     attr = true;
   }
+  cudaEvent_t* ev = profile_events();
+  if (ev) cudaEventRecord(ev[0], st);
   k_live_a<N><<<dim3(N / P::GA, njobs), P::GA * P::TN, 0, st>>>(d_jobs);
+  if (ev) cudaEventRecord(ev[1], st);
   k_live_b<N><<<dim3(N / P::CBL, njobs), P::CBL * P::TN, 0, st>>>(d_jobs);
+  if (ev) cudaEventRecord(ev[2], st);
   k_live_c<N><<<dim3(W, njobs), P::TW, 0, st>>>(d_jobs);
+  if (ev) cudaEventRecord(ev[3], st);
   k_live_d<N><<<dim3(W / P::CD, njobs), P::CD * P::TW, smem_d, st>>>(d_jobs);
+  if (ev) {
+    cudaEventRecord(ev[4], st);
+    profile_mark(4);
+  }
   FSIM_CHECK_LAUNCH();
   return FSIM_OK;
 }

@@ -91,6 +91,12 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
   return FSIM_OK;
 }
 
+static bool g_prof_on = false;
+static cudaEvent_t g_prof_ev[8];
+static int g_prof_n = 0;
+cudaEvent_t* profile_events() { return g_prof_on ? g_prof_ev : nullptr; }
+void profile_mark(int n_passes) { g_prof_n = n_passes; }
+
 size_t batch_workspace_bytes(const Plan* const* plans, int n) {
   size_t need = align256(sizeof(JobDesc) * n);
   for (int i = 0; i < n; i++) need += align256(plan_ws(plans[i]));
@@ -183,6 +189,26 @@ int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t w
   rc = recon_batch(jobs, n_jobs, workspace, workspace_bytes, st, (JobDesc*)s->ptr, true);
   if (rc) return rc;
   FSIM_CUDA(cudaEventRecord(s->done, st));
+  return FSIM_OK;
+}
+
+int fsim_profile_enable(int on) {
+  NEED_INIT();
+  if (on && !g_prof_ev[0])
+    for (int i = 0; i < 8; i++) FSIM_CUDA(cudaEventCreate(&g_prof_ev[i]));
+  g_prof_on = on != 0;
+  g_prof_n = 0;
+  return FSIM_OK;
+}
+
+int fsim_profile_read(float* ms, int max_passes, int* n_passes) {
+  FSIM_REQUIRE(ms && n_passes, FSIM_EINVAL, "profile_read: bad arguments");
+  *n_passes = 0;
+  if (!g_prof_on || g_prof_n == 0) return FSIM_OK;
+  FSIM_CUDA(cudaEventSynchronize(g_prof_ev[g_prof_n]));
+  int n = std::min(g_prof_n, max_passes);
+  for (int i = 0; i < n; i++) FSIM_CUDA(cudaEventElapsedTime(&ms[i], g_prof_ev[i], g_prof_ev[i + 1]));
+  *n_passes = n;
   return FSIM_OK;
 }
 

@@ -49,13 +49,15 @@ struct Cfg {
 
 // ---- pass A ------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(Cfg<N>::T) k_pass_a(const JobDesc* __restrict__ jobs) {
+__global__ void __launch_bounds__(Cfg<N>::T, (Cfg<N>::T <= 64 ? 8 : 4)) k_pass_a(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N>;
   constexpr int W = P::W, T = P::T, EN = N / T, EW = W / T;
   const JobDesc& J = jobs[blockIdx.z];
   const int y = blockIdx.x, a = blockIdx.y, t = threadIdx.x;
   if (a >= J.nA) return;  // uniform per block
   __shared__ float2 s[smem_line_elems(W, 1)];
+  __shared__ float2 tw[W];
+  stage_twiddles<W>(tw, t, T);
   const int nP = J.nP, nC = J.nC;
   const size_t frame = (size_t)N * N;
   const float* rawf = (const float*)J.raw;
@@ -84,7 +86,7 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_pass_a(const JobDesc* __restrict_
       s[sidx(x)] = z;
     }
     __syncthreads();
-    line_fft<N, T, 1, false>(s, t);
+    line_fft_tw<N, T, 1, false, W>(s, t, tw);
     // paste along x: m < N/2 stays, m >= N/2 moves to m + N; the middle becomes zero
     float2 v[EN];
 #pragma unroll
@@ -98,7 +100,7 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_pass_a(const JobDesc* __restrict_
     }
     __syncthreads();
     if (c > 0) {
-      line_fft<W, T, 1, true>(s, t);
+      line_fft_tw<W, T, 1, true, W>(s, t, tw);
       const float2* rx = J.ramps + (size_t)(a * nC + c) * 2 * W;
 #pragma unroll
       for (int i = 0; i < EW; i++) {
@@ -106,7 +108,7 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_pass_a(const JobDesc* __restrict_
         s[sidx(k)] = cmul(s[sidx(k)], __ldg(&rx[k]));
       }
       __syncthreads();
-      line_fft<W, T, 1, false>(s, t);
+      line_fft_tw<W, T, 1, false, W>(s, t, tw);
     }
     // keep the OTF-support window: columns Xs .. Xs+nWin-1 (mod W), quad layout
     const int Xs = J.win[2 * (a * nC + c)];
@@ -122,7 +124,7 @@ __global__ void __launch_bounds__(Cfg<N>::T) k_pass_a(const JobDesc* __restrict_
 
 // ---- pass B ------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T) k_pass_b(const JobDesc* __restrict__ jobs) {
+__global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T, (Cfg<N>::CB * Cfg<N>::T <= 256 ? 2 : 1)) k_pass_b(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N>;
   constexpr int W = P::W, T = P::T, CB = P::CB, EN = N / T, EW = W / T;
   const JobDesc& J = jobs[blockIdx.y];
@@ -131,6 +133,8 @@ __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T) k_pass_b(const JobDesc*
   extern __shared__ float2 sm[];
   float2* acc = sm;
   float2* wk = sm + smem_line_elems(W, CB);
+  float2* tw = wk + smem_line_elems(W, CB);
+  stage_twiddles<W>(tw, lt, CB * T);
   const int nC = J.nC, nWin = J.nWin;
 #pragma unroll
   for (int i = 0; i < EW; i++) acc[sidx((t + i * T) * CB + lane)] = make_float2(0.f, 0.f);
@@ -158,7 +162,7 @@ __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T) k_pass_b(const JobDesc*
         wk[sidx(k * CB + lane)] = v;
       }
       __syncthreads();
-      line_fft<N, T, CB, false>(wk, lt);
+      line_fft_tw<N, T, CB, false, W>(wk, lt, tw);
       float2 v[EN];
 #pragma unroll
       for (int i = 0; i < EN; i++) v[i] = wk[sidx((t + i * T) * CB + lane)];
@@ -171,7 +175,7 @@ __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T) k_pass_b(const JobDesc*
       }
       __syncthreads();
       if (c > 0) {
-        line_fft<W, T, CB, true>(wk, lt);
+        line_fft_tw<W, T, CB, true, W>(wk, lt, tw);
         const float2* ry = J.ramps + (size_t)(a * nC + c) * 2 * W + W;
 #pragma unroll
         for (int i = 0; i < EW; i++) {
@@ -179,7 +183,7 @@ __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T) k_pass_b(const JobDesc*
           wk[sidx(k * CB + lane)] = cmul(wk[sidx(k * CB + lane)], __ldg(&ry[k]));
         }
         __syncthreads();
-        line_fft<W, T, CB, false>(wk, lt);
+        line_fft_tw<W, T, CB, false, W>(wk, lt, tw);
       }
       // times conj(OTF) inside the window rows, accumulate
       const int Ys = J.win[2 * (aw * nC + c) + 1];
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T) k_pass_b(const JobDesc*
     o.y *= f;
   }
   __syncthreads();
-  line_fft<W, T, CB, true>(acc, lt);
+  line_fft_tw<W, T, CB, true, W>(acc, lt, tw);
 #pragma unroll
   for (int i = 0; i < EW; i++) {
     const int k = t + i * T;
@@ -225,12 +229,14 @@ __global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::T) k_pass_c(const JobDesc*
   const int g = threadIdx.x / T, t = threadIdx.x % T;
   const int Y = blockIdx.x * G + g;
   __shared__ float2 sm[G * smem_line_elems(W, 1)];
+  __shared__ float2 tw[W];
+  stage_twiddles<W>(tw, threadIdx.x, G * T);
   float2* s = sm + g * smem_line_elems(W, 1);
   const float2* row = J.O + (size_t)Y * W;
 #pragma unroll
   for (int i = 0; i < EW; i++) s[sidx(t + i * T)] = row[t + i * T];
   __syncthreads();
-  line_fft<W, T, 1, true>(s, t);
+  line_fft_tw<W, T, 1, true, W>(s, t, tw);
   const float scale = 1.f / ((float)W * (float)W);
   float* out = J.out + (size_t)Y * W;
 #pragma unroll
@@ -428,17 +434,25 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws
 // ---- launch --------------------------------------------------------------------------------------
 template <int N>
 static int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st) {
+  cudaEvent_t* ev = profile_events();
   using P = Cfg<N>;
   constexpr int W = P::W;
   static bool attr = false;
-  const size_t smem_b = sizeof(float2) * 2 * smem_line_elems(W, P::CB);
+  const size_t smem_b = sizeof(float2) * (2 * smem_line_elems(W, P::CB) + W);
   if (!attr) {
     FSIM_CUDA(cudaFuncSetAttribute(k_pass_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
     attr = true;
   }
+  if (ev) cudaEventRecord(ev[0], st);
   k_pass_a<N><<<dim3(N, maxA, njobs), P::T, 0, st>>>(d_jobs);
+  if (ev) cudaEventRecord(ev[1], st);
   k_pass_b<N><<<dim3(W / P::CB, njobs), P::CB * P::T, smem_b, st>>>(d_jobs);
+  if (ev) cudaEventRecord(ev[2], st);
   k_pass_c<N><<<dim3(W / P::GC, njobs), P::GC * P::T, 0, st>>>(d_jobs);
+  if (ev) {
+    cudaEventRecord(ev[3], st);
+    profile_mark(3);
+  }
   FSIM_CHECK_LAUNCH();
   return FSIM_OK;
 }

@@ -56,6 +56,11 @@ struct Plan {
   void fill_job_live(JobDesc& j, const void* raw, float* out, float* wf, char* ws) const;
 };
 
+// Optional per-pass CUDA-event timing of the next batches (fsim_profile_*): returns the
+// event array to record into, or nullptr when profiling is off.
+cudaEvent_t* profile_events();
+void profile_mark(int n_passes);
+
 bool offline_size_supported(int n);
 bool live_size_supported(int n);
 int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);

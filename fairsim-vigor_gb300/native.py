@@ -160,6 +160,8 @@ _SIGS = {
     "fsim_plan_info": (I32, [VP, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
     "fsim_recon_batch": (I32, [VP, I32, VP, C.c_size_t, VP]),
     "fsim_recon_host": (I32, [VP, VP, VP]),
+    "fsim_profile_enable": (I32, [I32]),
+    "fsim_profile_read": (I32, [VP, I32, C.POINTER(I32)]),
     "fsim_estimate_raw": (I32, [VP, VP, I32, I32, I32, F64, VP]),
     "fsim_live_refit": (I32, [VP, VP, VP]),
     "fsim_serve_open": (I32, [C.POINTER(VP), VP, VP, I32]),

@@ -158,6 +158,12 @@ typedef struct fsim_job {
  * size class. workspace: device memory of at least the sum of fsim_plan_workspace_bytes. */
 int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t workspace_bytes,
                      void* stream);
+/* Per-pass CUDA-event timing of fused batches (no reference counterpart): while enabled,
+ * every batch records events between its passes on its stream; fsim_profile_read waits
+ * for the last batch and returns the duration of each pass of its last size class
+ * (offline: A, B, C; live: LA, LB, LC, LD). */
+int fsim_profile_enable(int on);
+int fsim_profile_read(float* ms, int max_passes, int* n_passes);
 /* Host-buffer convenience: H2D copy of raw, reconstruction, D2H copy of out. */
 int fsim_recon_host(fsim_plan* plan, const void* raw_host, float* out_host);
 /* Parameter fit on device raw frames (fade + FFT + SimAlgorithm.estimateParameters). */

@@ -1,0 +1,74 @@
+"""GPU tests of the served form (fsim_serve_*), the continuous-batching replacement of
+ReconstructionRunner (org/fairsim/livemode/ReconstructionRunner.java:140-593):
+  * each result is identical alone and in a mix of concurrent requests from several
+    channels and sizes (continuous batching must not change a reconstruction);
+  * admission refuses work beyond the slot budget with FSIM_EBUSY (no silent drops);
+  * refits run on the device every N stacks and swap in parameters that match the
+    oracle's ParameterRefitThread.doRefit on the same stack."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def channel(fs, n, seed, lam=525.0):
+    raw, truth = fs.synth.make_dataset(n=n, seed=seed, em_wavelength=lam, as_u16=True)
+    return raw, fs.synth.sim_param_for(truth, n)
+
+
+def test_results_identical_alone_and_in_mix(fs):
+    specs = [(256, 1, 488.0), (256, 2, 525.0), (512, 3, 600.0), (384, 4, 525.0)]
+    chans = [channel(fs, n, s, lam) for n, s, lam in specs]
+    alone = []
+    for raw, sp in chans:
+        plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE, input_type=fs.native.INPUT_U16, fade_px=10)
+        alone.append(plan.reconstruct_host(raw))
+    srv = fs.plan.Server([sp for _, sp in chans], max_batch=8, max_inflight=32, streams=3, refit_every=0)
+    order = [0, 1, 2, 3, 2, 1, 0, 3, 3, 0, 1, 2, 0, 0, 2, 1]
+    tickets = [(srv.submit(c, chans[c][0]), c) for c in order]
+    for tk, c in tickets:
+        n = chans[c][1].w
+        out = np.empty((2 * n, 2 * n), np.float32)
+        lat = srv.wait(tk, out)
+        assert lat > 0
+        assert np.array_equal(out, alone[c])
+    st = srv.stats()
+    assert st["completed"] == len(order) and st["rejected"] == 0
+    srv.close()
+
+
+def test_admission_refuses_when_slots_are_full(fs):
+    raw, sp = channel(fs, 256, 7)
+    srv = fs.plan.Server([sp], max_batch=2, max_inflight=3, streams=1, refit_every=0)
+    got = [srv.try_submit(0, raw) for _ in range(3)]
+    assert all(t is not None for t in got)
+    assert srv.try_submit(0, raw) is None  # every slot is taken until a result is collected
+    out = np.empty((512, 512), np.float32)
+    srv.wait(got[0], out)
+    assert srv.try_submit(0, raw) is not None
+    assert srv.stats()["rejected"] == 1
+    srv.close()
+
+
+def test_refit_on_device_matches_oracle(fs, oracle):
+    raw, sp = channel(fs, 512, 11)
+    # start from deliberately wrong parameters; the refit must recover them from the stack
+    sp0 = sp.duplicate()
+    for d in range(3):
+        sp0.dir(d).pX += 0.7
+        sp0.dir(d).pY -= 0.4
+    srv = fs.plan.Server([sp0], max_batch=4, max_inflight=8, streams=2, refit_every=4)
+    out = np.empty((1024, 1024), np.float32)
+    for _ in range(4):
+        srv.wait(srv.submit(0, raw), out)
+    deadline = time.time() + 30
+    while srv.stats()["refits"] < 1 and time.time() < deadline:
+        time.sleep(0.05)
+    assert srv.stats()["refits"] >= 1
+    got = srv.channel_params(0)
+    exp, _ = oracle.live_refit(sp0, raw)
+    for d in range(3):
+        assert abs(got["pX"][d] - exp["pX"][d]) < 1e-9 and abs(got["pY"][d] - exp["pY"][d]) < 1e-9
+    srv.close()
