@@ -19,6 +19,25 @@
 
 namespace fsim {
 
+// ---- radix choice (used by the table layouts below) ----------------------------
+__host__ __device__ constexpr int pick_radix_fwd(int rem, int E) {
+  return (rem % 3 == 0 && E % 3 == 0)      ? 3
+         : (rem % 16 == 0 && E % 16 == 0) ? 16
+         : (rem % 8 == 0 && E % 8 == 0)   ? 8
+         : (rem % 4 == 0 && E % 4 == 0)   ? 4
+                                          : 2;
+}
+__host__ __device__ constexpr bool plan_ok(int L, int T) {
+  if (T <= 0 || L % T) return false;
+  int E = L / T, rem = L;
+  while (rem > 1) {
+    int R = pick_radix_fwd(rem, E);
+    if (rem % R || E % R) return false;
+    rem /= R;
+  }
+  return true;
+}
+
 // ---- twiddle tables -----------------------------------------------------------
 // Powers of two 16..8192 at [L-16, 2L-16); 3*2^k lengths 48..6144 after them.
 constexpr int TW_POW2_END = 2 * 8192 - 16;
@@ -47,6 +66,51 @@ static int upload_twiddles_this_tu() {
   return e == cudaSuccess ? 0 : -3;
 }
 static int g_tw_registered = register_twiddle_uploader(&upload_twiddles_this_tu);
+
+// ---- per-stage twiddle tables --------------------------------------------------
+// For a line FFT of length L with E elements per thread, stage s (radix R, stride NS)
+// needs W_L^{r*k*L/(NS*R)} for r = 1..R-1, k = 0..NS-1. The tables store them as
+// [stage][r-1][k]: threads of a warp read consecutive k, so the loads are conflict free
+// (reading the plain table at index r*k*stride serialises on shared-memory banks).
+__host__ __device__ constexpr int stw_e(int i) { return i == 0 ? 8 : i == 1 ? 12 : i == 2 ? 16 : 24; }
+__host__ __device__ constexpr int stw_len(int L, int E) {  // entries of one (L, E) table
+  int n = 0, rem = L, NS = 1;
+  while (rem > 1) {
+    int R = pick_radix_fwd(rem, E);
+    n += (R - 1) * NS;
+    NS *= R;
+    rem /= R;
+  }
+  return n;
+}
+__host__ __device__ constexpr bool stw_ok(int L, int E) { return supported_len(L) && L % E == 0 && plan_ok(L, L / E); }
+__host__ __device__ constexpr int stw_offset(int L, int E) {  // position of (L, E) in g_stw
+  int off = 0;
+  for (int L2 = 16; L2 <= 8192; L2 *= 2)
+    for (int e = 0; e < 4; e++) {
+      if (L2 == L && stw_e(e) == E) return off;
+      if (stw_ok(L2, stw_e(e))) off += stw_len(L2, stw_e(e));
+    }
+  for (int L2 = 48; L2 <= 6144; L2 *= 2)
+    for (int e = 0; e < 4; e++) {
+      if (L2 == L && stw_e(e) == E) return off;
+      if (stw_ok(L2, stw_e(e))) off += stw_len(L2, stw_e(e));
+    }
+  return off;  // total size when (L, E) is not a table
+}
+constexpr int STW_TOTAL = stw_offset(0, 0);
+static __device__ float2 g_stw[STW_TOTAL];
+void fill_stage_twiddle_host(float2* host);  // STW_TOTAL entries
+static int upload_stage_twiddles_this_tu() {
+  static float2* host = nullptr;
+  if (!host) {
+    host = new float2[STW_TOTAL];
+    fill_stage_twiddle_host(host);
+  }
+  cudaError_t e = cudaMemcpyToSymbol(g_stw, host, sizeof(float2) * STW_TOTAL);
+  return e == cudaSuccess ? 0 : -3;
+}
+static int g_stw_registered = register_twiddle_uploader(&upload_stage_twiddles_this_tu);
 
 // ---- shared-memory addressing: one pad slot every 16 entries -------------------
 __device__ __forceinline__ int sidx(int a) { return a + (a >> 4); }
@@ -149,27 +213,13 @@ __device__ __forceinline__ void dft(float2* v) {
 }
 
 // ---- radix choice ---------------------------------------------------------------
-__host__ __device__ constexpr int pick_radix(int rem, int E) {
-  return (rem % 3 == 0 && E % 3 == 0)      ? 3
-         : (rem % 16 == 0 && E % 16 == 0) ? 16
-         : (rem % 8 == 0 && E % 8 == 0)   ? 8
-         : (rem % 4 == 0 && E % 4 == 0)   ? 4
-                                          : 2;
-}
-__host__ __device__ constexpr bool plan_ok(int L, int T) {
-  if (L % T) return false;
-  int E = L / T, rem = L;
-  while (rem > 1) {
-    int R = pick_radix(rem, E);
-    if (rem % R || E % R) return false;
-    rem /= R;
-  }
-  return true;
-}
+__host__ __device__ constexpr int pick_radix(int rem, int E) { return pick_radix_fwd(rem, E); }
 
 // ---- one Stockham stage ---------------------------------------------------------
 template <int L, int T, int C, int R, int NS, bool INV, int TS>
 __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2* tw) {
+  // TS > 0: plain table exp(-2 pi i m/(L*TS)) read at stride TS; TS == 0: stage table
+  // [r-1][k] of this stage (tw points at the stage's first entry)
   constexpr int E = L / T, NB = E / R, LR = L / R;
   float2 v[NB][R];
 #pragma unroll
@@ -186,7 +236,7 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2*
     if constexpr (NS > 1) {
 #pragma unroll
       for (int r = 1; r < R; r++) {
-        float2 w = tw[r * k * (L / (NS * R)) * TS];
+        float2 w = (TS > 0) ? tw[r * k * (L / (NS * R)) * TS] : tw[(r - 1) * NS + k];
         if (INV) w.y = -w.y;
         v[b][r] = cmul(v[b][r], w);
       }
@@ -205,7 +255,8 @@ __device__ __forceinline__ void fft_stages(float2* s, int c, int t, const float2
     constexpr int R = pick_radix(L / NS, L / T);
     static_assert((L / NS) % R == 0 && (L / T) % R == 0, "bad radix plan");
     fft_stage<L, T, C, R, NS, INV, TS>(s, c, t, tw);
-    fft_stages<L, T, C, INV, NS * R, TS>(s, c, t, tw);
+    // stage tables: the next stage's entries follow this stage's (R-1)*NS entries
+    fft_stages<L, T, C, INV, NS * R, TS>(s, c, t, TS > 0 ? tw : tw + (R - 1) * NS);
   }
 }
 
@@ -224,6 +275,19 @@ __device__ __forceinline__ void line_fft_tw(float2* s, int lt, const float2* tw_
   static_assert(supported_len(L) && LT % L == 0, "unsupported FFT length / table");
   static_assert(plan_ok(L, T), "L/T must be divisible by every radix");
   fft_stages<L, T, C, INV, 1, LT / L>(s, lt % C, lt / C, tw_smem);
+}
+// Line FFT with per-stage twiddle tables (g_stw layout) staged in shared memory by
+// stage_stage_twiddles<L, L/T>.
+template <int L, int T, int C, bool INV>
+__device__ __forceinline__ void line_fft_st(float2* s, int lt, const float2* stw_smem) {
+  static_assert(supported_len(L) && plan_ok(L, T) && stw_ok(L, L / T), "no stage table for this plan");
+  fft_stages<L, T, C, INV, 1, 0>(s, lt % C, lt / C, stw_smem);
+}
+template <int L, int E>
+__device__ __forceinline__ void stage_stage_twiddles(float2* dst, int tid, int nthreads) {
+  static_assert(stw_ok(L, E), "no stage table for this plan");
+  const float2* g = g_stw + stw_offset(L, E);
+  for (int i = tid; i < stw_len(L, E); i += nthreads) dst[i] = g[i];
 }
 // Stage the exp(-2 pi i m / LT) table into shared memory (all threads of the block).
 template <int LT>

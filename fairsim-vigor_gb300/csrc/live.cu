@@ -60,6 +60,8 @@ __global__ void __launch_bounds__(LCfg<N>::GA* LCfg<N>::TN) k_live_a(const JobDe
   const int g = threadIdx.x / T, t = threadIdx.x % T;
   const int y = blockIdx.x * G + g;
   __shared__ float2 sm[G * smem_line_elems(N, 1)];
+  __shared__ float2 tw[stw_len(N, E)];
+  stage_stage_twiddles<N, E>(tw, threadIdx.x, G * T);
   float2* s = sm + g * smem_line_elems(N, 1);
   const size_t frame = (size_t)N * N, row = (size_t)y * N;
   const float* rawf = (const float*)J.raw;
@@ -97,7 +99,7 @@ __global__ void __launch_bounds__(LCfg<N>::GA* LCfg<N>::TN) k_live_a(const JobDe
         s[sidx(x)] = z;
       }
       __syncthreads();
-      line_fft<N, T, 1, false>(s, t);
+      line_fft_st<N, T, 1, false>(s, t, tw);
       float2* X = J.I + (size_t)(a * nC + c) * frame + row;
 #pragma unroll
       for (int i = 0; i < E; i++) X[t + i * T] = s[sidx(t + i * T)];
@@ -114,6 +116,8 @@ __global__ void __launch_bounds__(LCfg<N>::CBL* LCfg<N>::TN) k_live_b(const JobD
   const int lt = threadIdx.x, lane = lt % C, t = lt / C;
   const int x = blockIdx.x * C + lane;
   __shared__ float2 s[smem_line_elems(N, C)];
+  __shared__ float2 tw[stw_len(N, E)];
+  stage_stage_twiddles<N, E>(tw, lt, C * T);
   const size_t frame = (size_t)N * N;
   for (int a = 0; a < J.nA; a++)
     for (int c = 0; c < J.nC; c++) {
@@ -124,7 +128,7 @@ __global__ void __launch_bounds__(LCfg<N>::CBL* LCfg<N>::TN) k_live_b(const JobD
         s[sidx(k * C + lane)] = X[(size_t)k * N + x];
       }
       __syncthreads();
-      line_fft<N, T, C, false>(s, lt);
+      line_fft_st<N, T, C, false>(s, lt, tw);
       // times conj(OTF): the OTF vector is real (estimate), conj(OTF)*v = (v.re*o, v.im*o)
 #pragma unroll
       for (int i = 0; i < E; i++) {
@@ -135,7 +139,7 @@ __global__ void __launch_bounds__(LCfg<N>::CBL* LCfg<N>::TN) k_live_b(const JobD
       }
       __syncthreads();
       if (c > 0) {
-        line_fft<N, T, C, true>(s, lt);
+        line_fft_st<N, T, C, true>(s, lt, tw);
         const float2* ry = J.ramps + (size_t)(a * J.nC + c) * 2 * N + N;
 #pragma unroll
         for (int i = 0; i < E; i++) {
@@ -143,7 +147,7 @@ __global__ void __launch_bounds__(LCfg<N>::CBL* LCfg<N>::TN) k_live_b(const JobD
           s[sidx(k * C + lane)] = cmul(s[sidx(k * C + lane)], __ldg(&ry[k]));
         }
         __syncthreads();
-        line_fft<N, T, C, false>(s, lt);
+        line_fft_st<N, T, C, false>(s, lt, tw);
       }
 #pragma unroll
       for (int i = 0; i < E; i++) {
@@ -163,6 +167,9 @@ __global__ void __launch_bounds__(LCfg<N>::TW) k_live_c(const JobDesc* __restric
   const int Y = blockIdx.x, t = threadIdx.x;
   __shared__ float2 acc[smem_line_elems(W, 1)];
   __shared__ float2 s[smem_line_elems(N, 1)];
+  __shared__ float2 twN[stw_len(N, EN)], twW[stw_len(W, EW)];
+  stage_stage_twiddles<N, EN>(twN, t, TW);
+  stage_stage_twiddles<W, EW>(twW, t, TW);
 #pragma unroll
   for (int i = 0; i < EW; i++) acc[sidx(t + i * TW)] = make_float2(0.f, 0.f);
   const size_t frame = (size_t)N * N;
@@ -176,7 +183,7 @@ __global__ void __launch_bounds__(LCfg<N>::TW) k_live_c(const JobDesc* __restric
       for (int i = 0; i < EN; i++) s[sidx(t + i * TW)] = X[t + i * TW];
       __syncthreads();
       if (c > 0) {
-        line_fft<N, TW, 1, true>(s, t);
+        line_fft_st<N, TW, 1, true>(s, t, twN);
         const float2* rx = J.ramps + (size_t)(a * J.nC + c) * 2 * N;
 #pragma unroll
         for (int i = 0; i < EN; i++) {
@@ -184,7 +191,7 @@ __global__ void __launch_bounds__(LCfg<N>::TW) k_live_c(const JobDesc* __restric
           s[sidx(k)] = cmul(s[sidx(k)], __ldg(&rx[k]));
         }
         __syncthreads();
-        line_fft<N, TW, 1, false>(s, t);
+        line_fft_st<N, TW, 1, false>(s, t, twN);
       }
       // pasteFreq at (xInt, yInt) and fullResult.add
 #pragma unroll
@@ -208,7 +215,7 @@ __global__ void __launch_bounds__(LCfg<N>::TW) k_live_c(const JobDesc* __restric
     o = make_float2(o.x * f, o.y * f);
   }
   __syncthreads();
-  line_fft<W, TW, 1, true>(acc, t);
+  line_fft_st<W, TW, 1, true>(acc, t, twW);
   float2* O = J.O + (size_t)Y * W;
 #pragma unroll
   for (int i = 0; i < EW; i++) O[t + i * TW] = acc[sidx(t + i * TW)];
@@ -223,13 +230,15 @@ __global__ void __launch_bounds__(LCfg<N>::CD* LCfg<N>::TW) k_live_d(const JobDe
   const int lt = threadIdx.x, lane = lt % C, t = lt / C;
   const int X = blockIdx.x * C + lane;
   extern __shared__ float2 s[];
+  __shared__ float2 tw[stw_len(W, EW)];
+  stage_stage_twiddles<W, EW>(tw, lt, C * TW);
 #pragma unroll
   for (int i = 0; i < EW; i++) {
     const int k = t + i * TW;
     s[sidx(k * C + lane)] = J.O[(size_t)k * W + X];
   }
   __syncthreads();
-  line_fft<W, TW, C, true>(s, lt);
+  line_fft_st<W, TW, C, true>(s, lt, tw);
   const float scale = 1.f / ((float)W * (float)W);
 #pragma unroll
   for (int i = 0; i < EW; i++) {

@@ -78,13 +78,14 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
   int k = 0;
   while (k < n) {
     const Plan* p0 = static_cast<const Plan*>(jobs[order[k]].plan);
-    int e = k, maxA = 0;
+    int e = k, maxA = 0, maxP = 0;
     while (e < n && key(order[e]) == key(order[k])) {
       maxA = std::max(maxA, static_cast<const Plan*>(jobs[order[e]].plan)->prm.nr_dirs);
+      maxP = std::max(maxP, static_cast<const Plan*>(jobs[order[e]].plan)->prm.nr_phases);
       e++;
     }
     int rc = (p0->path == FSIM_PATH_LIVE) ? launch_live_size(p0->prm.w, d_table + k, e - k, maxA, st)
-                                          : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, st);
+                                          : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxP, st);
     if (rc) return rc;
     k = e;
   }

@@ -48,45 +48,63 @@ struct Cfg {
 };
 
 // ---- pass A ------------------------------------------------------------------------------
+// Copies a job descriptor into shared memory once per block (the passes read its fields
+// after global stores, which would otherwise force reloads).
+__device__ __forceinline__ void load_job(JobDesc* dst, const JobDesc* src, int tid, int nthreads) {
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int i = tid; i < (int)(sizeof(JobDesc) / sizeof(int)); i += nthreads) d[i] = s[i];
+}
+
 template <int N>
 __global__ void __launch_bounds__(Cfg<N>::T, (Cfg<N>::T <= 64 ? 8 : 4)) k_pass_a(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N>;
   constexpr int W = P::W, T = P::T, EN = N / T, EW = W / T;
-  const JobDesc& J = jobs[blockIdx.z];
   const int y = blockIdx.x, a = blockIdx.y, t = threadIdx.x;
-  if (a >= J.nA) return;  // uniform per block
+  __shared__ JobDesc J;
   __shared__ float2 s[smem_line_elems(W, 1)];
-  __shared__ float2 tw[W];
-  stage_twiddles<W>(tw, t, T);
+  __shared__ float2 twN[stw_len(N, EN)], twW[stw_len(W, EW)];
+  __shared__ float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
+  extern __shared__ float rows[];  // nP raw rows of this image row, damped
+  load_job(&J, jobs + blockIdx.z, t, T);
+  stage_stage_twiddles<N, EN>(twN, t, T);
+  stage_stage_twiddles<W, EW>(twW, t, T);
+  __syncthreads();
+  if (a >= J.nA) return;  // uniform per block
   const int nP = J.nP, nC = J.nC;
-  const size_t frame = (size_t)N * N;
-  const float* rawf = (const float*)J.raw;
-  const uint16_t* rawu = (const uint16_t*)J.raw;
-  const size_t row = (size_t)y * N;
-  for (int c = 0; c < nC; c++) {
-    const float2* coef = J.coef + (a * nC + c) * nP;
-    // band mix of the raw rows (background clip, border damping), re-read from L1 per component
+  for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
+  const size_t frame = (size_t)N * N, row = (size_t)y * N;
+  for (int p = 0; p < nP; p++) {
+    const size_t base = (size_t)(a * nP + p) * frame + row;
 #pragma unroll
     for (int i = 0; i < EN; i++) {
       const int x = t + i * T;
-      const float dmp = J.damp ? __ldg(&J.damp[row + x]) : 1.f;
+      float v = J.input_u16 ? (float)((const uint16_t*)J.raw)[base + x] : ((const float*)J.raw)[base + x];
+      if (J.bgr != 0.f) {
+        v = v - J.bgr;
+        if (v < 0) v = 0;
+      }
+      if (J.damp) v = v * J.damp[row + x];
+      rows[p * N + x] = v;
+    }
+  }
+  __syncthreads();
+  for (int c = 0; c < nC; c++) {
+    // band mix of the raw rows in real space
+#pragma unroll
+    for (int i = 0; i < EN; i++) {
+      const int x = t + i * T;
       float2 z = make_float2(0.f, 0.f);
       for (int p = 0; p < nP; p++) {
-        const size_t at = (size_t)(a * nP + p) * frame + row + x;
-        float v = J.input_u16 ? (float)__ldg(&rawu[at]) : __ldg(&rawf[at]);
-        if (J.bgr != 0.f) {
-          v = v - J.bgr;
-          if (v < 0) v = 0;
-        }
-        v = v * dmp;
-        const float2 m = coef[p];
+        const float2 m = coef[c * nP + p];
+        const float v = rows[p * N + x];
         z.x += m.x * v;
         z.y += m.y * v;
       }
       s[sidx(x)] = z;
     }
     __syncthreads();
-    line_fft_tw<N, T, 1, false, W>(s, t, tw);
+    line_fft_st<N, T, 1, false>(s, t, twN);
     // paste along x: m < N/2 stays, m >= N/2 moves to m + N; the middle becomes zero
     float2 v[EN];
 #pragma unroll
@@ -100,7 +118,7 @@ __global__ void __launch_bounds__(Cfg<N>::T, (Cfg<N>::T <= 64 ? 8 : 4)) k_pass_a
     }
     __syncthreads();
     if (c > 0) {
-      line_fft_tw<W, T, 1, true, W>(s, t, tw);
+      line_fft_st<W, T, 1, true>(s, t, twW);
       const float2* rx = J.ramps + (size_t)(a * nC + c) * 2 * W;
 #pragma unroll
       for (int i = 0; i < EW; i++) {
@@ -108,7 +126,7 @@ __global__ void __launch_bounds__(Cfg<N>::T, (Cfg<N>::T <= 64 ? 8 : 4)) k_pass_a
         s[sidx(k)] = cmul(s[sidx(k)], __ldg(&rx[k]));
       }
       __syncthreads();
-      line_fft_tw<W, T, 1, false, W>(s, t, tw);
+      line_fft_st<W, T, 1, false>(s, t, twW);
     }
     // keep the OTF-support window: columns Xs .. Xs+nWin-1 (mod W), quad layout
     const int Xs = J.win[2 * (a * nC + c)];
@@ -127,14 +145,17 @@ template <int N>
 __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T, (Cfg<N>::CB * Cfg<N>::T <= 256 ? 2 : 1)) k_pass_b(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N>;
   constexpr int W = P::W, T = P::T, CB = P::CB, EN = N / T, EW = W / T;
-  const JobDesc& J = jobs[blockIdx.y];
   const int q = blockIdx.x;  // column group: X = q*CB + lane
   const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
+  __shared__ JobDesc J;
+  __shared__ float2 twN[stw_len(N, EN)], twW[stw_len(W, EW)];
   extern __shared__ float2 sm[];
   float2* acc = sm;
   float2* wk = sm + smem_line_elems(W, CB);
-  float2* tw = wk + smem_line_elems(W, CB);
-  stage_twiddles<W>(tw, lt, CB * T);
+  load_job(&J, jobs + blockIdx.y, lt, CB * T);
+  stage_stage_twiddles<N, EN>(twN, lt, CB * T);
+  stage_stage_twiddles<W, EW>(twW, lt, CB * T);
+  __syncthreads();
   const int nC = J.nC, nWin = J.nWin;
 #pragma unroll
   for (int i = 0; i < EW; i++) acc[sidx((t + i * T) * CB + lane)] = make_float2(0.f, 0.f);
@@ -162,7 +183,7 @@ __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T, (Cfg<N>::CB * Cfg<N>::T
         wk[sidx(k * CB + lane)] = v;
       }
       __syncthreads();
-      line_fft_tw<N, T, CB, false, W>(wk, lt, tw);
+      line_fft_st<N, T, CB, false>(wk, lt, twN);
       float2 v[EN];
 #pragma unroll
       for (int i = 0; i < EN; i++) v[i] = wk[sidx((t + i * T) * CB + lane)];
@@ -175,7 +196,7 @@ __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T, (Cfg<N>::CB * Cfg<N>::T
       }
       __syncthreads();
       if (c > 0) {
-        line_fft_tw<W, T, CB, true, W>(wk, lt, tw);
+        line_fft_st<W, T, CB, true>(wk, lt, twW);
         const float2* ry = J.ramps + (size_t)(a * nC + c) * 2 * W + W;
 #pragma unroll
         for (int i = 0; i < EW; i++) {
@@ -183,7 +204,7 @@ __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T, (Cfg<N>::CB * Cfg<N>::T
           wk[sidx(k * CB + lane)] = cmul(wk[sidx(k * CB + lane)], __ldg(&ry[k]));
         }
         __syncthreads();
-        line_fft_tw<W, T, CB, false, W>(wk, lt, tw);
+        line_fft_st<W, T, CB, false>(wk, lt, twW);
       }
       // times conj(OTF) inside the window rows, accumulate
       const int Ys = J.win[2 * (aw * nC + c) + 1];
@@ -212,7 +233,7 @@ __global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T, (Cfg<N>::CB * Cfg<N>::T
     o.y *= f;
   }
   __syncthreads();
-  line_fft_tw<W, T, CB, true, W>(acc, lt, tw);
+  line_fft_st<W, T, CB, true>(acc, lt, twW);
 #pragma unroll
   for (int i = 0; i < EW; i++) {
     const int k = t + i * T;
@@ -229,14 +250,14 @@ __global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::T) k_pass_c(const JobDesc*
   const int g = threadIdx.x / T, t = threadIdx.x % T;
   const int Y = blockIdx.x * G + g;
   __shared__ float2 sm[G * smem_line_elems(W, 1)];
-  __shared__ float2 tw[W];
-  stage_twiddles<W>(tw, threadIdx.x, G * T);
+  __shared__ float2 tw[stw_len(W, EW)];
+  stage_stage_twiddles<W, EW>(tw, threadIdx.x, G * T);
   float2* s = sm + g * smem_line_elems(W, 1);
   const float2* row = J.O + (size_t)Y * W;
 #pragma unroll
   for (int i = 0; i < EW; i++) s[sidx(t + i * T)] = row[t + i * T];
   __syncthreads();
-  line_fft_tw<W, T, 1, true, W>(s, t, tw);
+  line_fft_st<W, T, 1, true>(s, t, tw);
   const float scale = 1.f / ((float)W * (float)W);
   float* out = J.out + (size_t)Y * W;
 #pragma unroll
@@ -433,18 +454,20 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws
 
 // ---- launch --------------------------------------------------------------------------------------
 template <int N>
-static int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st) {
+static int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st) {
   cudaEvent_t* ev = profile_events();
   using P = Cfg<N>;
   constexpr int W = P::W;
   static bool attr = false;
-  const size_t smem_b = sizeof(float2) * (2 * smem_line_elems(W, P::CB) + W);
+  const size_t smem_b = sizeof(float2) * (2 * smem_line_elems(W, P::CB));
   if (!attr) {
     FSIM_CUDA(cudaFuncSetAttribute(k_pass_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
+    FSIM_CUDA(cudaFuncSetAttribute(k_pass_a<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(float) * FSIM_MAX_PHASES * N)));
     attr = true;
   }
   if (ev) cudaEventRecord(ev[0], st);
-  k_pass_a<N><<<dim3(N, maxA, njobs), P::T, 0, st>>>(d_jobs);
+  k_pass_a<N><<<dim3(N, maxA, njobs), P::T, sizeof(float) * maxP * N, st>>>(d_jobs);
   if (ev) cudaEventRecord(ev[1], st);
   k_pass_b<N><<<dim3(W / P::CB, njobs), P::CB * P::T, smem_b, st>>>(d_jobs);
   if (ev) cudaEventRecord(ev[2], st);
@@ -470,11 +493,11 @@ bool offline_size_supported(int n) {
   }
 }
 
-int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st) {
+int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st) {
   switch (n) {
 #define CASE(v) \
   case v:       \
-    return launch_offline<v>(d_jobs, njobs, maxA, st);
+    return launch_offline<v>(d_jobs, njobs, maxA, maxP, st);
     FSIM_RECON_SIZES(CASE)
 #undef CASE
   }

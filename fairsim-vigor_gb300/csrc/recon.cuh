@@ -63,7 +63,7 @@ void profile_mark(int n_passes);
 
 bool offline_size_supported(int n);
 bool live_size_supported(int n);
-int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);
+int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st);
 int launch_live_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);
 
 }  // namespace fsim

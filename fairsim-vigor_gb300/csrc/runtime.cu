@@ -37,6 +37,29 @@ void fill_twiddle_host(float2* h) {
   for (int L = 48; L <= 6144; L *= 2) fill(L);
 }
 
+void fill_stage_twiddle_host(float2* h) {
+  auto fill = [&](int L) {
+    for (int e = 0; e < 4; e++) {
+      const int E = stw_e(e);
+      if (!stw_ok(L, E)) continue;
+      float2* t = h + stw_offset(L, E);
+      int rem = L, NS = 1, pos = 0;
+      while (rem > 1) {
+        const int R = pick_radix_fwd(rem, E);
+        for (int r = 1; r < R; r++)
+          for (int k = 0; k < NS; k++) {
+            double a = -2.0 * M_PI * (double)r * (double)k / ((double)NS * R);
+            t[pos++] = make_float2((float)std::cos(a), (float)std::sin(a));
+          }
+        NS *= R;
+        rem /= R;
+      }
+    }
+  };
+  for (int L = 16; L <= 8192; L *= 2) fill(L);
+  for (int L = 48; L <= 6144; L *= 2) fill(L);
+}
+
 static std::vector<tw_upload_fn>& uploaders() {
   static std::vector<tw_upload_fn> v;
   return v;
