@@ -72,7 +72,8 @@ static int g_tw_registered = register_twiddle_uploader(&upload_twiddles_this_tu)
 // needs W_L^{r*k*L/(NS*R)} for r = 1..R-1, k = 0..NS-1. The tables store them as
 // [stage][r-1][k]: threads of a warp read consecutive k, so the loads are conflict free
 // (reading the plain table at index r*k*stride serialises on shared-memory banks).
-__host__ __device__ constexpr int stw_e(int i) { return i == 0 ? 8 : i == 1 ? 12 : i == 2 ? 16 : 24; }
+constexpr int STW_NE = 6;
+__host__ __device__ constexpr int stw_e(int i) { return i == 0 ? 4 : i == 1 ? 6 : i == 2 ? 8 : i == 3 ? 12 : i == 4 ? 16 : 24; }
 __host__ __device__ constexpr int stw_len(int L, int E) {  // entries of one (L, E) table
   int n = 0, rem = L, NS = 1;
   while (rem > 1) {
@@ -87,12 +88,12 @@ __host__ __device__ constexpr bool stw_ok(int L, int E) { return supported_len(L
 __host__ __device__ constexpr int stw_offset(int L, int E) {  // position of (L, E) in g_stw
   int off = 0;
   for (int L2 = 16; L2 <= 8192; L2 *= 2)
-    for (int e = 0; e < 4; e++) {
+    for (int e = 0; e < STW_NE; e++) {
       if (L2 == L && stw_e(e) == E) return off;
       if (stw_ok(L2, stw_e(e))) off += stw_len(L2, stw_e(e));
     }
   for (int L2 = 48; L2 <= 6144; L2 *= 2)
-    for (int e = 0; e < 4; e++) {
+    for (int e = 0; e < STW_NE; e++) {
       if (L2 == L && stw_e(e) == E) return off;
       if (stw_ok(L2, stw_e(e))) off += stw_len(L2, stw_e(e));
     }

@@ -193,6 +193,20 @@ int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t w
   return FSIM_OK;
 }
 
+int fsim_tune_set(int n, int path, int pass, int variant) {
+  FSIM_REQUIRE(path == FSIM_PATH_OFFLINE, FSIM_EINVAL, "tune: only the offline passes have variants");
+  return offline_tune_set(n, pass, variant);
+}
+
+int fsim_tune_get(int n, int path, int pass, int* variant, int* n_variants) {
+  FSIM_REQUIRE(variant && n_variants, FSIM_EINVAL, "tune_get: bad arguments");
+  FSIM_REQUIRE(path == FSIM_PATH_OFFLINE && pass >= 0 && pass <= 1, FSIM_EINVAL, "tune_get: bad path/pass");
+  *variant = offline_tune_get(n, pass);
+  *n_variants = offline_variants(pass);
+  FSIM_REQUIRE(*variant >= 0, FSIM_EINVAL, "tune_get: unsupported size %d", n);
+  return FSIM_OK;
+}
+
 int fsim_profile_enable(int on) {
   NEED_INIT();
   if (on && !g_prof_ev[0])

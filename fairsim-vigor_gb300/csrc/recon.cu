@@ -30,239 +30,13 @@
 #include "filters.cuh"
 #include "otf.cuh"
 #include "recon.cuh"
+#include "recon_kernels.cuh"
 #include "runtime.cuh"
 #include "sim_host.h"
 
 namespace fsim {
 
 std::vector<float> fade_vector(int w, int h, int px);
-
-// ---- per-size launch configuration -------------------------------------------------------
-template <int N>
-struct Cfg {
-  static constexpr int W = 2 * N;
-  static constexpr int EW = (N % 3 == 0) ? 24 : 16;  // elements per thread in W-length lines
-  static constexpr int T = W / EW;                    // threads per line
-  static constexpr int CB = (N >= 2048) ? 2 : 4;      // interleaved columns in pass B
-  static constexpr int GC = (T >= 128) ? 1 : (128 / T);  // rows per block in pass C
-};
-
-// ---- pass A ------------------------------------------------------------------------------
-// Copies a job descriptor into shared memory once per block (the passes read its fields
-// after global stores, which would otherwise force reloads).
-__device__ __forceinline__ void load_job(JobDesc* dst, const JobDesc* src, int tid, int nthreads) {
-  const int* s = reinterpret_cast<const int*>(src);
-  int* d = reinterpret_cast<int*>(dst);
-  for (int i = tid; i < (int)(sizeof(JobDesc) / sizeof(int)); i += nthreads) d[i] = s[i];
-}
-
-template <int N>
-__global__ void __launch_bounds__(Cfg<N>::T, (Cfg<N>::T <= 64 ? 8 : 4)) k_pass_a(const JobDesc* __restrict__ jobs) {
-  using P = Cfg<N>;
-  constexpr int W = P::W, T = P::T, EN = N / T, EW = W / T;
-  const int y = blockIdx.x, a = blockIdx.y, t = threadIdx.x;
-  __shared__ JobDesc J;
-  __shared__ float2 s[smem_line_elems(W, 1)];
-  __shared__ float2 twN[stw_len(N, EN)], twW[stw_len(W, EW)];
-  __shared__ float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
-  extern __shared__ float rows[];  // nP raw rows of this image row, damped
-  load_job(&J, jobs + blockIdx.z, t, T);
-  stage_stage_twiddles<N, EN>(twN, t, T);
-  stage_stage_twiddles<W, EW>(twW, t, T);
-  __syncthreads();
-  if (a >= J.nA) return;  // uniform per block
-  const int nP = J.nP, nC = J.nC;
-  for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
-  const size_t frame = (size_t)N * N, row = (size_t)y * N;
-  for (int p = 0; p < nP; p++) {
-    const size_t base = (size_t)(a * nP + p) * frame + row;
-#pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int x = t + i * T;
-      float v = J.input_u16 ? (float)((const uint16_t*)J.raw)[base + x] : ((const float*)J.raw)[base + x];
-      if (J.bgr != 0.f) {
-        v = v - J.bgr;
-        if (v < 0) v = 0;
-      }
-      if (J.damp) v = v * J.damp[row + x];
-      rows[p * N + x] = v;
-    }
-  }
-  __syncthreads();
-  for (int c = 0; c < nC; c++) {
-    // band mix of the raw rows in real space
-#pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int x = t + i * T;
-      float2 z = make_float2(0.f, 0.f);
-      for (int p = 0; p < nP; p++) {
-        const float2 m = coef[c * nP + p];
-        const float v = rows[p * N + x];
-        z.x += m.x * v;
-        z.y += m.y * v;
-      }
-      s[sidx(x)] = z;
-    }
-    __syncthreads();
-    line_fft_st<N, T, 1, false>(s, t, twN);
-    // paste along x: m < N/2 stays, m >= N/2 moves to m + N; the middle becomes zero
-    float2 v[EN];
-#pragma unroll
-    for (int i = 0; i < EN; i++) v[i] = s[sidx(t + i * T)];
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int m = t + i * T;
-      s[sidx(m < N / 2 ? m : m + N)] = v[i];
-      s[sidx(N / 2 + m)] = make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    if (c > 0) {
-      line_fft_st<W, T, 1, true>(s, t, twW);
-      const float2* rx = J.ramps + (size_t)(a * nC + c) * 2 * W;
-#pragma unroll
-      for (int i = 0; i < EW; i++) {
-        const int k = t + i * T;
-        s[sidx(k)] = cmul(s[sidx(k)], __ldg(&rx[k]));
-      }
-      __syncthreads();
-      line_fft_st<W, T, 1, false>(s, t, twW);
-    }
-    // keep the OTF-support window: columns Xs .. Xs+nWin-1 (mod W), quad layout
-    const int Xs = J.win[2 * (a * nC + c)];
-    float2* I = J.I + (size_t)(a * nC + c) * J.nWin * N;
-    for (int xl = t; xl < J.nWin; xl += T) {
-      int X = Xs + xl;
-      if (X >= W) X -= W;
-      I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = s[sidx(X)];
-    }
-    __syncthreads();
-  }
-}
-
-// ---- pass B ------------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(Cfg<N>::CB* Cfg<N>::T, (Cfg<N>::CB * Cfg<N>::T <= 256 ? 2 : 1)) k_pass_b(const JobDesc* __restrict__ jobs) {
-  using P = Cfg<N>;
-  constexpr int W = P::W, T = P::T, CB = P::CB, EN = N / T, EW = W / T;
-  const int q = blockIdx.x;  // column group: X = q*CB + lane
-  const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
-  __shared__ JobDesc J;
-  __shared__ float2 twN[stw_len(N, EN)], twW[stw_len(W, EW)];
-  extern __shared__ float2 sm[];
-  float2* acc = sm;
-  float2* wk = sm + smem_line_elems(W, CB);
-  load_job(&J, jobs + blockIdx.y, lt, CB * T);
-  stage_stage_twiddles<N, EN>(twN, lt, CB * T);
-  stage_stage_twiddles<W, EW>(twW, lt, CB * T);
-  __syncthreads();
-  const int nC = J.nC, nWin = J.nWin;
-#pragma unroll
-  for (int i = 0; i < EW; i++) acc[sidx((t + i * T) * CB + lane)] = make_float2(0.f, 0.f);
-  // components: band 0 of all angles shares the unshifted mask and is summed before its
-  // FFT; every shifted component is transformed on its own.
-  for (int a = -1; a < J.nA; a++) {
-    for (int c = (a < 0 ? 0 : 1); c < (a < 0 ? 1 : nC); c++) {
-      const int aw = a < 0 ? 0 : a;
-      int xl = q * CB - J.win[2 * (aw * nC + c)];
-      if (xl < 0) xl += W;
-      if (xl >= nWin) continue;  // uniform: the whole group is outside this window
-      const int qi = xl / 4, sub = xl & 3;
-      // load the window column(s), summing band 0 over angles
-#pragma unroll
-      for (int i = 0; i < EN; i++) {
-        const int k = t + i * T;
-        float2 v = make_float2(0.f, 0.f);
-        const int a0 = a < 0 ? 0 : a, a1 = a < 0 ? J.nA : a + 1;
-        for (int aa = a0; aa < a1; aa++) {
-          const float2* I = J.I + (size_t)(aa * nC + c) * nWin * N;
-          const float2 u = I[((size_t)qi * N + k) * 4 + sub + lane];
-          v.x += u.x;
-          v.y += u.y;
-        }
-        wk[sidx(k * CB + lane)] = v;
-      }
-      __syncthreads();
-      line_fft_st<N, T, CB, false>(wk, lt, twN);
-      float2 v[EN];
-#pragma unroll
-      for (int i = 0; i < EN; i++) v[i] = wk[sidx((t + i * T) * CB + lane)];
-      __syncthreads();
-#pragma unroll
-      for (int i = 0; i < EN; i++) {
-        const int m = t + i * T;
-        wk[sidx((m < N / 2 ? m : m + N) * CB + lane)] = v[i];
-        wk[sidx((N / 2 + m) * CB + lane)] = make_float2(0.f, 0.f);
-      }
-      __syncthreads();
-      if (c > 0) {
-        line_fft_st<W, T, CB, true>(wk, lt, twW);
-        const float2* ry = J.ramps + (size_t)(a * nC + c) * 2 * W + W;
-#pragma unroll
-        for (int i = 0; i < EW; i++) {
-          const int k = t + i * T;
-          wk[sidx(k * CB + lane)] = cmul(wk[sidx(k * CB + lane)], __ldg(&ry[k]));
-        }
-        __syncthreads();
-        line_fft_st<W, T, CB, false>(wk, lt, twW);
-      }
-      // times conj(OTF) inside the window rows, accumulate
-      const int Ys = J.win[2 * (aw * nC + c) + 1];
-      const float* mk = J.masks + (size_t)(aw * nC + c) * nWin * nWin;
-      for (int yl = t; yl < nWin; yl += T) {
-        int Y = Ys + yl;
-        if (Y >= W) Y -= W;
-        const float m = __ldg(&mk[((size_t)qi * nWin + yl) * 4 + sub + lane]);
-        const float2 u = wk[sidx(Y * CB + lane)];
-        float2& o = acc[sidx(Y * CB + lane)];
-        o.x += m * u.x;
-        o.y += m * u.y;
-      }
-      __syncthreads();
-    }
-  }
-  // Wiener denominator x apodization, then the inverse transform along y
-  const int X0 = q * CB;
-  const float* wa = J.wa + (size_t)(X0 / 4) * W * 4 + (X0 & 3);
-#pragma unroll
-  for (int i = 0; i < EW; i++) {
-    const int k = t + i * T;
-    const float f = __ldg(&wa[(size_t)k * 4 + lane]);
-    float2& o = acc[sidx(k * CB + lane)];
-    o.x *= f;
-    o.y *= f;
-  }
-  __syncthreads();
-  line_fft_st<W, T, CB, true>(acc, lt, twW);
-#pragma unroll
-  for (int i = 0; i < EW; i++) {
-    const int k = t + i * T;
-    J.O[(size_t)k * W + X0 + lane] = acc[sidx(k * CB + lane)];
-  }
-}
-
-// ---- pass C ------------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::T) k_pass_c(const JobDesc* __restrict__ jobs) {
-  using P = Cfg<N>;
-  constexpr int W = P::W, T = P::T, G = P::GC, EW = W / T;
-  const JobDesc& J = jobs[blockIdx.y];
-  const int g = threadIdx.x / T, t = threadIdx.x % T;
-  const int Y = blockIdx.x * G + g;
-  __shared__ float2 sm[G * smem_line_elems(W, 1)];
-  __shared__ float2 tw[stw_len(W, EW)];
-  stage_stage_twiddles<W, EW>(tw, threadIdx.x, G * T);
-  float2* s = sm + g * smem_line_elems(W, 1);
-  const float2* row = J.O + (size_t)Y * W;
-#pragma unroll
-  for (int i = 0; i < EW; i++) s[sidx(t + i * T)] = row[t + i * T];
-  __syncthreads();
-  line_fft_st<W, T, 1, true>(s, t, tw);
-  const float scale = 1.f / ((float)W * (float)W);
-  float* out = J.out + (size_t)Y * W;
-#pragma unroll
-  for (int i = 0; i < EW; i++) out[t + i * T] = s[sidx(t + i * T)].x * scale;
-}
 
 // ---- plan build kernels -------------------------------------------------------------------------
 // conj(OTF(r - k)) mask of one component over its window, quad layout [xl/4][yl][xl%4]
@@ -346,15 +120,21 @@ int Plan::build(cudaStream_t st) {
     for (int c = 0; c < nC; c++) {
       double kx, ky;
       comp_shift(&prm, a, c, &kx, &ky);
-      float2* rx = &ramps[(size_t)(a * nC + c) * 2 * W];
-      float2* ry = rx + W;
-      for (int n = 0; n < W; n++) {
-        // x: exp(+2 pi i kx n/W)/W ; y: exp(-2 pi i ky n/W)/W  (fourierShift(kx, -ky))
-        double fx = kx * n / W, fy = -ky * n / W;
-        fx -= std::floor(fx);
-        fy -= std::floor(fy);
-        rx[n] = make_float2((float)(std::cos(2 * M_PI * fx) / W), (float)(std::sin(2 * M_PI * fx) / W));
-        ry[n] = make_float2((float)(std::cos(2 * M_PI * fy) / W), (float)(std::sin(2 * M_PI * fy) / W));
+      // even/odd samples of the shift ramps on the W grid, the upsampling factors folded in:
+      // x: 0.5 exp(+2 pi i kx 2n/W), exp(+2 pi i kx (2n+1)/W)/W; y likewise with -ky
+      // (SimUtils.fourierShift multiplies exp(i 2 pi (kx x - ky y)/W), S/SimUtils.java:43-50)
+      float2* r = &ramps[(size_t)(a * nC + c) * 2 * W];
+      auto ph = [&](double k, int n) {
+        double f = k * n / W;
+        f -= std::floor(f);
+        return 2 * M_PI * f;
+      };
+      for (int n = 0; n < N; n++) {
+        const double e = ph(kx, 2 * n), o = ph(kx, 2 * n + 1), ey = ph(-ky, 2 * n), oy = ph(-ky, 2 * n + 1);
+        r[n] = make_float2((float)(0.5 * std::cos(e)), (float)(0.5 * std::sin(e)));
+        r[N + n] = make_float2((float)(std::cos(o) / W), (float)(std::sin(o) / W));
+        r[W + n] = make_float2((float)(0.5 * std::cos(ey)), (float)(0.5 * std::sin(ey)));
+        r[W + N + n] = make_float2((float)(std::cos(oy) / W), (float)(std::sin(oy) / W));
       }
       int xs, ys;
       if (nwin >= W) {
@@ -452,33 +232,33 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws
   j.O = (float2*)(ws + ((I + 255) & ~(size_t)255));
 }
 
-// ---- launch --------------------------------------------------------------------------------------
-template <int N>
-static int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st) {
-  cudaEvent_t* ev = profile_events();
-  using P = Cfg<N>;
-  constexpr int W = P::W;
-  static bool attr = false;
-  const size_t smem_b = sizeof(float2) * (2 * smem_line_elems(W, P::CB));
-  if (!attr) {
-    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
-    FSIM_CUDA(cudaFuncSetAttribute(k_pass_a<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)(sizeof(float) * FSIM_MAX_PHASES * N)));
-    attr = true;
-  }
-  if (ev) cudaEventRecord(ev[0], st);
-  k_pass_a<N><<<dim3(N, maxA, njobs), P::T, sizeof(float) * maxP * N, st>>>(d_jobs);
-  if (ev) cudaEventRecord(ev[1], st);
-  k_pass_b<N><<<dim3(W / P::CB, njobs), P::CB * P::T, smem_b, st>>>(d_jobs);
-  if (ev) cudaEventRecord(ev[2], st);
-  k_pass_c<N><<<dim3(W / P::GC, njobs), P::GC * P::T, 0, st>>>(d_jobs);
-  if (ev) {
-    cudaEventRecord(ev[3], st);
-    profile_mark(3);
-  }
-  FSIM_CHECK_LAUNCH();
+// ---- autotuned variants ------------------------------------------------------------------------
+int g_var_a[16] = {0}, g_var_b[16] = {0};
+// variant lists: pass A elements/thread {default, alternative}; pass B (elements, columns)
+//   pow2 sizes:  A {16, 8}      B {(16,4), (8,4), (16,2), (8,2)}
+//   3*2^k sizes: A {24, 12}     B {(24,4), (12,4), (24,2), (12,2)}
+int offline_variants(int pass) { return pass == 0 ? 2 : 4; }
+int offline_tune_set(int n, int pass, int v) {
+  int k = size_slot(n);
+  FSIM_REQUIRE(k >= 0 && pass >= 0 && pass <= 1 && v >= 0 && v < offline_variants(pass), FSIM_EINVAL,
+               "tune: bad size/pass/variant %d/%d/%d", n, pass, v);
+  (pass == 0 ? g_var_a : g_var_b)[k] = v;
   return FSIM_OK;
 }
+int offline_tune_get(int n, int pass) {
+  int k = size_slot(n);
+  return k < 0 ? -1 : (pass == 0 ? g_var_a : g_var_b)[k];
+}
+
+extern template int launch_offline<64>(const JobDesc*, int, int, int, cudaStream_t);
+extern template int launch_offline<128>(const JobDesc*, int, int, int, cudaStream_t);
+extern template int launch_offline<192>(const JobDesc*, int, int, int, cudaStream_t);
+extern template int launch_offline<256>(const JobDesc*, int, int, int, cudaStream_t);
+extern template int launch_offline<384>(const JobDesc*, int, int, int, cudaStream_t);
+extern template int launch_offline<512>(const JobDesc*, int, int, int, cudaStream_t);
+extern template int launch_offline<768>(const JobDesc*, int, int, int, cudaStream_t);
+extern template int launch_offline<1024>(const JobDesc*, int, int, int, cudaStream_t);
+extern template int launch_offline<2048>(const JobDesc*, int, int, int, cudaStream_t);
 
 #define FSIM_RECON_SIZES(X) X(64) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(2048)
 

@@ -62,6 +62,9 @@ cudaEvent_t* profile_events();
 void profile_mark(int n_passes);
 
 bool offline_size_supported(int n);
+int offline_variants(int pass);
+int offline_tune_set(int n, int pass, int v);
+int offline_tune_get(int n, int pass);
 bool live_size_supported(int n);
 int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st);
 int launch_live_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);

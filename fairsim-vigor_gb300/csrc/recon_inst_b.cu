@@ -1,0 +1,7 @@
+// Instantiations of the fused offline passes for sizes 512 (one translation unit per
+// group so the library builds in parallel).
+#include "recon_kernels.cuh"
+
+namespace fsim {
+template int launch_offline<512>(const JobDesc*, int, int, int, cudaStream_t);
+}  // namespace fsim

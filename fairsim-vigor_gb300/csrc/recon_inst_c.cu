@@ -1,0 +1,8 @@
+// Instantiations of the fused offline passes for sizes 768, 1024 (one translation unit per
+// group so the library builds in parallel).
+#include "recon_kernels.cuh"
+
+namespace fsim {
+template int launch_offline<768>(const JobDesc*, int, int, int, cudaStream_t);
+template int launch_offline<1024>(const JobDesc*, int, int, int, cudaStream_t);
+}  // namespace fsim

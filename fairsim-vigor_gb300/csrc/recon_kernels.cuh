@@ -1,0 +1,383 @@
+// Kernels of the fused offline reconstruction (templates instantiated per size in
+// recon_inst_*.cu). See recon.cu for the algorithm and the pass structure.
+//
+// Every 1D operation here is done with N-length line FFTs. The reference's shift of a
+// pasted N-point spectrum Z on the W = 2N grid, FFT_W(r * iFFT_W(paste(Z))), is evaluated
+// through its exact even/odd split: with u = iFFT_W(paste(Z)),
+//   u[2n]   = z[n] / 2                       (z = iFFT_N(Z), the line in real space)
+//   u[2n+1] = iFFT_N(Z * s)[n] / W,  s(m) = exp(+i pi m~/N), m~ the pasted signed frequency
+// so that, with E = FFT_N(r[2n] u[2n]) and O = FFT_N(r[2n+1] u[2n+1]),
+//   FFT_W(r * u)[X] = E[X mod N] + exp(-2 pi i X/W) O[X mod N].
+// The per-component ramps r (even and odd samples, 1/2 and 1/W folded in) are resident
+// tables; s and exp(-2 pi i X/W) come from the W-point twiddle table. The final inverse
+// FFT_W along y is folded the same way into two N-point inverse FFTs (even/odd rows).
+#pragma once
+
+#include "common.cuh"
+#include "fft_line.cuh"
+#include "filters.cuh"
+#include "otf.cuh"
+#include "recon.cuh"
+
+namespace fsim {
+
+// ---- launch configuration (variants picked per size by the autotuner) --------------------
+// ENV: elements per thread of the N-length lines (radix plan and threads per line follow);
+// CBV: interleaved columns per block in pass B.
+template <int N, int ENV = 0, int CBV = 0>
+struct Cfg {
+  static constexpr int W = 2 * N;
+  static constexpr int EN = ENV ? ENV : ((N % 3 == 0) ? 12 : 8);
+  static constexpr int T = N / EN;  // threads per line
+  static constexpr int CB = CBV ? CBV : 4;
+  static constexpr int EW = (N % 3 == 0) ? 24 : 16;  // pass C: W-length lines
+  static constexpr int TC = W / EW;
+  static constexpr int GC = (TC >= 128) ? 1 : (128 / TC);  // rows per block in pass C
+};
+
+// Copies a job descriptor into shared memory once per block (the passes read its fields
+// after global stores, which would otherwise force reloads).
+__device__ __forceinline__ void load_job(JobDesc* dst, const JobDesc* src, int tid, int nthreads) {
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int i = tid; i < (int)(sizeof(JobDesc) / sizeof(int)); i += nthreads) d[i] = s[i];
+}
+
+// exp(+i pi m~ / N) for the pasted signed frequency m~ of index m (m < N/2: m, else m - N)
+template <int N>
+__device__ __forceinline__ float2 half_shift(const float2* twW, int m) {
+  const int ms = m < N / 2 ? m : m - N;
+  return cconjf(twW[ms < 0 ? ms + 2 * N : ms]);
+}
+// source index in an N-point spectrum of output index X of pasteFreq onto 2N (or -1)
+template <int N>
+__device__ __forceinline__ int paste_src(int X) {
+  return X < N / 2 ? X : (X >= 3 * N / 2 ? X - N : -1);
+}
+
+// ---- pass A: rows ----------------------------------------------------------------------------
+template <int N, int ENV>
+__global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __restrict__ jobs) {
+  using P = Cfg<N, ENV>;
+  constexpr int W = P::W, T = P::T, EN = P::EN;
+  const int y = blockIdx.x, a = blockIdx.y, t = threadIdx.x;
+  __shared__ JobDesc J;
+  __shared__ float2 bz[smem_line_elems(N, 1)], bh[smem_line_elems(N, 1)], sv[N];
+  __shared__ float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
+  const float2* twN = g_stw + stw_offset(N, EN);  // stage table, read through L1
+  const float2* twW = g_tw + tw_offset(W);
+  load_job(&J, jobs + blockIdx.z, t, T);
+  __syncthreads();
+  if (a >= J.nA) return;  // uniform per block
+  const int nP = J.nP, nC = J.nC;
+  for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
+  __syncthreads();
+  const size_t frame = (size_t)N * N, row = (size_t)y * N;
+  // raw pixel of phase p at column x: background clip and border damping
+  auto px = [&](int p, int x) {
+    const size_t at = (size_t)(a * nP + p) * frame + row + x;
+    float v = J.input_u16 ? (float)__ldg((const uint16_t*)J.raw + at) : __ldg((const float*)J.raw + at);
+    if (J.bgr != 0.f) {
+      v = v - J.bgr;
+      if (v < 0) v = 0;
+    }
+    if (J.damp) v = v * __ldg(J.damp + row + x);
+    return v;
+  };
+  auto mix = [&](int cm, int x) {  // band separation in real space
+    float2 z = make_float2(0.f, 0.f);
+    for (int p = 0; p < nP; p++) {
+      const float2 m = coef[cm * nP + p];
+      const float v = px(p, x);
+      z.x += m.x * v;
+      z.y += m.y * v;
+    }
+    return z;
+  };
+  // Components: band 0, then per band b the pair neg = 2b-1, pos = 2b. The separation
+  // coefficients of a pair are exact complex conjugates in float, so z_pos = conj(z_neg)
+  // and FFT(z_pos)[m] = conj(FFT(z_neg)[-m]): one forward FFT serves both.
+  for (int b = 0; b < (nC + 1) / 2; b++) {
+    const int cm = b == 0 ? 0 : 2 * b - 1;
+#pragma unroll
+    for (int i = 0; i < EN; i++) {
+      const int x = t + i * T;
+      const float2 z = mix(cm, x);
+      bz[sidx(x)] = z;
+      bh[sidx(x)] = z;
+    }
+    __syncthreads();
+    line_fft_st<N, T, 1, false>(bh, t, twN);  // Z = FFT_N(z)
+    if (b == 0) {
+      // band 0: pasteFreq only; keep the OTF-support window in quad layout
+      const int Xs = J.win[2 * (a * nC)];
+      float2* I = J.I + (size_t)(a * nC) * J.nWin * N;
+      for (int xl = t; xl < J.nWin; xl += T) {
+        int X = Xs + xl;
+        if (X >= W) X -= W;
+        const int m = paste_src<N>(X);
+        I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = m >= 0 ? bh[sidx(m)] : make_float2(0.f, 0.f);
+      }
+      __syncthreads();
+      continue;
+    }
+#pragma unroll
+    for (int i = 0; i < EN; i++) sv[t + i * T] = bh[sidx(t + i * T)];
+    for (int k = 0; k < 2; k++) {
+      const int c = 2 * b - 1 + k;
+      if (k == 1) {  // pos: z = conj(z_neg), Z = mirrored conj(Z_neg)
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < EN; i++) {
+          const int m = t + i * T;
+          bz[sidx(m)] = cconjf(mix(cm, m));
+          bh[sidx(m)] = cconjf(sv[m == 0 ? 0 : N - m]);
+        }
+      }
+      // odd samples of the upsampled line: iFFT_N(Z * s)
+#pragma unroll
+      for (int i = 0; i < EN; i++) {
+        const int m = t + i * T;
+        bh[sidx(m)] = cmul(bh[sidx(m)], half_shift<N>(twW, m));
+      }
+      __syncthreads();
+      line_fft_st<N, T, 1, true>(bh, t, twN);
+      // times the even/odd ramp samples, forward transforms
+      const float2* re = J.ramps + (size_t)(a * nC + c) * 2 * W;
+      const float2* ro = re + N;
+#pragma unroll
+      for (int i = 0; i < EN; i++) {
+        const int m = t + i * T;
+        bz[sidx(m)] = cmul(bz[sidx(m)], __ldg(re + m));
+        bh[sidx(m)] = cmul(bh[sidx(m)], __ldg(ro + m));
+      }
+      __syncthreads();
+      line_fft_st<N, T, 1, false>(bz, t, twN);
+      line_fft_st<N, T, 1, false>(bh, t, twN);
+      // window of the shifted spectrum: E[X mod N] + exp(-2 pi i X/W) O[X mod N]
+      const int Xs = J.win[2 * (a * nC + c)];
+      float2* I = J.I + (size_t)(a * nC + c) * J.nWin * N;
+      for (int xl = t; xl < J.nWin; xl += T) {
+        int X = Xs + xl;
+        if (X >= W) X -= W;
+        const int m = X < N ? X : X - N;
+        const float2 e = bz[sidx(m)], o = bh[sidx(m)];
+        I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(e, cmul(twW[X], o));
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ---- pass B: columns ---------------------------------------------------------------------------
+template <int N, int ENV, int CBV>
+__global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_pass_b(const JobDesc* __restrict__ jobs) {
+  using P = Cfg<N, ENV, CBV>;
+  constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN;
+  const int q = blockIdx.x;  // column group: X = q*CB + lane
+  const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
+  __shared__ JobDesc J;
+  extern __shared__ float2 sm[];
+  float2* acc = sm;                                // W x CB
+  float2* bz = acc + smem_line_elems(W, CB);       // N x CB
+  float2* bh = bz + smem_line_elems(N, CB);        // N x CB
+  const float2* twN = g_stw + stw_offset(N, EN);
+  const float2* twW = g_tw + tw_offset(W);
+  load_job(&J, jobs + blockIdx.y, lt, CB * T);
+#pragma unroll
+  for (int i = 0; i < 2 * EN; i++) acc[sidx((t + i * T) * CB + lane)] = make_float2(0.f, 0.f);
+  __syncthreads();
+  const int nC = J.nC, nWin = J.nWin;
+  // components: band 0 of all angles shares the unshifted mask and is summed before its
+  // FFT; every shifted component is transformed on its own.
+  for (int a = -1; a < J.nA; a++) {
+    for (int c = (a < 0 ? 0 : 1); c < (a < 0 ? 1 : nC); c++) {
+      const int aw = a < 0 ? 0 : a;
+      int xl = q * CB - J.win[2 * (aw * nC + c)];
+      if (xl < 0) xl += W;
+      if (xl >= nWin) continue;  // uniform: the whole group is outside this window
+      const int qi = xl / 4, sub = xl & 3;
+#pragma unroll
+      for (int i = 0; i < EN; i++) {
+        const int k = t + i * T;
+        float2 v = make_float2(0.f, 0.f);
+        const int a0 = a < 0 ? 0 : a, a1 = a < 0 ? J.nA : a + 1;
+        for (int aa = a0; aa < a1; aa++) {
+          const float2 u = J.I[(size_t)(aa * nC + c) * nWin * N + ((size_t)qi * N + k) * 4 + sub + lane];
+          v.x += u.x;
+          v.y += u.y;
+        }
+        bz[sidx(k * CB + lane)] = v;
+        bh[sidx(k * CB + lane)] = v;
+      }
+      __syncthreads();
+      line_fft_st<N, T, CB, false>(bh, lt, twN);  // Z along y
+      const int Ys = J.win[2 * (aw * nC + c) + 1];
+      const float* mk = J.masks + (size_t)(aw * nC + c) * nWin * nWin + (size_t)qi * nWin * 4 + sub + lane;
+      if (c == 0) {
+        for (int yl = t; yl < nWin; yl += T) {
+          int Y = Ys + yl;
+          if (Y >= W) Y -= W;
+          const int m = paste_src<N>(Y);
+          if (m >= 0) {
+            const float f = __ldg(mk + (size_t)yl * 4);
+            const float2 u = bh[sidx(m * CB + lane)];
+            float2& o = acc[sidx(Y * CB + lane)];
+            o.x += f * u.x;
+            o.y += f * u.y;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < EN; i++) {
+          const int m = t + i * T;
+          bh[sidx(m * CB + lane)] = cmul(bh[sidx(m * CB + lane)], half_shift<N>(twW, m));
+        }
+        __syncthreads();
+        line_fft_st<N, T, CB, true>(bh, lt, twN);
+        const float2* re = J.ramps + (size_t)(a * nC + c) * 2 * W + W;  // y ramps
+        const float2* ro = re + N;
+#pragma unroll
+        for (int i = 0; i < EN; i++) {
+          const int m = t + i * T;
+          bz[sidx(m * CB + lane)] = cmul(bz[sidx(m * CB + lane)], __ldg(re + m));
+          bh[sidx(m * CB + lane)] = cmul(bh[sidx(m * CB + lane)], __ldg(ro + m));
+        }
+        __syncthreads();
+        line_fft_st<N, T, CB, false>(bz, lt, twN);
+        line_fft_st<N, T, CB, false>(bh, lt, twN);
+        for (int yl = t; yl < nWin; yl += T) {
+          int Y = Ys + yl;
+          if (Y >= W) Y -= W;
+          const int m = Y < N ? Y : Y - N;
+          const float f = __ldg(mk + (size_t)yl * 4);
+          const float2 u = cadd(bz[sidx(m * CB + lane)], cmul(twW[Y], bh[sidx(m * CB + lane)]));
+          float2& o = acc[sidx(Y * CB + lane)];
+          o.x += f * u.x;
+          o.y += f * u.y;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // Wiener denominator x apodization, then iFFT_W along y as two N-point inverse FFTs:
+  //   out[2n] = iFFT_N(A[k] + A[k+N]),  out[2n+1] = iFFT_N((A[k] - A[k+N]) exp(i pi k/N))
+  const int X0 = q * CB;
+  const float* wa = J.wa + (size_t)(X0 / 4) * W * 4 + (X0 & 3) + lane;
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int k = t + i * T;
+    const float f0 = __ldg(wa + (size_t)k * 4), f1 = __ldg(wa + (size_t)(k + N) * 4);
+    const float2 a0 = acc[sidx(k * CB + lane)], a1 = acc[sidx((k + N) * CB + lane)];
+    const float2 u0 = make_float2(a0.x * f0, a0.y * f0), u1 = make_float2(a1.x * f1, a1.y * f1);
+    bz[sidx(k * CB + lane)] = cadd(u0, u1);
+    bh[sidx(k * CB + lane)] = cmul(csub(u0, u1), cconjf(twW[k]));
+  }
+  __syncthreads();
+  line_fft_st<N, T, CB, true>(bz, lt, twN);
+  line_fft_st<N, T, CB, true>(bh, lt, twN);
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int k = t + i * T;
+    J.O[(size_t)(2 * k) * W + X0 + lane] = bz[sidx(k * CB + lane)];
+    J.O[(size_t)(2 * k + 1) * W + X0 + lane] = bh[sidx(k * CB + lane)];
+  }
+}
+
+// ---- pass C: rows of the output ---------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::TC) k_pass_c(const JobDesc* __restrict__ jobs) {
+  using P = Cfg<N>;
+  constexpr int W = P::W, T = P::TC, G = P::GC, EW = P::EW;
+  const JobDesc& J = jobs[blockIdx.y];
+  const int g = threadIdx.x / T, t = threadIdx.x % T;
+  const int Y = blockIdx.x * G + g;
+  __shared__ float2 sm[G * smem_line_elems(W, 1)];
+  __shared__ float2 tw[stw_len(W, EW)];
+  stage_stage_twiddles<W, EW>(tw, threadIdx.x, G * T);
+  float2* s = sm + g * smem_line_elems(W, 1);
+  const float2* row = J.O + (size_t)Y * W;
+#pragma unroll
+  for (int i = 0; i < EW; i++) s[sidx(t + i * T)] = row[t + i * T];
+  __syncthreads();
+  line_fft_st<W, T, 1, true>(s, t, tw);
+  const float scale = 1.f / ((float)W * (float)W);
+  float* out = J.out + (size_t)Y * W;
+#pragma unroll
+  for (int i = 0; i < EW; i++) out[t + i * T] = s[sidx(t + i * T)].x * scale;
+}
+
+// ---- launch ---------------------------------------------------------------------------------------
+template <int N, int ENA, int ENB, int CBB>
+static int launch_offline_v(const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st) {
+  using PA = Cfg<N, ENA>;
+  using PB = Cfg<N, ENB, CBB>;
+  using PC = Cfg<N>;
+  constexpr int W = PC::W;
+  (void)maxP;
+  cudaEvent_t* ev = profile_events();
+  static bool attr = false;
+  const size_t smem_b = sizeof(float2) * (smem_line_elems(W, PB::CB) + 2 * smem_line_elems(N, PB::CB));
+  if (!attr) {
+    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
+    attr = true;
+  }
+  if (ev) cudaEventRecord(ev[0], st);
+  k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, 0, st>>>(d_jobs);
+  if (ev) cudaEventRecord(ev[1], st);
+  k_pass_b<N, ENB, CBB><<<dim3(W / PB::CB, njobs), PB::CB * PB::T, smem_b, st>>>(d_jobs);
+  if (ev) cudaEventRecord(ev[2], st);
+  k_pass_c<N><<<dim3(W / PC::GC, njobs), PC::GC * PC::TC, 0, st>>>(d_jobs);
+  if (ev) {
+    cudaEventRecord(ev[3], st);
+    profile_mark(3);
+  }
+  FSIM_CHECK_LAUNCH();
+  return FSIM_OK;
+}
+
+// tuned variants per size: index into the variant lists of launch_offline
+extern int g_var_a[16], g_var_b[16];
+__host__ inline int size_slot(int n) {
+  switch (n) {
+    case 64: return 0;
+    case 128: return 1;
+    case 192: return 2;
+    case 256: return 3;
+    case 384: return 4;
+    case 512: return 5;
+    case 768: return 6;
+    case 1024: return 7;
+    case 2048: return 8;
+  }
+  return -1;
+}
+
+// variant lists: pass A elements/thread {E0, E1}; pass B (elements, columns)
+// {(E0,4), (E0,2), (E1,4), (E1,2)} with E0 = 8, E1 = 16 (3*2^k sizes: 12, 24)
+template <int N>
+int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st) {
+  constexpr bool p3 = (N % 3 == 0);
+  constexpr int E0 = p3 ? 12 : 8, E1 = p3 ? 24 : 16;
+  const int k = size_slot(N);
+  const int va = g_var_a[k], vb = g_var_b[k];
+#define L_(EA, EB, CB) return launch_offline_v<N, EA, EB, CB>(d_jobs, njobs, maxA, maxP, st)
+  if constexpr (N <= 128 || N >= 2048) {
+    L_(E0, E0, (N >= 2048 ? 2 : 4));  // single variant at the extremes
+  } else {
+    if (va == 0) {
+      if (vb == 0) L_(E0, E0, 4);
+      if (vb == 1) L_(E0, E0, 2);
+      if (vb == 2) L_(E0, E1, 4);
+      L_(E0, E1, 2);
+    } else {
+      if (vb == 0) L_(E1, E0, 4);
+      if (vb == 1) L_(E1, E0, 2);
+      if (vb == 2) L_(E1, E1, 4);
+      L_(E1, E1, 2);
+    }
+  }
+#undef L_
+}
+
+}  // namespace fsim

@@ -39,7 +39,7 @@ void fill_twiddle_host(float2* h) {
 
 void fill_stage_twiddle_host(float2* h) {
   auto fill = [&](int L) {
-    for (int e = 0; e < 4; e++) {
+    for (int e = 0; e < STW_NE; e++) {
       const int E = stw_e(e);
       if (!stw_ok(L, E)) continue;
       float2* t = h + stw_offset(L, E);

@@ -160,6 +160,8 @@ _SIGS = {
     "fsim_plan_info": (I32, [VP, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
     "fsim_recon_batch": (I32, [VP, I32, VP, C.c_size_t, VP]),
     "fsim_recon_host": (I32, [VP, VP, VP]),
+    "fsim_tune_set": (I32, [I32, I32, I32, I32]),
+    "fsim_tune_get": (I32, [I32, I32, I32, C.POINTER(I32), C.POINTER(I32)]),
     "fsim_profile_enable": (I32, [I32]),
     "fsim_profile_read": (I32, [VP, I32, C.POINTER(I32)]),
     "fsim_estimate_raw": (I32, [VP, VP, I32, I32, I32, F64, VP]),
@@ -203,5 +205,28 @@ def check(rc):
     return rc
 
 
-def init(device=0):
-    return check(lib().fsim_init(device))
+_tuned = False
+
+
+def apply_tuning(path=None):
+    """Apply the autotuner's table (tuning.json) to the library (fsim_tune_set)."""
+    import json
+
+    global _tuned
+    path = path or os.path.join(_HERE, "tuning.json")
+    if not os.path.exists(path):
+        return False
+    with open(path) as f:
+        t = json.load(f)
+    for n, v in t.get("offline", {}).items():
+        check(lib().fsim_tune_set(int(n), PATH_OFFLINE, 0, int(v["a"])))
+        check(lib().fsim_tune_set(int(n), PATH_OFFLINE, 1, int(v["b"])))
+    _tuned = True
+    return True
+
+
+def init(device=0, apply_tuning=True):
+    check(lib().fsim_init(device))
+    if apply_tuning and not _tuned:
+        globals()["apply_tuning"]()
+    return FSIM_OK

@@ -125,3 +125,21 @@ def sim_param_for(truth, n, n_dirs=3, n_phases=3, n_bands=2, known=True):
             for b in range(1, n_bands):
                 sp.dir(d).setModulation(b, truth["modulation"])
     return sp
+
+
+def synthetic_params(n, n_dirs=3, n_phases=3, n_bands=2, na=1.4, em_wavelength=525.0, pxl_um=0.08, k0_frac=0.85,
+                     modulation=0.8, seed=0):
+    """SimParam mirror with the generator's geometry, without generating images (for
+    launch-shape tuning and timing, where the pixel values do not matter)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cut_px = cutoff_cycles_per_micron(na, em_wavelength) * n * pxl_um
+    k0 = k0_frac * cut_px
+    hb = n_bands - 1
+    pxpy, phi0 = [], []
+    for d in range(n_dirs):
+        th = math.radians(180.0 * d / n_dirs + rng.uniform(0, 5.0))
+        pxpy.append((hb * k0 * math.cos(th), -hb * k0 * math.sin(th)))
+        phi0.append(rng.uniform(0, 2 * math.pi))
+    truth = dict(pxpy=pxpy, phi0=phi0, modulation=modulation, na=na, em_wavelength=em_wavelength, pxl_um=pxl_um,
+                 otf_a=1.0)
+    return sim_param_for(truth, n, n_dirs, n_phases, n_bands)

@@ -158,6 +158,12 @@ typedef struct fsim_job {
  * size class. workspace: device memory of at least the sum of fsim_plan_workspace_bytes. */
 int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t workspace_bytes,
                      void* stream);
+/* Kernel variant per image size (no reference counterpart), chosen by the project's
+ * autotuner (fairsim-vigor_gb300/autotune.py, results in tuning.json): pass 0 = row pass
+ * (elements per thread), pass 1 = column pass (elements per thread x interleaved columns).
+ * Variants only change launch shapes; results are identical to float rounding. */
+int fsim_tune_set(int n, int path, int pass, int variant);
+int fsim_tune_get(int n, int path, int pass, int* variant, int* n_variants);
 /* Per-pass CUDA-event timing of fused batches (no reference counterpart): while enabled,
  * every batch records events between its passes on its stream; fsim_profile_read waits
  * for the last batch and returns the duration of each pass of its last size class

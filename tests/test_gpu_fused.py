@@ -154,3 +154,27 @@ def test_live_refit_vs_oracle(fs, oracle, torch_cuda):
     for d in range(3):
         assert abs(got["pX"][d] - est["pX"][d]) < 1e-9 and abs(got["pY"][d] - est["pY"][d]) < 1e-9
         assert abs(got["modulations"][d][1] - est["modulations"][d][1]) < 1e-4
+
+
+@pytest.mark.parametrize("n", [384, 512, 1024])
+def test_every_tuned_variant_matches_oracle(fs, oracle, n):
+    """The autotuner may pick any launch-shape variant: each must give the same result."""
+    import ctypes as C
+    lib = fs.native.lib()
+    raw, truth, sp = make(fs, n, seed=100 + n)
+    exp = oracle.recon_raw(sp, raw, fade=10)
+    plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    v, cnt = C.c_int(), C.c_int()
+    saved = []
+    for p in (0, 1):
+        fs.native.check(lib.fsim_tune_get(n, fs.native.PATH_OFFLINE, p, C.byref(v), C.byref(cnt)))
+        saved.append((v.value, cnt.value))
+    try:
+        for va in range(saved[0][1]):
+            for vb in range(saved[1][1]):
+                fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 0, va))
+                fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 1, vb))
+                assert rel_l2(plan.reconstruct_host(raw), exp) < 1e-4, (va, vb)
+    finally:
+        fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 0, saved[0][0]))
+        fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 1, saved[1][0]))
