@@ -235,11 +235,37 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2*
     const int j = t + b * T;
     const int k = j % NS;
     if constexpr (NS > 1) {
+      float2 w[R];
+      if constexpr (TS > 0) {
+#pragma unroll
+        for (int r = 1; r < R; r++) w[r] = tw[r * k * (L / (NS * R)) * TS];
+      } else {
+        // stage table [r-1][k]: load W^k (and W^4k for radix 8/16), the rest by products
+        // (at most three roundings beyond the table's)
+        w[1] = tw[k];
+        if constexpr (R == 3) w[2] = tw[NS + k];
+        if constexpr (R == 4) {
+          w[2] = cmul(w[1], w[1]);
+          w[3] = cmul(w[2], w[1]);
+        }
+        if constexpr (R >= 8) {
+          w[4] = tw[3 * NS + k];
+          w[2] = cmul(w[1], w[1]);
+          w[3] = cmul(w[2], w[1]);
+#pragma unroll
+          for (int r = 5; r < 8; r++) w[r] = cmul(w[4], w[r - 4]);
+        }
+        if constexpr (R == 16) {
+          w[8] = tw[7 * NS + k];
+#pragma unroll
+          for (int r = 9; r < 16; r++) w[r] = cmul(w[8], w[r - 8]);
+        }
+      }
 #pragma unroll
       for (int r = 1; r < R; r++) {
-        float2 w = (TS > 0) ? tw[r * k * (L / (NS * R)) * TS] : tw[(r - 1) * NS + k];
-        if (INV) w.y = -w.y;
-        v[b][r] = cmul(v[b][r], w);
+        float2 ww = w[r];
+        if (INV) ww.y = -ww.y;
+        v[b][r] = cmul(v[b][r], ww);
       }
     }
     dft<R, INV>(v[b]);

@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
   __shared__ JobDesc J;
   __shared__ float2 bz[smem_line_elems(N, 1)], bh[smem_line_elems(N, 1)], sv[N];
   __shared__ float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
+  extern __shared__ float rows[];  // nP raw rows of this image row (background clip, damping)
   const float2* twN = g_stw + stw_offset(N, EN);  // stage table, read through L1
   const float2* twW = g_tw + tw_offset(W);
   load_job(&J, jobs + blockIdx.z, t, T);
@@ -71,24 +72,27 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
   if (a >= J.nA) return;  // uniform per block
   const int nP = J.nP, nC = J.nC;
   for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
-  __syncthreads();
   const size_t frame = (size_t)N * N, row = (size_t)y * N;
-  // raw pixel of phase p at column x: background clip and border damping
-  auto px = [&](int p, int x) {
-    const size_t at = (size_t)(a * nP + p) * frame + row + x;
-    float v = J.input_u16 ? (float)__ldg((const uint16_t*)J.raw + at) : __ldg((const float*)J.raw + at);
-    if (J.bgr != 0.f) {
-      v = v - J.bgr;
-      if (v < 0) v = 0;
+  for (int p = 0; p < nP; p++) {
+#pragma unroll
+    for (int i = 0; i < EN; i++) {
+      const int x = t + i * T;
+      const size_t at = (size_t)(a * nP + p) * frame + row + x;
+      float v = J.input_u16 ? (float)__ldg((const uint16_t*)J.raw + at) : __ldg((const float*)J.raw + at);
+      if (J.bgr != 0.f) {
+        v = v - J.bgr;
+        if (v < 0) v = 0;
+      }
+      if (J.damp) v = v * __ldg(J.damp + row + x);
+      rows[p * N + x] = v;
     }
-    if (J.damp) v = v * __ldg(J.damp + row + x);
-    return v;
-  };
+  }
+  __syncthreads();
   auto mix = [&](int cm, int x) {  // band separation in real space
     float2 z = make_float2(0.f, 0.f);
     for (int p = 0; p < nP; p++) {
       const float2 m = coef[cm * nP + p];
-      const float v = px(p, x);
+      const float v = rows[p * N + x];
       z.x += m.x * v;
       z.y += m.y * v;
     }
@@ -314,16 +318,17 @@ static int launch_offline_v(const JobDesc* d_jobs, int njobs, int maxA, int maxP
   using PB = Cfg<N, ENB, CBB>;
   using PC = Cfg<N>;
   constexpr int W = PC::W;
-  (void)maxP;
   cudaEvent_t* ev = profile_events();
   static bool attr = false;
   const size_t smem_b = sizeof(float2) * (smem_line_elems(W, PB::CB) + 2 * smem_line_elems(N, PB::CB));
   if (!attr) {
     FSIM_CUDA(cudaFuncSetAttribute(k_pass_b<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
+    FSIM_CUDA(cudaFuncSetAttribute(k_pass_a<N, ENA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(float) * FSIM_MAX_PHASES * N)));
     attr = true;
   }
   if (ev) cudaEventRecord(ev[0], st);
-  k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, 0, st>>>(d_jobs);
+  k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, sizeof(float) * maxP * N, st>>>(d_jobs);
   if (ev) cudaEventRecord(ev[1], st);
   k_pass_b<N, ENB, CBB><<<dim3(W / PB::CB, njobs), PB::CB * PB::T, smem_b, st>>>(d_jobs);
   if (ev) cudaEventRecord(ev[2], st);
