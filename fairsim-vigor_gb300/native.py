@@ -166,6 +166,7 @@ _SIGS = {
     "fsim_profile_read": (I32, [VP, I32, C.POINTER(I32)]),
     "fsim_estimate_raw": (I32, [VP, VP, I32, I32, I32, F64, VP]),
     "fsim_live_refit": (I32, [VP, VP, VP]),
+    "fsim_corr_grid_noalloc": (I32, [VP, VP, I32, VP, I32, VP, I32, F64, VP, VP]),
     "fsim_serve_open": (I32, [C.POINTER(VP), VP, VP, I32]),
     "fsim_serve_submit": (I32, [VP, I32, VP, C.POINTER(C.c_uint64)]),
     "fsim_serve_wait": (I32, [VP, C.c_uint64, VP, I32, C.POINTER(F64)]),

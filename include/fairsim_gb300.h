@@ -178,6 +178,19 @@ int fsim_estimate_raw(fsim_sim_param* p, const void* raw_device, int input_type,
 /* ParameterRefitThread.doRefit (ReconstructionRunner.java:642-746) on u16 device frames. */
 int fsim_live_refit(fsim_sim_param* p, const uint16_t* raw_device, double* peaks_out);
 
+/* ---- allocation-free correlation sweep (no counterpart in the reference) ---------------
+ * For callers that cannot allocate device memory at this point (a real-time acquisition
+ * thread, work being captured into a CUDA graph, or a process whose device memory was
+ * partitioned up front): the fit's 10 x 10 correlation grid of Correlation.fitPeak's
+ * inner loop, evaluated on caller-provided real-space bands b0, b1 (n x n complex float,
+ * device) for shifts kx[nx], ky[ny] (host arrays), scaled by scal; out (host, nx*ny*2
+ * doubles, [yi][xi] re/im). Scratch is one static device array per GPU (n <= 2048,
+ * nx, ny <= 10; ~0.66 MB kept until exit); the call allocates nothing. Overlapping calls
+ * race on that scratch. The first call on a device resolves the array's address; make it
+ * before any stream capture. stream: cudaStream_t (NULL = legacy default stream). */
+int fsim_corr_grid_noalloc(const void* b0, const void* b1, int n, const double* kx, int nx, const double* ky,
+                           int ny, double scal, double* out, void* stream);
+
 /* ---- served form: continuous batching over channels (replaces ReconstructionRunner) --- */
 typedef struct fsim_server fsim_server;
 typedef struct fsim_serve_config {
