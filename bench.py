@@ -167,6 +167,27 @@ def run_reference(args):
     return 0
 
 
+# DRAM bytes (read + write) per dataset of each pass at 512^2 3x3, from one ncu capture of a
+# 16-dataset batch (raw 151 MB, larger than L2; the command is in
+# profiles/offline_512_3x3_passes_ncu.md); per-launch traffic = this x the batch size.
+TRAFFIC_PER_DATASET = {}
+
+
+def pass_bytes(n=N, n_dirs=NA, n_phases=NP, n_bands=NB, na=1.4, lam=525.0, pxl=0.08):
+    """Algorithmic bytes per dataset of the offline passes A, B, C (each input read once,
+    each output written once): A reads the raw frames and writes the row-transformed OTF
+    support windows I; B reads I, the masks and Wiener x apodization and writes the
+    column-transformed W x W plane O; C reads O and writes the W x W image."""
+    nc = 2 * n_bands - 1
+    W = 2 * n
+    R = (2 * na / (lam / 1000.0)) / (1.0 / (n * pxl))
+    nwin = min(W, ((2 * int(np.ceil(R)) + 6) // 4) * 4 + 4)
+    a = n_dirs * n_phases * n * n * 4 + n_dirs * nc * nwin * n * 8
+    b = n_dirs * nc * nwin * n * 8 + n_dirs * nc * nwin * nwin * 4 + W * W * 4 + W * W * 8
+    c = W * W * 8 + W * W * 4
+    return [a, b, c]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -175,7 +196,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--distinct", type=int, default=16)
-    ap.add_argument("--no-extras", action="store_true", help="skip plain-GPU, serve and CPU legs")
+    ap.add_argument("--no-extras", action="store_true", help="skip plain-GPU, serve, mixed, large and CPU legs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -210,9 +231,11 @@ def main():
     stream = torch.cuda.Stream()
     sp_ = stream.cuda_stream
     jobs = [(job_plans[i], raw_dev[i].data_ptr(), out_dev[i].data_ptr()) for i in range(B)]
+    graph = fs.plan.BatchGraph(jobs, ws.data_ptr(), ws_bytes, sp_)
+    kernels_per_step = graph.info()["kernels"]
 
     def step():
-        fs.plan.recon_batch(jobs, ws.data_ptr(), ws_bytes, sp_)
+        graph.launch(sp_)
 
     def barrier():
         if world > 1:
@@ -236,104 +259,82 @@ def main():
             ms = float(t.item())
         return ms
 
-    # ---- resident (device) throughput ----
+    def wall(fn, k):
+        """Host wall time of k calls that return with their results on the host."""
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            fn()
+        torch.cuda.synchronize()
+        barrier()
+        ms = (time.perf_counter() - t0) * 1000.0
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    # ---- resident (device) throughput: the batch replayed as one CUDA graph ----
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
     ms = timed(step, args.steps)
-    clk = clocks.stop()
     value = B * args.steps * world / (ms / 1000.0)
-    launches_per_step = 3  # one size class: passes A, B, C
 
-    # ---- end to end through the C ABI with host buffers ----
+    # ---- end to end through the C ABI with host buffers: pinned raw in, pinned image out ----
+    host_jobs = [(job_plans[i], raw_host[i].data_ptr(), out_host[i].data_ptr()) for i in range(B)]
+
     def e2e_step():
-        raw_dev.copy_(raw_host, non_blocking=True)
-        fs.plan.recon_batch(jobs, ws.data_ptr(), ws_bytes, sp_)
-        out_host.copy_(out_dev, non_blocking=True)
+        fs.plan.recon_batch_host(host_jobs)
 
-    with torch.cuda.stream(stream):
-        for _ in range(2):
-            e2e_step()
-    e2e_ms = timed(lambda: None, 0)  # sync
+    for _ in range(2):
+        e2e_step()
     e2e_steps = max(3, args.steps // 2)
-    with torch.cuda.stream(stream):
-        e2e_ms = timed(e2e_step, e2e_steps)
+    e2e_ms = wall(e2e_step, e2e_steps)
     e2e_value = B * e2e_steps * world / (e2e_ms / 1000.0)
     h2d = B * NA * NP * N * N * 4
     d2h = B * 4 * N * N * 4
+    clk = clocks.stop()
 
-    # ---- per-pass timing of the dominant kernel (CUDA events between passes) ----
+    # ---- per-pass timing (CUDA events between the passes of the direct batch call) ----
     import ctypes as C
 
     N_.check(N_.lib().fsim_profile_enable(1))
     pass_ms = []
     with torch.cuda.stream(stream):
         for _ in range(3):
-            step()
+            fs.plan.recon_batch(jobs, ws.data_ptr(), ws_bytes, sp_)
             arr = (C.c_float * 8)()
             n = C.c_int()
             N_.check(N_.lib().fsim_profile_read(arr, 8, C.byref(n)))
             pass_ms.append([arr[i] for i in range(n.value)])
     N_.check(N_.lib().fsim_profile_enable(0))
     pm = np.median(np.array(pass_ms), axis=0)
-    nwin = int(np.ceil((2 * np.ceil(1000 / (525 / 1.4 / 2) / (1 / (N * 0.08))) + 6) / 4) * 4 + 4)
-    nwin = min(nwin, 2 * N)
-    W = 2 * N
-    bytes_a = NA * NP * N * N * 4 + NA * (2 * NB - 1) * nwin * N * 8
-    bytes_b = NA * (2 * NB - 1) * nwin * N * 8 + NA * (2 * NB - 1) * nwin * nwin * 4 + W * W * 4 + W * W * 8
-    bytes_c = W * W * 8 + W * W * 4
-    algo = [bytes_a, bytes_b, bytes_c]
+    algo = pass_bytes()
     names = ["k_pass_a<512>", "k_pass_b<512>", "k_pass_c<512>"]
     dom = int(np.argmax(pm))
     peak, peak_kind = peaks()
     achieved = algo[dom] * B / (pm[dom] / 1000.0) / 1e9
     passes = {names[i]: {"ms": float(pm[i]), "algorithmic_MB_per_dataset": algo[i] / 1e6,
-                         "GB_per_s": algo[i] * B / (pm[i] / 1000.0) / 1e9} for i in range(len(pm))}
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            tr = json.load(f)
-            traffic = tr.get(names[dom])
-    except Exception:
-        pass
+                         "GB_per_s": algo[i] * B / (pm[i] / 1000.0) / 1e9,
+                         "frac_of_measured_hbm": algo[i] * B / (pm[i] / 1000.0) / 1e9 / peak}
+              for i in range(len(pm))}
+    traffic = TRAFFIC_PER_DATASET.get(names[dom])
+    traffic = traffic * B if traffic else None
 
     extras = {}
     if rank == 0 and not args.no_extras:
-        # plain GPU form: one dataset at a time through the op-by-op vector path
-        V = fs.vectors
-        raw, sp = datasets[0]
-        from oracle import refcpu  # input preparation reference only for shapes
-
-        spec_vecs = [[V.Vec2dCplx(N, N) for _ in range(NP)] for _ in range(NA)]
-        fade = V.Vec2dReal(N, N)
-        fade.setData(np.ones((N, N), np.float32))
-        host_raw = [raw[i] for i in range(NA * NP)]
-
-        def plain():
-            for a in range(NA):
-                for p in range(NP):
-                    v = spec_vecs[a][p]
-                    v.setData(host_raw[a * NP + p].astype(np.complex64))
-                    v.times(fade)
-                    v.fft2d(False)
-            out = fs.algorithm.SimAlgorithm.runReconstruction(sp, spec_vecs, False, 0)
-            out.vectorData()
-
-        plain()
-        t0 = time.perf_counter()
-        k = 5
-        for _ in range(k):
-            plain()
-        plain_rate = k / (time.perf_counter() - t0)
-        extras["plain_gpu"] = {"value": plain_rate, "unit": "recon/s",
-                               "note": "op-by-op device vector path, one dataset at a time, host buffers"}
-        extras["speedup_batched_vs_plain"] = value / plain_rate
-        extras["speedup_e2e_vs_plain"] = e2e_value / plain_rate
-        # served form: Poisson arrivals, 3 channels x 100 stacks/s at 512^2 u16, 10% at 1024^2
+        extras["plain_gpu"] = plain_gpu_leg(fs, datasets[0])
+        extras["speedup_batched_vs_plain"] = value / extras["plain_gpu"]["value"]
+        extras["speedup_e2e_vs_plain"] = e2e_value / extras["plain_gpu"]["value"]
         extras["serve"] = serve_leg(fs, seconds=3.0)
-        # CPU baseline (oracle) on a bounded sample
+        extras["serve"]["speedup_vs_plain"] = extras["serve"]["recon_per_s"] / extras["plain_gpu"]["value"]
+        extras["mixed_batch"] = mixed_leg(fs, torch, stream, timed)
+        extras["large_3x5_2048"] = large_leg(fs, torch, stream, timed)
+        extras["estimate_1024"] = estimate_leg(fs, torch)
         rate, cores, n, dt = cpu_recon_rate(fs, datasets)
         extras["cpu_baseline"] = {"value": rate, "unit": "recon/s", "cores": cores, "kind": "port",
                                   "sample": "%d reconstructions of one 512x512 3x3 dataset in %.1f s (oracle: C++ "
@@ -347,24 +348,163 @@ def main():
             "data": "synthetic (seeded: 2000 lognormal points + 40 filaments, cos patterns m=0.8, |k0|=0.85 cutoff, "
                     "500 photons + N(0,2)); %d distinct datasets tiled to the batch" % args.distinct,
             "config": {"workload": WORKLOAD, "batch": B, "n": N, "out": 2 * N, "path": "offline (runReconstruction)",
+                       "form": "batch recorded as one CUDA graph (fsim_batch_graph), replayed per step",
                        "l2": "inputs larger than L2 (%.0f MiB raw per step)" % (h2d / 2 ** 20),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "e2e": {"value": e2e_value, "unit": "recon/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_value, "unit": "recon/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "call": "fsim_recon_batch_host (pinned host buffers; chunked upload/passes/download overlapped)"},
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "algorithmic_bytes_per_launch": algo[dom] * B},
             "passes": passes,
             "e2e_fraction_of_hbm": (18874368 * value) / (peak * 1e9),
             "clocks": clk,
-            "gpu_launches": launches_per_step * args.steps,
+            "gpu_launches": kernels_per_step * args.steps,
         }
         if "cpu_baseline" in extras:
             line["cpu_baseline"] = extras.pop("cpu_baseline")
         line.update(extras)
         print(json.dumps(line))
+    graph.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def plain_gpu_leg(fs, dataset, k=5):
+    """The plain GPU form: one dataset at a time through the op-by-op device vector path
+    (the reference's accel-backed Java pipeline, one library call per vector op)."""
+    V = fs.vectors
+    raw, sp = dataset
+    spec_vecs = [[V.Vec2dCplx(N, N) for _ in range(NP)] for _ in range(NA)]
+    fade = V.Vec2dReal(N, N)
+    fade.setData(np.ones((N, N), np.float32))
+    host_raw = [raw[i] for i in range(NA * NP)]
+
+    def plain():
+        for a in range(NA):
+            for p in range(NP):
+                v = spec_vecs[a][p]
+                v.setData(host_raw[a * NP + p].astype(np.complex64))
+                v.times(fade)
+                v.fft2d(False)
+        out = fs.algorithm.SimAlgorithm.runReconstruction(sp, spec_vecs, False, 0)
+        out.vectorData()
+
+    plain()
+    t0 = time.perf_counter()
+    for _ in range(k):
+        plain()
+    return {"value": k / (time.perf_counter() - t0), "unit": "recon/s",
+            "note": "op-by-op device vector path (fsim_vec_* + fsim_run_reconstruction), one dataset at a time, "
+                    "host buffers"}
+
+
+def mixed_leg(fs, torch, stream, timed, n_datasets=64, steps=5, seed=77):
+    """64 datasets, sizes uniform over {256, 384, 512, 768, 1024}, each with 1-3 channels
+    (emission 488 / 525 / 600 nm, separate OTFs), 3x3 stacks, per-dataset seeded k0 angle and
+    modulation in [0.5, 0.9]; all channels of all datasets in one CUDA-graph replay."""
+    N_ = fs.native
+    rng = np.random.default_rng(seed)
+    sizes = [256, 384, 512, 768, 1024]
+    lams = [488.0, 525.0, 600.0]
+    # one generated stack per (size, emission) supplies the pixels; each dataset's channels
+    # get their own seeded parameters (the work per stack does not depend on pixel values)
+    pix = {}
+    for n in sizes:
+        for lam in lams:
+            raw, _ = fs.synth.make_dataset(n=n, seed=300 + n + int(lam), em_wavelength=lam)
+            pix[(n, lam)] = torch.from_numpy(raw).cuda()
+    plans, raws, outs = [], [], []
+    n_stacks = 0
+    for d in range(n_datasets):
+        n = sizes[rng.integers(len(sizes))]
+        nch = int(rng.integers(1, 4))
+        for ch in range(nch):
+            lam = lams[ch]
+            sp = fs.synth.synthetic_params(n, em_wavelength=lam, modulation=float(rng.uniform(0.5, 0.9)),
+                                           seed=int(rng.integers(1 << 30)))
+            plans.append(fs.plan.ReconPlan(sp, path=N_.PATH_OFFLINE, input_type=N_.INPUT_F32, fade_px=10))
+            raws.append(pix[(n, lam)].clone())
+            outs.append(torch.empty((2 * n, 2 * n), dtype=torch.float32, device="cuda"))
+            n_stacks += 1
+    ws = torch.empty(fs.plan.batch_workspace_bytes(plans), dtype=torch.uint8, device="cuda")
+    jobs = [(p, r.data_ptr(), o.data_ptr()) for p, r, o in zip(plans, raws, outs)]
+    g = fs.plan.BatchGraph(jobs, ws.data_ptr(), ws.numel(), stream.cuda_stream)
+    for _ in range(3):
+        g.launch(stream.cuda_stream)
+    ms = timed(lambda: g.launch(stream.cuda_stream), steps)
+    info = g.info()
+    g.close()
+    hist = {n: sum(1 for p in plans if p.w == n) for n in sizes}
+    res = {"datasets_per_s": n_datasets * steps / (ms / 1000.0), "stacks_per_s": n_stacks * steps / (ms / 1000.0),
+           "ms_per_batch": ms / steps, "datasets": n_datasets, "stacks": n_stacks, "stacks_per_size": hist,
+           "kernels_per_replay": info["kernels"],
+           "raw_MB_per_batch": sum(r.numel() * 4 for r in raws) / 1e6}
+    for p in plans:
+        p.close()
+    return res
+
+
+def large_leg(fs, torch, stream, timed, steps=5):
+    """2048^2 raw, 3 angles x 5 phases (phases 2 pi k/5, pseudo-inverse separation),
+    |k0| = 0.9 cutoff, modulation 0.6, 200 photons, reconstructed to 4096^2; throughput
+    against the 20 stacks/s stream, and rel-L2 against the float and FP64 oracles."""
+    from oracle import refcpu
+
+    N_ = fs.native
+    n = 2048
+    raw, truth = fs.synth.make_dataset(n=n, n_phases=5, seed=500, k0_frac=0.9, modulation=0.6, photons=200.0)
+    sp = fs.synth.sim_param_for(truth, n, n_phases=5)
+    plan = fs.plan.ReconPlan(sp, path=N_.PATH_OFFLINE, input_type=N_.INPUT_F32, fade_px=10)
+    d_raw = torch.from_numpy(raw).cuda()
+    d_out = torch.empty((2 * n, 2 * n), dtype=torch.float32, device="cuda")
+    ws = torch.empty(fs.plan.batch_workspace_bytes([plan]), dtype=torch.uint8, device="cuda")
+    g = fs.plan.BatchGraph([(plan, d_raw.data_ptr(), d_out.data_ptr())], ws.data_ptr(), ws.numel(),
+                           stream.cuda_stream)
+    for _ in range(3):
+        g.launch(stream.cuda_stream)
+    ms = timed(lambda: g.launch(stream.cuda_stream), steps)
+    got = d_out.cpu().numpy()
+    g.close()
+    t0 = time.perf_counter()
+    got_host = plan.reconstruct_host(raw)
+    host_ms = (time.perf_counter() - t0) * 1000
+    refcpu.set_threads(os.cpu_count() or 1)
+    exp32 = refcpu.recon_raw(sp, raw, fade=10)
+    exp64 = refcpu.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+    rl = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+    plan.close()
+    return {"stacks_per_s": 1000.0 / (ms / steps), "ms_per_stack": ms / steps,
+            "host_call_ms": host_ms, "stream_target_stacks_per_s": 20.0,
+            "rel_l2_vs_oracle_f32": rl(got, exp32), "rel_l2_vs_oracle_f64": rl(got, exp64),
+            "oracle_f32_vs_f64": rl(exp32, exp64), "device_vs_host_call_identical": bool(np.array_equal(got, got_host))}
+
+
+def estimate_leg(fs, torch, reps=3):
+    """Full parameter fit at 1024^2 on the device (fade, FFT, locatePeak, fitPeak 3 x 10 x
+    10, getPeak per angle), with the fitted k0 compared to the generator's."""
+    import ctypes as C
+
+    N_ = fs.native
+    n = 1024
+    raw, truth = fs.synth.make_dataset(n=n, seed=600)
+    sp = fs.synth.sim_param_for(truth, n)
+    sp.directions = [fs.Dir(NB, NP) for _ in range(NA)]  # start from no knowledge of the shifts
+    d_raw = torch.from_numpy(raw).cuda()
+    out = (C.c_double * 12)()
+    ts = []
+    for _ in range(reps + 1):
+        c = N_.to_c_param(sp)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        N_.check(N_.lib().fsim_estimate_raw(C.byref(c), C.c_void_p(d_raw.data_ptr()), N_.INPUT_F32, 10, 1,
+                                            C.c_double(0.6), out))
+        ts.append((time.perf_counter() - t0) * 1000)
+    got = N_.from_c_param(c)
+    err = max(max(abs(got["pX"][d] - truth["pxpy"][d][0]), abs(got["pY"][d] - truth["pxpy"][d][1]))
+              for d in range(NA))
+    return {"ms_per_fit": float(np.median(ts[1:])), "max_k0_error_px": err}
 
 
 def serve_leg(fs, seconds=3.0, rate_per_channel=100.0, seed=5):

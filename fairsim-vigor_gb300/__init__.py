@@ -5,7 +5,9 @@ Layout:
   native.py      ctypes binding of lib/libfairsim_gb300.so
   vectors.py     Vector API (AccelVectorFactory / Vec2d.Real / Vec2d.Cplx) on device memory
   algorithm.py   SimAlgorithm / BandSeparation / SimUtils / Correlation / WienerFilter / OTF writers
-  plan.py        fused batched reconstruction plans and the served (live) form
+  plan.py        fused batched reconstruction plans, CUDA-graph batches, host-buffer batches
+                 and the served (live) form
+  replicas.py    multi-GPU form: disjoint dataset shares per rank, max-over-ranks timing
   sim_param.py   SimParam / SimParam.Dir / OtfProvider records
   synth.py       seeded synthetic SIM datasets
 """
@@ -18,7 +20,7 @@ def __getattr__(name):
     # vector/algorithm modules load the native library lazily
     import importlib
 
-    if name in ("vectors", "algorithm", "plan"):
+    if name in ("vectors", "algorithm", "plan", "replicas", "autotune"):
         return importlib.import_module("." + name, __name__)
     if name in ("AccelVectorFactory", "Vec2dReal", "Vec2dCplx"):
         return getattr(importlib.import_module(".vectors", __name__), name)

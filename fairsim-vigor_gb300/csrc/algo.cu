@@ -40,7 +40,7 @@ struct DevOtf {
   int set(const fsim_sim_param* p, cudaStream_t st) {
     OtfTable h;
     build_otf_table(p, &h);
-    if (!d) FSIM_CUDA(cudaMallocAsync(&d, sizeof(OtfTable), st));
+    if (!d) FSIM_CUDA(fsim::dev_alloc_async(&d, sizeof(OtfTable), st));
     FSIM_CUDA(cudaMemcpyAsync(d, &h, sizeof(OtfTable), cudaMemcpyHostToDevice, st));
     FSIM_CUDA(cudaStreamSynchronize(st));  // h is on this stack frame
     return FSIM_OK;
@@ -59,7 +59,7 @@ struct DevBufs {
   template <class T>
   int get(T** p, size_t bytes) {
     void* q = nullptr;
-    cudaError_t e = cudaMallocAsync(&q, bytes, st);
+    cudaError_t e = fsim::dev_alloc_async(&q, bytes, st);
     if (e != cudaSuccess) {
       set_error("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
       return FSIM_EOOM;

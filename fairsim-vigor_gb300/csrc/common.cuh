@@ -14,6 +14,17 @@ namespace fsim {
 // ---- status handling -------------------------------------------------------
 void set_error(const char* fmt, ...);
 const char* last_error();
+// every device allocation of the library goes through here (fsim_debug_fail_alloc hook)
+cudaError_t dev_alloc(void** p, size_t bytes);
+template <class T>
+cudaError_t dev_alloc(T** p, size_t bytes) {
+  return dev_alloc(reinterpret_cast<void**>(p), bytes);
+}
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t st);
+template <class T>
+cudaError_t dev_alloc_async(T** p, size_t bytes, cudaStream_t st) {
+  return dev_alloc_async(reinterpret_cast<void**>(p), bytes, st);
+}
 
 #define FSIM_CUDA(call)                                                                \
   do {                                                                                 \

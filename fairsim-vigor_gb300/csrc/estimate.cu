@@ -230,17 +230,23 @@ int locate_peak_device(const float2* v, int w, int h, double kmin, EstScratch& s
 int EstScratch::alloc(int N, cudaStream_t st) {
   if (n == N && b0) return FSIM_OK;
   free(st);
+  const size_t img = (size_t)N * N * sizeof(float2);
+  // all or nothing: a partial set would pass the reuse test above next time
+  cudaError_t e = fsim::dev_alloc_async(&b0, img, st);
+  if (e == cudaSuccess) e = fsim::dev_alloc_async(&b1, img, st);
+  if (e == cudaSuccess) e = fsim::dev_alloc_async(&tx, sizeof(float2) * 10 * N, st);
+  if (e == cudaSuccess) e = fsim::dev_alloc_async(&ty, sizeof(float2) * 10 * N, st);
+  if (e == cudaSuccess) e = fsim::dev_alloc_async(&Q, sizeof(double2) * 10 * N, st);
+  if (e == cudaSuccess) e = fsim::dev_alloc_async(&corr, sizeof(double2) * 100, st);
+  if (e == cudaSuccess) e = fsim::dev_alloc_async(&kbuf, sizeof(double) * 20, st);
+  if (e == cudaSuccess) e = fsim::dev_alloc_async(&pmag, sizeof(float) * 256, st);
+  if (e == cudaSuccess) e = fsim::dev_alloc_async(&pidx, sizeof(int) * 256, st);
+  if (e != cudaSuccess) {
+    free(st);
+    set_error("estimation scratch for %d x %d: %s", N, N, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? FSIM_EOOM : FSIM_ECUDA;
+  }
   n = N;
-  size_t img = (size_t)N * N * sizeof(float2);
-  FSIM_CUDA(cudaMallocAsync(&b0, img, st));
-  FSIM_CUDA(cudaMallocAsync(&b1, img, st));
-  FSIM_CUDA(cudaMallocAsync(&tx, sizeof(float2) * 10 * N, st));
-  FSIM_CUDA(cudaMallocAsync(&ty, sizeof(float2) * 10 * N, st));
-  FSIM_CUDA(cudaMallocAsync(&Q, sizeof(double2) * 10 * N, st));
-  FSIM_CUDA(cudaMallocAsync(&corr, sizeof(double2) * 100, st));
-  FSIM_CUDA(cudaMallocAsync(&kbuf, sizeof(double) * 20, st));
-  FSIM_CUDA(cudaMallocAsync(&pmag, sizeof(float) * 256, st));
-  FSIM_CUDA(cudaMallocAsync(&pidx, sizeof(int) * 256, st));
   return FSIM_OK;
 }
 void EstScratch::free(cudaStream_t st) {

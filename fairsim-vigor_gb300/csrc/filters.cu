@@ -136,10 +136,8 @@ int upload_otf_table(const fsim_sim_param* p, OtfTable** dev, cudaStream_t st) {
   static OtfTable* host = nullptr;
   static double key[7] = {0, 0, 0, 0, 0, 0, 0};
   std::lock_guard<std::mutex> g(g_otf_mu);
-  if (!buf) {
-    FSIM_CUDA(cudaMalloc(&buf, sizeof(OtfTable)));
-    FSIM_CUDA(cudaMallocHost(&host, sizeof(OtfTable)));
-  }
+  if (!buf) FSIM_CUDA(fsim::dev_alloc(&buf, sizeof(OtfTable)));
+  if (!host) FSIM_CUDA(cudaMallocHost(&host, sizeof(OtfTable)));
   const double k[7] = {p->na, p->em_wavelength, p->otf_a, p->att_strength, p->att_fwhm, (double)p->w,
                        p->microns_per_pixel};
   bool same = true;

@@ -1,0 +1,176 @@
+// fsim_recon_batch_host: batched reconstruction from host buffers with the copies overlapped.
+//
+// The reference hands every stack over from Java arrays (AccelVectorReal.setFrom*,
+// org/fairsim/accel/AccelVectorReal.java:218-247, then one JNI op per step). Here a whole
+// batch of host stacks is reconstructed in chunks that flow through three library-owned
+// streams: the upload of chunk i+1, the passes of chunk i and the download of chunk i-1 run
+// at the same time. Two slots of device buffers (raw frames, outputs, workspace) alternate
+// between chunks; events order each slot's reuse:
+//   upload(i)   waits for passes(i-2)    (raw slot free)
+//   passes(i)   waits for upload(i), download(i-2) (out slot free)
+//   download(i) waits for passes(i)
+// The host fills chunk i's job table only after passes(i-2) finished with it, so the host
+// runs at most two chunks ahead. The call returns when every output is in host memory.
+// Host buffers that are page-locked (cudaHostAlloc / cudaHostRegister) are copied by DMA
+// directly; pageable ones make each copy synchronous on the host.
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "recon.cuh"
+#include "runtime.cuh"
+
+namespace fsim {
+namespace {
+
+struct Slot {
+  char* dev = nullptr;  // raw | out | widefield | workspace
+  size_t bytes = 0;
+  JobDesc* table = nullptr;  // pinned job table of the chunk in this slot
+  int table_cap = 0;
+  cudaEvent_t up = nullptr, done = nullptr, down = nullptr;
+  bool used = false;
+};
+
+struct HostPipe {
+  std::mutex mu;
+  bool ready = false;
+  cudaStream_t s_up = nullptr, s_comp = nullptr, s_down = nullptr;
+  Slot slot[2];
+};
+HostPipe g_pipe;
+
+size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+size_t raw_bytes(const Plan* p) {
+  return (size_t)p->prm.w * p->prm.w * p->prm.nr_dirs * p->prm.nr_phases * (p->input_type == FSIM_INPUT_U16 ? 2 : 4);
+}
+size_t out_bytes(const Plan* p) { return (size_t)4 * p->prm.w * p->prm.w * sizeof(float); }
+size_t wf_bytes(const Plan* p) { return (size_t)p->prm.w * p->prm.w * sizeof(float); }
+
+// device bytes of one chunk: per job raw + out (+ widefield) + workspace, plus the table
+size_t chunk_bytes(const fsim_host_job* jobs, int k0, int k1) {
+  size_t b = a256(sizeof(JobDesc) * (k1 - k0));
+  for (int k = k0; k < k1; k++) {
+    const Plan* p = reinterpret_cast<const Plan*>(jobs[k].plan);
+    b += a256(raw_bytes(p)) + a256(out_bytes(p)) + (jobs[k].widefield_host ? a256(wf_bytes(p)) : 0) +
+         a256(plan_ws(p));
+  }
+  return b;
+}
+
+int init_pipe(HostPipe& P) {
+  if (P.ready) return FSIM_OK;
+  FSIM_CUDA(cudaStreamCreateWithFlags(&P.s_up, cudaStreamNonBlocking));
+  FSIM_CUDA(cudaStreamCreateWithFlags(&P.s_comp, cudaStreamNonBlocking));
+  FSIM_CUDA(cudaStreamCreateWithFlags(&P.s_down, cudaStreamNonBlocking));
+  for (auto& s : P.slot) {
+    FSIM_CUDA(cudaEventCreateWithFlags(&s.up, cudaEventDisableTiming));
+    FSIM_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    FSIM_CUDA(cudaEventCreateWithFlags(&s.down, cudaEventDisableTiming));
+  }
+  P.ready = true;
+  return FSIM_OK;
+}
+
+}  // namespace
+}  // namespace fsim
+
+using namespace fsim;
+
+extern "C" int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int chunk) {
+  FSIM_REQUIRE(jobs && n_jobs > 0, FSIM_EINVAL, "recon_batch_host: no jobs");
+  for (int k = 0; k < n_jobs; k++) {
+    const Plan* p = reinterpret_cast<const Plan*>(jobs[k].plan);
+    FSIM_REQUIRE(p && jobs[k].raw_host && jobs[k].out_host, FSIM_EINVAL, "host job %d: null plan/raw/out", k);
+    FSIM_REQUIRE(!jobs[k].widefield_host || p->path == FSIM_PATH_LIVE, FSIM_EINVAL,
+                 "host job %d: widefield output needs a live-path plan", k);
+  }
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (chunk <= 0) {
+    // about 96 MiB of raw frames per chunk: enough blocks to fill the GPU, and a pipeline
+    // fill/drain of a small fraction of a large batch
+    const size_t rb = raw_bytes(reinterpret_cast<const Plan*>(jobs[0].plan));
+    chunk = (int)std::max<size_t>(1, ((size_t)96 << 20) / std::max<size_t>(rb, 1));
+  }
+  chunk = std::min(chunk, n_jobs);
+  std::lock_guard<std::mutex> lock(g_pipe.mu);
+  HostPipe& P = g_pipe;
+  rc = init_pipe(P);
+  if (rc) return rc;
+  // size both slots for the largest chunk of this batch (the previous call has finished)
+  size_t need = 0;
+  for (int k0 = 0; k0 < n_jobs; k0 += chunk) need = std::max(need, chunk_bytes(jobs, k0, std::min(n_jobs, k0 + chunk)));
+  for (auto& s : P.slot) {
+    if (s.bytes < need) {
+      if (s.dev) cudaFree(s.dev);
+      s.dev = nullptr;
+      s.bytes = 0;
+      FSIM_CUDA(fsim::dev_alloc(&s.dev, need));
+      s.bytes = need;
+    }
+    if (s.table_cap < chunk) {
+      if (s.table) cudaFreeHost(s.table);
+      s.table = nullptr;
+      s.table_cap = 0;
+      FSIM_CUDA(cudaMallocHost(&s.table, sizeof(JobDesc) * chunk));
+      s.table_cap = chunk;
+    }
+    s.used = false;
+  }
+  std::vector<fsim_job> dj(chunk);
+  int c = 0;
+  for (int k0 = 0; k0 < n_jobs; k0 += chunk, c++) {
+    const int k1 = std::min(n_jobs, k0 + chunk), m = k1 - k0;
+    Slot& S = P.slot[c & 1];
+    if (S.used) {
+      // the table and raw buffers of chunk c-2 must be consumed, and its outputs downloaded
+      FSIM_CUDA(cudaEventSynchronize(S.done));
+      FSIM_CUDA(cudaStreamWaitEvent(P.s_up, S.done, 0));
+      FSIM_CUDA(cudaStreamWaitEvent(P.s_comp, S.down, 0));
+    }
+    // carve the slot: per job raw, out, widefield | job table and workspaces (recon_batch
+    // lays out [table | ws_0 | ws_1 ...] from the pointer it is given)
+    char* cur = S.dev;
+    for (int i = 0; i < m; i++) {
+      const fsim_host_job& h = jobs[k0 + i];
+      const Plan* p = reinterpret_cast<const Plan*>(h.plan);
+      dj[i].plan = h.plan;
+      dj[i].raw = cur;
+      FSIM_CUDA(cudaMemcpyAsync(cur, h.raw_host, raw_bytes(p), cudaMemcpyHostToDevice, P.s_up));
+      cur += a256(raw_bytes(p));
+      dj[i].out = reinterpret_cast<float*>(cur);
+      cur += a256(out_bytes(p));
+      dj[i].widefield = nullptr;
+      if (h.widefield_host) {
+        dj[i].widefield = reinterpret_cast<float*>(cur);
+        cur += a256(wf_bytes(p));
+      }
+    }
+    FSIM_CUDA(cudaEventRecord(S.up, P.s_up));
+    FSIM_CUDA(cudaStreamWaitEvent(P.s_comp, S.up, 0));
+    rc = recon_batch(dj.data(), m, cur, S.bytes - (size_t)(cur - S.dev), P.s_comp, S.table, true);
+    if (rc) {
+      cudaStreamSynchronize(P.s_up);
+      cudaStreamSynchronize(P.s_comp);
+      cudaStreamSynchronize(P.s_down);
+      return rc;
+    }
+    FSIM_CUDA(cudaEventRecord(S.done, P.s_comp));
+    FSIM_CUDA(cudaStreamWaitEvent(P.s_down, S.done, 0));
+    for (int i = 0; i < m; i++) {
+      const fsim_host_job& h = jobs[k0 + i];
+      const Plan* p = reinterpret_cast<const Plan*>(h.plan);
+      FSIM_CUDA(cudaMemcpyAsync(h.out_host, dj[i].out, out_bytes(p), cudaMemcpyDeviceToHost, P.s_down));
+      if (h.widefield_host)
+        FSIM_CUDA(cudaMemcpyAsync(h.widefield_host, dj[i].widefield, wf_bytes(p), cudaMemcpyDeviceToHost, P.s_down));
+    }
+    FSIM_CUDA(cudaEventRecord(S.down, P.s_down));
+    S.used = true;
+  }
+  FSIM_CUDA(cudaStreamSynchronize(P.s_down));
+  FSIM_CUDA(cudaStreamSynchronize(P.s_comp));
+  return FSIM_OK;
+}

@@ -11,6 +11,16 @@
 
 struct fsim_plan : fsim::Plan {};
 
+// A fixed batch recorded as a CUDA graph (fsim_batch_graph_*).
+struct fsim_batch_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  void* table = nullptr;  // pinned job table, copied to the workspace head by every replay
+  cudaStream_t aux[3] = {};
+  int n_jobs = 0;
+  int kernels = 0;
+};
+
 namespace fsim {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -47,7 +57,7 @@ static int get_staging(size_t bytes, Staging** out) {
 
 // Fill job tables and launch: jobs are grouped by (path, size) with one set of passes each.
 int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStream_t st, JobDesc* host_table,
-                bool upload_table) {
+                bool upload_table, const cudaStream_t* aux, int naux) {
   FSIM_REQUIRE(jobs && n > 0, FSIM_EINVAL, "recon_batch: no jobs");
   std::vector<int> order(n);
   for (int i = 0; i < n; i++) {
@@ -75,20 +85,61 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
     cur += align256(plan_ws(p));
   }
   if (upload_table) FSIM_CUDA(cudaMemcpyAsync(d_table, host_table, sizeof(JobDesc) * n, cudaMemcpyHostToDevice, st));
-  int k = 0;
-  while (k < n) {
-    const Plan* p0 = static_cast<const Plan*>(jobs[order[k]].plan);
-    int e = k, maxA = 0, maxP = 0;
-    while (e < n && key(order[e]) == key(order[k])) {
-      maxA = std::max(maxA, static_cast<const Plan*>(jobs[order[e]].plan)->prm.nr_dirs);
-      maxP = std::max(maxP, static_cast<const Plan*>(jobs[order[e]].plan)->prm.nr_phases);
-      e++;
-    }
-    int rc = (p0->path == FSIM_PATH_LIVE) ? launch_live_size(p0->prm.w, d_table + k, e - k, maxA, st)
-                                          : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxP, st);
-    if (rc) return rc;
+  // size classes: [start, end) ranges of the sorted table
+  std::vector<std::pair<int, int>> groups;
+  for (int k = 0; k < n;) {
+    int e = k;
+    while (e < n && key(order[e]) == key(order[k])) e++;
+    groups.emplace_back(k, e);
     k = e;
   }
+  // per-pass profiling times one stream's passes: no fork while it is on
+  const int nfork = (profile_events() || !aux) ? 0 : std::min<int>(naux, (int)groups.size() - 1);
+  cudaEvent_t fork_ev = nullptr, join_ev[8] = {};
+  if (nfork > 0) {
+    FSIM_REQUIRE(nfork <= 8, FSIM_EINVAL, "recon_batch: at most 8 auxiliary streams");
+    FSIM_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    FSIM_CUDA(cudaEventRecord(fork_ev, st));
+    for (int i = 0; i < nfork; i++) {
+      FSIM_CUDA(cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming));
+      FSIM_CUDA(cudaStreamWaitEvent(aux[i], fork_ev, 0));
+    }
+  }
+  int rc = FSIM_OK;
+  for (size_t g = 0; g < groups.size() && rc == FSIM_OK; g++) {
+    const int k = groups[g].first, e = groups[g].second;
+    const Plan* p0 = static_cast<const Plan*>(jobs[order[k]].plan);
+    int maxA = 0, maxP = 0;
+    for (int i = k; i < e; i++) {
+      maxA = std::max(maxA, static_cast<const Plan*>(jobs[order[i]].plan)->prm.nr_dirs);
+      maxP = std::max(maxP, static_cast<const Plan*>(jobs[order[i]].plan)->prm.nr_phases);
+    }
+    // largest classes sort last; the first class stays on st, the rest spread over aux
+    cudaStream_t s = (nfork > 0 && g > 0) ? aux[(g - 1) % nfork] : st;
+    rc = (p0->path == FSIM_PATH_LIVE) ? launch_live_size(p0->prm.w, d_table + k, e - k, maxA, s)
+                                      : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxP, s);
+  }
+  if (nfork > 0) {
+    // join even after a failed launch, so that a capture in progress can still end
+    for (int i = 0; i < nfork; i++) {
+      cudaEventRecord(join_ev[i], aux[i]);
+      cudaStreamWaitEvent(st, join_ev[i], 0);
+      cudaEventDestroy(join_ev[i]);
+    }
+    cudaEventDestroy(fork_ev);
+  }
+  return rc;
+}
+
+// auxiliary streams of fsim_recon_batch: the size classes of one batch run side by side
+constexpr int FSIM_AUX_STREAMS = 3;
+static std::mutex g_aux_mu;
+static cudaStream_t g_aux[FSIM_AUX_STREAMS] = {};
+
+static int aux_streams(cudaStream_t** out) {
+  if (!g_aux[0])
+    for (auto& a : g_aux) FSIM_CUDA(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+  *out = g_aux;
   return FSIM_OK;
 }
 
@@ -117,10 +168,12 @@ using namespace fsim;
 extern "C" {
 
 int fsim_plan_create(fsim_plan** out, const fsim_sim_param* p, int path, int input_type, int fade_px, double bgr) {
-  NEED_INIT();
   FSIM_REQUIRE(out, FSIM_EINVAL, "null output pointer");
+  *out = nullptr;
   int rc = validate_param(p);
   if (rc) return rc;
+  FSIM_REQUIRE(fade_px >= 0 && 2 * fade_px <= p->w, FSIM_EINVAL, "fade of %d pixels on a %d-pixel image", fade_px,
+               p->w);
   FSIM_REQUIRE(path == FSIM_PATH_OFFLINE || path == FSIM_PATH_LIVE, FSIM_EINVAL, "unknown path %d", path);
   FSIM_REQUIRE(input_type == FSIM_INPUT_F32 || input_type == FSIM_INPUT_U16, FSIM_EINVAL, "unknown input type");
   if (path == FSIM_PATH_OFFLINE)
@@ -128,6 +181,7 @@ int fsim_plan_create(fsim_plan** out, const fsim_sim_param* p, int path, int inp
   else
     FSIM_REQUIRE(live_size_supported(p->w), FSIM_EINVAL, "live reconstruction: unsupported image size %d", p->w);
   FSIM_REQUIRE(p->nr_phases <= FSIM_MAX_PHASES && 2 * p->nr_bands - 1 <= 7, FSIM_EINVAL, "too many phases/bands");
+  NEED_INIT();
   fsim_plan* pl = new fsim_plan();
   pl->prm = *p;
   pl->path = path;
@@ -182,14 +236,124 @@ int fsim_plan_info(const fsim_plan* plan, int* w, int* path, int* input_type) {
 }
 
 int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t workspace_bytes, void* stream) {
+  FSIM_REQUIRE(jobs && n_jobs > 0, FSIM_EINVAL, "recon_batch: no jobs");
   NEED_INIT();
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx().stream;
   Staging* s = nullptr;
   int rc = get_staging(sizeof(JobDesc) * std::max(1, n_jobs), &s);
   if (rc) return rc;
-  rc = recon_batch(jobs, n_jobs, workspace, workspace_bytes, st, (JobDesc*)s->ptr, true);
+  {
+    // the shared auxiliary streams carry one caller's fork/join at a time
+    std::lock_guard<std::mutex> g(g_aux_mu);
+    cudaStream_t* aux = nullptr;
+    rc = aux_streams(&aux);
+    if (rc) return rc;
+    rc = recon_batch(jobs, n_jobs, workspace, workspace_bytes, st, (JobDesc*)s->ptr, true, aux, FSIM_AUX_STREAMS);
+  }
   if (rc) return rc;
   FSIM_CUDA(cudaEventRecord(s->done, st));
+  return FSIM_OK;
+}
+
+int fsim_batch_graph_create(fsim_batch_graph** out, const fsim_job* jobs, int n_jobs, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+  FSIM_REQUIRE(out && jobs && n_jobs > 0, FSIM_EINVAL, "batch_graph_create: bad arguments");
+  *out = nullptr;
+  NEED_INIT();
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx().stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  FSIM_CUDA(cudaStreamIsCapturing(st, &cs));
+  FSIM_REQUIRE(cs == cudaStreamCaptureStatusNone, FSIM_EINVAL, "batch_graph_create: stream is already capturing");
+  fsim_batch_graph* g = new fsim_batch_graph();
+  g->n_jobs = n_jobs;
+  auto fail = [&](int rc) {
+    for (auto a : g->aux)
+      if (a) cudaStreamDestroy(a);
+    if (g->table) cudaFreeHost(g->table);
+    delete g;
+    return rc;
+  };
+  // the job table lives in pinned memory owned by the graph; every replay copies it to the
+  // workspace head before the passes, so the graph does not depend on what else used the
+  // workspace in between
+  if (cudaMallocHost(&g->table, sizeof(JobDesc) * n_jobs) != cudaSuccess) {
+    set_error("batch_graph_create: pinned table allocation failed");
+    return fail(FSIM_EOOM);
+  }
+  for (auto& a : g->aux)
+    if (cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking) != cudaSuccess) {
+      set_error("batch_graph_create: stream creation failed");
+      return fail(FSIM_ECUDA);
+    }
+  const bool prof = g_prof_on;
+  g_prof_on = false;  // profiling events are not recorded inside a graph
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+  int rc = FSIM_OK;
+  if (e != cudaSuccess) {
+    set_error("batch_graph_create: begin capture: %s", cudaGetErrorString(e));
+    rc = FSIM_ECUDA;
+  } else {
+    rc = recon_batch(jobs, n_jobs, workspace, workspace_bytes, st, static_cast<JobDesc*>(g->table), true, g->aux,
+                     FSIM_AUX_STREAMS);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(st, &graph);
+    if (rc == FSIM_OK && e != cudaSuccess) {
+      set_error("batch_graph_create: end capture: %s", cudaGetErrorString(e));
+      rc = FSIM_ECUDA;
+    }
+    g->graph = graph;
+  }
+  g_prof_on = prof;
+  if (rc == FSIM_OK) {
+    e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) {
+      set_error("batch_graph_create: instantiate: %s", cudaGetErrorString(e));
+      rc = FSIM_ECUDA;
+    }
+  }
+  if (rc == FSIM_OK) {
+    size_t nn = 0;
+    cudaGraphGetNodes(g->graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(g->graph, nodes.data(), &nn);
+    for (auto nd : nodes) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) g->kernels++;
+    }
+  }
+  if (rc != FSIM_OK) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    cudaGetLastError();
+    return fail(rc);
+  }
+  *out = g;
+  return FSIM_OK;
+}
+
+int fsim_batch_graph_launch(fsim_batch_graph* g, void* stream) {
+  FSIM_REQUIRE(g && g->exec, FSIM_EINVAL, "batch_graph_launch: null graph");
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx().stream;
+  FSIM_CUDA(cudaGraphLaunch(g->exec, st));
+  return FSIM_OK;
+}
+
+int fsim_batch_graph_info(const fsim_batch_graph* g, int* n_jobs, int* n_kernels) {
+  FSIM_REQUIRE(g, FSIM_EINVAL, "batch_graph_info: null graph");
+  if (n_jobs) *n_jobs = g->n_jobs;
+  if (n_kernels) *n_kernels = g->kernels;
+  return FSIM_OK;
+}
+
+int fsim_batch_graph_destroy(fsim_batch_graph* g) {
+  if (!g) return FSIM_OK;
+  cudaDeviceSynchronize();
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  for (auto a : g->aux)
+    if (a) cudaStreamDestroy(a);
+  if (g->table) cudaFreeHost(g->table);
+  delete g;
   return FSIM_OK;
 }
 
@@ -238,12 +402,12 @@ int fsim_recon_host(fsim_plan* plan, const void* raw_host, float* out_host) {
   const size_t ws = align256(sizeof(JobDesc)) + align256(plan_ws(plan));
   if (plan->h_ws_bytes < ws) {
     if (plan->h_ws) cudaFree(plan->h_ws);
-    FSIM_CUDA(cudaMalloc(&plan->h_ws, ws));
+    FSIM_CUDA(fsim::dev_alloc(&plan->h_ws, ws));
     plan->h_ws_bytes = ws;
   }
   if (plan->h_io_bytes < align256(raw_bytes) + out_bytes) {
     if (plan->h_io) cudaFree(plan->h_io);
-    FSIM_CUDA(cudaMalloc(&plan->h_io, align256(raw_bytes) + out_bytes));
+    FSIM_CUDA(fsim::dev_alloc(&plan->h_io, align256(raw_bytes) + out_bytes));
     plan->h_io_bytes = align256(raw_bytes) + out_bytes;
   }
   if (!plan->h_job) FSIM_CUDA(cudaMallocHost(&plan->h_job, sizeof(JobDesc)));

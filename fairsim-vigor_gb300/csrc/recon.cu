@@ -161,7 +161,7 @@ int Plan::build(cudaStream_t st) {
   if (total > dev_bytes) {
     if (dev) cudaFree(dev);
     dev = nullptr;
-    FSIM_CUDA(cudaMalloc(&dev, total));
+    FSIM_CUDA(fsim::dev_alloc(&dev, total));
     dev_bytes = total;
   }
   char* b = (char*)dev;

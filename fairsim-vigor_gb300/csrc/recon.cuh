@@ -69,4 +69,11 @@ bool live_size_supported(int n);
 int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st);
 int launch_live_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);
 
+// Fill the job table of a batch (sorted by path and size) into host_table, optionally copy it
+// to the head of the workspace, and launch every size class's passes. With aux streams, the
+// size classes after the first run on them, forked from and joined back into st by events.
+int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStream_t st, JobDesc* host_table,
+                bool upload_table, const cudaStream_t* aux = nullptr, int naux = 0);
+size_t plan_ws(const Plan* p);
+
 }  // namespace fsim

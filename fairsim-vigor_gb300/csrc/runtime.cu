@@ -1,4 +1,5 @@
 // Library runtime: error state, device/stream context, FFT twiddle tables.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <mutex>
@@ -19,6 +20,37 @@ void set_error(const char* fmt, ...) {
   va_end(ap);
 }
 const char* last_error() { return g_errbuf; }
+
+// Test hook: the n-th next device allocation of the library fails (fsim_debug_fail_alloc).
+static std::atomic<int> g_fail_alloc{0};
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+  int n = g_fail_alloc.load();
+  while (n > 0) {
+    if (g_fail_alloc.compare_exchange_weak(n, n - 1)) {
+      if (n == 1) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+      }
+      break;
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
+
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t st) {
+  int n = g_fail_alloc.load();
+  while (n > 0) {
+    if (g_fail_alloc.compare_exchange_weak(n, n - 1)) {
+      if (n == 1) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+      }
+      break;
+    }
+  }
+  return cudaMallocAsync(p, bytes, st);
+}
 
 static std::mutex g_mu;
 static Ctx g_ctx;
@@ -94,7 +126,7 @@ int ensure_init() {
     FSIM_CUDA(cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking));
     g_ctx.own_stream = true;
   }
-  FSIM_CUDA(cudaMalloc(&g_ctx.red, sizeof(double) * RED_SLOTS));
+  FSIM_CUDA(fsim::dev_alloc(&g_ctx.red, sizeof(double) * RED_SLOTS));
   FSIM_CUDA(cudaMallocHost(&g_ctx.red_host, sizeof(double) * RED_SLOTS));
   cudaDeviceProp prop;
   FSIM_CUDA(cudaGetDeviceProperties(&prop, g_ctx.device));
@@ -133,6 +165,12 @@ int fsim_sync(void) {
 }
 
 int fsim_version(void) { return 10000; }
+
+int fsim_debug_fail_alloc(int nth) {
+  FSIM_REQUIRE(nth >= 0, FSIM_EINVAL, "debug_fail_alloc: nth must be >= 0");
+  fsim::g_fail_alloc.store(nth);
+  return FSIM_OK;
+}
 
 int fsim_set_stream(void* stream) {
   int rc = fsim::ensure_init();

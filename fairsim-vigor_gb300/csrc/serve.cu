@@ -18,6 +18,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <string>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -29,11 +30,6 @@
 #include "runtime.cuh"
 #include "sim_host.h"
 
-namespace fsim {
-int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStream_t st, JobDesc* host_table,
-                bool upload_table);
-size_t plan_ws(const Plan* p);
-}  // namespace fsim
 
 using namespace fsim;
 using clk = std::chrono::steady_clock;
@@ -60,6 +56,7 @@ struct fsim_server {
     float* h_out = nullptr;
     float* d_out = nullptr;
     int state = FREE;
+    bool cancelled = false;  // the client gave the ticket up; the slot frees itself when done
     uint64_t ticket = 0;
     int channel = 0;
     double t_submit = 0, t_done = 0;
@@ -90,7 +87,7 @@ struct fsim_server {
   bool stop = false;
   // stats
   std::vector<double> lat;
-  uint64_t submitted = 0, completed = 0, rejected = 0, refits = 0;
+  uint64_t submitted = 0, completed = 0, rejected = 0, refits = 0, cancelled = 0;
   double t_first = 0, t_last = 0;
 };
 
@@ -107,6 +104,13 @@ static void CUDART_CB on_batch_done(void* arg) {
       s->lat.push_back(t - sl.t_submit);
       s->completed++;
       s->t_last = t;
+      if (sl.cancelled) {
+        sl.state = fsim_server::FREE;
+        sl.cancelled = false;
+        s->by_ticket.erase(sl.ticket);
+        sl.ticket = 0;
+        s->free_list.push_back(i);
+      }
     }
   }
   s->cv_done.notify_all();
@@ -206,7 +210,7 @@ static void refit_loop(fsim_server* s) {
     int rc = FSIM_OK;
     // ParameterRefitThread.doRefit on the device: damp, FFT, estimate (live mode)
     float2* spec = nullptr;
-    if (cudaMallocAsync(&spec, sizeof(float2) * n * frames, st) != cudaSuccess) rc = FSIM_EOOM;
+    if (fsim::dev_alloc_async(&spec, sizeof(float2) * n * frames, st) != cudaSuccess) rc = FSIM_EOOM;
     if (!rc) {
       extern int refit_spectra(const fsim_sim_param* p, const void* raw, int input_u16, int fade, float2* spec,
                                cudaStream_t st);
@@ -248,7 +252,7 @@ int refit_spectra(const fsim_sim_param* p, const void* raw, int input_u16, int f
   float* damp = nullptr;
   if (fade > 0) {
     std::vector<float> h = fade_vector(N, N, fade);
-    FSIM_CUDA(cudaMallocAsync(&damp, sizeof(float) * n, st));
+    FSIM_CUDA(fsim::dev_alloc_async(&damp, sizeof(float) * n, st));
     FSIM_CUDA(cudaMemcpyAsync(damp, h.data(), sizeof(float) * n, cudaMemcpyHostToDevice, st));
     FSIM_CUDA(cudaStreamSynchronize(st));
   }
@@ -260,13 +264,41 @@ int refit_spectra(const fsim_sim_param* p, const void* raw, int input_u16, int f
 
 extern "C" {
 
+static int serve_setup(fsim_server* s, const fsim_serve_config* cfg, const fsim_sim_param* channels,
+                       int n_channels);
+
 int fsim_serve_open(fsim_server** out, const fsim_serve_config* cfg, const fsim_sim_param* channels, int n_channels) {
-  int rc = ensure_init();
-  if (rc) return rc;
   FSIM_REQUIRE(out && cfg && channels && n_channels > 0, FSIM_EINVAL, "serve_open: bad arguments");
+  *out = nullptr;
   FSIM_REQUIRE(cfg->max_batch > 0 && cfg->max_inflight > 0 && cfg->streams > 0, FSIM_EINVAL,
                "serve_open: max_batch, max_inflight and streams must be positive");
+  FSIM_REQUIRE(cfg->input_type == FSIM_INPUT_U16 || cfg->input_type == FSIM_INPUT_F32, FSIM_EINVAL,
+               "serve_open: unknown input type %d", cfg->input_type);
+  for (int c = 0; c < n_channels; c++) {
+    int rc = validate_param(&channels[c]);
+    if (rc) return rc;
+    FSIM_REQUIRE(live_size_supported(channels[c].w), FSIM_EINVAL, "serve_open: channel %d: unsupported size %d", c,
+                 channels[c].w);
+  }
+  int rc = ensure_init();
+  if (rc) return rc;
   auto* s = new fsim_server();
+  rc = serve_setup(s, cfg, channels, n_channels);
+  if (rc) {
+    const std::string msg = last_error();
+    fsim_serve_close(s);  // releases whatever was set up
+    set_error("%s", msg.c_str());
+    return rc;
+  }
+  s->worker = std::thread(worker_loop, s);
+  s->refitter = std::thread(refit_loop, s);
+  *out = s;
+  return FSIM_OK;
+}
+
+static int serve_setup(fsim_server* s, const fsim_serve_config* cfg, const fsim_sim_param* channels,
+                       int n_channels) {
+  int rc = FSIM_OK;
   s->cfg = *cfg;
   s->ch.resize(n_channels);
   size_t max_raw = 0, max_out = 0, max_ws = 0;
@@ -277,16 +309,13 @@ int fsim_serve_open(fsim_server** out, const fsim_serve_config* cfg, const fsim_
     for (int k = 0; k < 2; k++) {
       fsim_plan* pl = nullptr;
       rc = fsim_plan_create(&pl, &channels[c], FSIM_PATH_LIVE, cfg->input_type, cfg->fade_px, 0.0);
-      if (rc) {
-        fsim_serve_close(s);
-        return rc;
-      }
+      if (rc) return rc;
       chn.plans[k] = reinterpret_cast<Plan*>(pl);
       cudaEventCreateWithFlags(&chn.last_use[k], cudaEventDisableTiming);
     }
     const size_t N = channels[c].w;
     chn.raw_bytes = N * N * channels[c].nr_dirs * channels[c].nr_phases * in_sz;
-    FSIM_CUDA(cudaMalloc(&chn.d_refit_raw, chn.raw_bytes));
+    FSIM_CUDA(fsim::dev_alloc(&chn.d_refit_raw, chn.raw_bytes));
     max_raw = std::max(max_raw, chn.raw_bytes);
     max_out = std::max(max_out, 4 * N * N * sizeof(float));
     max_ws = std::max(max_ws, (plan_ws(chn.plans[0]) + 255) & ~(size_t)255);
@@ -307,8 +336,8 @@ int fsim_serve_open(fsim_server** out, const fsim_serve_config* cfg, const fsim_
     auto& sl = s->slots[i];
     FSIM_CUDA(cudaMallocHost(&sl.h_raw, max_raw));
     FSIM_CUDA(cudaMallocHost(&sl.h_out, max_out));
-    FSIM_CUDA(cudaMalloc(&sl.d_raw, max_raw));
-    FSIM_CUDA(cudaMalloc(&sl.d_out, max_out));
+    FSIM_CUDA(fsim::dev_alloc(&sl.d_raw, max_raw));
+    FSIM_CUDA(fsim::dev_alloc(&sl.d_out, max_out));
     s->free_list.push_back(nslots - 1 - i);
   }
   s->streams.resize(cfg->streams);
@@ -317,21 +346,22 @@ int fsim_serve_open(fsim_server** out, const fsim_serve_config* cfg, const fsim_
   s->table_ev.resize(cfg->streams);
   for (int k = 0; k < cfg->streams; k++) {
     FSIM_CUDA(cudaStreamCreateWithFlags(&s->streams[k], cudaStreamNonBlocking));
-    FSIM_CUDA(cudaMalloc(&s->ws[k], s->ws_bytes));
+    FSIM_CUDA(fsim::dev_alloc(&s->ws[k], s->ws_bytes));
     FSIM_CUDA(cudaMallocHost(&s->tables[k], sizeof(JobDesc) * cfg->max_batch));
     FSIM_CUDA(cudaEventCreateWithFlags(&s->table_ev[k], cudaEventDisableTiming));
   }
   FSIM_CUDA(cudaStreamCreateWithFlags(&s->refit_stream, cudaStreamNonBlocking));
   FSIM_CUDA(cudaDeviceSynchronize());
-  s->worker = std::thread(worker_loop, s);
-  s->refitter = std::thread(refit_loop, s);
-  *out = s;
   return FSIM_OK;
 }
 
-int fsim_serve_submit(fsim_server* s, int channel, const void* raw_host, uint64_t* ticket) {
+int fsim_serve_submit(fsim_server* s, int channel, const void* raw_host, size_t raw_bytes, uint64_t* ticket) {
   FSIM_REQUIRE(s && raw_host && ticket, FSIM_EINVAL, "serve_submit: bad arguments");
   FSIM_REQUIRE(channel >= 0 && channel < (int)s->ch.size(), FSIM_EINVAL, "serve_submit: no channel %d", channel);
+  FSIM_REQUIRE(raw_bytes == s->ch[channel].raw_bytes, FSIM_EINVAL,
+               "serve_submit: stack of %zu bytes for channel %d, which takes %zu (%d frames of %d x %d)", raw_bytes,
+               channel, s->ch[channel].raw_bytes, s->ch[channel].prm.nr_dirs * s->ch[channel].prm.nr_phases,
+               s->ch[channel].prm.w, s->ch[channel].prm.w);
   int i;
   {
     std::lock_guard<std::mutex> g(s->mu);
@@ -369,16 +399,51 @@ int fsim_serve_wait(fsim_server* s, uint64_t ticket, float* out_host, int timeou
   FSIM_REQUIRE(it != s->by_ticket.end(), FSIM_ENOTFOUND, "serve_wait: unknown ticket %llu", (unsigned long long)ticket);
   const int i = it->second;
   auto& sl = s->slots[i];
-  if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return sl.state == fsim_server::DONE; })) {
+  FSIM_REQUIRE(!sl.cancelled, FSIM_ENOTFOUND, "serve_wait: ticket %llu was cancelled", (unsigned long long)ticket);
+  // the slot may be cancelled by another thread (and reused) while this one waits
+  auto mine = [&] { return sl.ticket == ticket && !sl.cancelled; };
+  if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms),
+                           [&] { return !mine() || sl.state == fsim_server::DONE; })) {
     set_error("serve_wait: ticket %llu not done after %d ms", (unsigned long long)ticket, timeout_ms);
     return FSIM_ETIMEOUT;
   }
+  FSIM_REQUIRE(mine(), FSIM_ENOTFOUND, "serve_wait: ticket %llu was cancelled while waiting",
+               (unsigned long long)ticket);
   const size_t W = 2 * (size_t)s->ch[sl.channel].prm.w;
   std::memcpy(out_host, sl.h_out, W * W * sizeof(float));
   if (latency_ms) *latency_ms = sl.t_done - sl.t_submit;
   sl.state = fsim_server::FREE;
-  s->by_ticket.erase(it);
+  s->by_ticket.erase(ticket);
   s->free_list.push_back(i);
+  return FSIM_OK;
+}
+
+int fsim_serve_cancel(fsim_server* s, uint64_t ticket) {
+  FSIM_REQUIRE(s, FSIM_EINVAL, "serve_cancel: null server");
+  std::lock_guard<std::mutex> g(s->mu);
+  auto it = s->by_ticket.find(ticket);
+  FSIM_REQUIRE(it != s->by_ticket.end(), FSIM_ENOTFOUND, "serve_cancel: unknown ticket %llu",
+               (unsigned long long)ticket);
+  const int i = it->second;
+  auto& sl = s->slots[i];
+  FSIM_REQUIRE(!sl.cancelled, FSIM_ENOTFOUND, "serve_cancel: ticket %llu already cancelled", (unsigned long long)ticket);
+  s->cancelled++;
+  if (sl.state == fsim_server::PENDING) {
+    // not started: drop it from the queue and free the slot now
+    s->pending.erase(std::find(s->pending.begin(), s->pending.end(), i));
+    sl.state = fsim_server::FREE;
+    sl.ticket = 0;
+    s->by_ticket.erase(it);
+    s->free_list.push_back(i);
+  } else if (sl.state == fsim_server::DONE) {
+    sl.state = fsim_server::FREE;
+    sl.ticket = 0;
+    s->by_ticket.erase(it);
+    s->free_list.push_back(i);
+  } else {
+    sl.cancelled = true;  // on the GPU: the completion callback frees the slot
+  }
+  s->cv_done.notify_all();
   return FSIM_OK;
 }
 
@@ -390,6 +455,7 @@ int fsim_serve_stats_get(fsim_server* s, fsim_serve_stats* out) {
   out->completed = s->completed;
   out->rejected = s->rejected;
   out->refits = s->refits;
+  out->cancelled = s->cancelled;
   if (!s->lat.empty()) {
     std::vector<double> v = s->lat;
     std::sort(v.begin(), v.end());

@@ -341,10 +341,10 @@ int fsim_vec_create(fsim_vec** out, int w, int h, int is_complex) {
   v->cplx = is_complex ? 1 : 0;
   v->n = (size_t)w * h;
   size_t bytes = v->floats() * sizeof(float);
-  cudaError_t e = cudaMalloc(&v->d, bytes);
+  cudaError_t e = fsim::dev_alloc(&v->d, bytes);
   if (e != cudaSuccess) {
     delete v;
-    set_error("fsim_vec_create: cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    set_error("fsim_vec_create: device allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
     return FSIM_EOOM;
   }
   FSIM_CUDA(cudaMemsetAsync(v->d, 0, bytes, ctx().stream));
@@ -392,7 +392,7 @@ int fsim_vec_upload_u16(fsim_vec* v, const uint16_t* host) {
   NEED_VEC(v);
   Ctx& c = ctx();
   uint16_t* tmp = nullptr;
-  FSIM_CUDA(cudaMallocAsync(&tmp, v->n * sizeof(uint16_t), c.stream));
+  FSIM_CUDA(fsim::dev_alloc_async(&tmp, v->n * sizeof(uint16_t), c.stream));
   FSIM_CUDA(cudaMemcpyAsync(tmp, host, v->n * sizeof(uint16_t), cudaMemcpyHostToDevice, c.stream));
   if (v->cplx)
     k_u16_to_c<<<grid_for(v->n, 256), 256, 0, c.stream>>>(reinterpret_cast<float2*>(v->d), tmp, v->n);

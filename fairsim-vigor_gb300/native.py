@@ -25,6 +25,32 @@ class FsimError(RuntimeError):
         self.code = code
 
 
+# Status codes map to exception types the way the reference's JNI layer maps failures to
+# Java exceptions: bad sizes/arguments -> IllegalArgument/RuntimeException (Vec.failSize),
+# allocation failure -> OutOfMemoryError (AccelVectorCplx.java:51-54).
+class FsimInvalidArgument(FsimError, ValueError):
+    pass
+
+
+class FsimOutOfMemory(FsimError, MemoryError):
+    pass
+
+
+class FsimTimeout(FsimError, TimeoutError):
+    pass
+
+
+class FsimBusy(FsimError):
+    pass
+
+
+class FsimNotFound(FsimError, KeyError):
+    pass
+
+
+_ERRORS = {-1: FsimInvalidArgument, -2: FsimOutOfMemory, -4: FsimTimeout, -5: FsimBusy, -6: FsimNotFound}
+
+
 class SimParamC(C.Structure):
     _fields_ = [
         ("w", C.c_int32),
@@ -54,6 +80,9 @@ class Job(C.Structure):
     _fields_ = [("plan", C.c_void_p), ("raw", C.c_void_p), ("out", C.c_void_p), ("widefield", C.c_void_p)]
 
 
+HostJob = Job  # fsim_host_job: same four pointer fields, host addresses
+
+
 class ServeConfig(C.Structure):
     _fields_ = [
         ("max_batch", C.c_int32),
@@ -78,6 +107,7 @@ class ServeStats(C.Structure):
         ("max_ms", C.c_double),
         ("recon_per_s", C.c_double),
         ("wall_s", C.c_double),
+        ("cancelled", C.c_uint64),
     ]
 
 
@@ -159,6 +189,11 @@ _SIGS = {
     "fsim_plan_filter_bytes": (C.c_size_t, [VP]),
     "fsim_plan_info": (I32, [VP, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
     "fsim_recon_batch": (I32, [VP, I32, VP, C.c_size_t, VP]),
+    "fsim_recon_batch_host": (I32, [VP, I32, I32]),
+    "fsim_batch_graph_create": (I32, [VP, VP, I32, VP, C.c_size_t, VP]),
+    "fsim_batch_graph_launch": (I32, [VP, VP]),
+    "fsim_batch_graph_info": (I32, [VP, VP, VP]),
+    "fsim_batch_graph_destroy": (I32, [VP]),
     "fsim_recon_host": (I32, [VP, VP, VP]),
     "fsim_tune_set": (I32, [I32, I32, I32, I32]),
     "fsim_tune_get": (I32, [I32, I32, I32, C.POINTER(I32), C.POINTER(I32)]),
@@ -168,7 +203,9 @@ _SIGS = {
     "fsim_live_refit": (I32, [VP, VP, VP]),
     "fsim_corr_grid_noalloc": (I32, [VP, VP, I32, VP, I32, VP, I32, F64, VP, VP]),
     "fsim_serve_open": (I32, [C.POINTER(VP), VP, VP, I32]),
-    "fsim_serve_submit": (I32, [VP, I32, VP, C.POINTER(C.c_uint64)]),
+    "fsim_serve_submit": (I32, [VP, I32, VP, C.c_size_t, C.POINTER(C.c_uint64)]),
+    "fsim_serve_cancel": (I32, [VP, C.c_uint64]),
+    "fsim_debug_fail_alloc": (I32, [I32]),
     "fsim_serve_wait": (I32, [VP, C.c_uint64, VP, I32, C.POINTER(F64)]),
     "fsim_serve_stats_get": (I32, [VP, VP]),
     "fsim_serve_params": (I32, [VP, I32, VP]),
@@ -202,7 +239,7 @@ def lib():
 def check(rc):
     if rc != FSIM_OK:
         msg = lib().fsim_last_error()
-        raise FsimError(rc, msg.decode() if msg else "")
+        raise _ERRORS.get(rc, FsimError)(rc, msg.decode() if msg else "")
     return rc
 
 
@@ -226,8 +263,17 @@ def apply_tuning(path=None):
     return True
 
 
-def init(device=0, apply_tuning=True):
+_device = None
+
+
+def init(device=None, apply_tuning=True):
+    """Initialise the library on `device` (None: the device chosen before, else 0) and apply
+    the autotuner's launch shapes once."""
+    global _device
+    if device is None:
+        device = _device if _device is not None else 0
     check(lib().fsim_init(device))
+    _device = device
     if apply_tuning and not _tuned:
         globals()["apply_tuning"]()
     return FSIM_OK

@@ -18,13 +18,22 @@ from . import native as N
 
 class ReconPlan:
     def __init__(self, sp, path=N.PATH_OFFLINE, input_type=N.INPUT_F32, fade_px=10, bgr=0.0):
-        N.init()
         self.sp = sp
         self.path, self.input_type = path, input_type
         h = C.c_void_p()
         self._c = N.to_c_param(sp)
-        N.check(N.lib().fsim_plan_create(C.byref(h), C.byref(self._c), int(path), int(input_type), int(fade_px), float(bgr)))
-        self._h = h
+        if N._device is None:
+            # the library checks the arguments before it touches a device: malformed
+            # parameters raise ValueError even on a host without a GPU
+            N.check(N.lib().fsim_plan_create(C.byref(h), C.byref(self._c), int(path), int(input_type), int(fade_px),
+                                             float(bgr)))
+            self._h = h
+            N.init()
+        else:
+            N.init()
+            N.check(N.lib().fsim_plan_create(C.byref(h), C.byref(self._c), int(path), int(input_type), int(fade_px),
+                                             float(bgr)))
+            self._h = h
 
     @property
     def handle(self):
@@ -76,8 +85,7 @@ def batch_workspace_bytes(plans) -> int:
     return job_table + sum((p.workspace_bytes() + 255) // 256 * 256 for p in plans)
 
 
-def recon_batch(jobs, workspace_ptr: int, workspace_bytes: int, stream_ptr: int = 0):
-    """jobs: iterable of (plan, raw_device_ptr, out_device_ptr[, widefield_device_ptr])."""
+def _job_array(jobs):
     jobs = list(jobs)
     arr = (N.Job * len(jobs))()
     for i, j in enumerate(jobs):
@@ -85,8 +93,54 @@ def recon_batch(jobs, workspace_ptr: int, workspace_bytes: int, stream_ptr: int 
         arr[i].raw = j[1]
         arr[i].out = j[2]
         arr[i].widefield = j[3] if len(j) > 3 else None
-    N.check(N.lib().fsim_recon_batch(arr, len(jobs), C.c_void_p(workspace_ptr), C.c_size_t(workspace_bytes),
+    return arr
+
+
+def recon_batch(jobs, workspace_ptr: int, workspace_bytes: int, stream_ptr: int = 0):
+    """jobs: iterable of (plan, raw_device_ptr, out_device_ptr[, widefield_device_ptr])."""
+    arr = _job_array(jobs)
+    N.check(N.lib().fsim_recon_batch(arr, len(arr), C.c_void_p(workspace_ptr), C.c_size_t(workspace_bytes),
                                      C.c_void_p(stream_ptr) if stream_ptr else None))
+
+
+def recon_batch_host(jobs, chunk: int = 0):
+    """Host-buffer batch (fsim_recon_batch_host): jobs is an iterable of
+    (plan, raw_host_ptr, out_host_ptr[, widefield_host_ptr]); uploads, passes and downloads
+    of successive chunks overlap, and the call returns when every output is on the host."""
+    arr = _job_array(jobs)
+    N.check(N.lib().fsim_recon_batch_host(arr, len(arr), int(chunk)))
+
+
+class BatchGraph:
+    """A fixed batch recorded once as a CUDA graph (fsim_batch_graph_*); ``launch()``
+    replays the job-table copy and every size class's passes in one call."""
+
+    def __init__(self, jobs, workspace_ptr: int, workspace_bytes: int, stream_ptr: int = 0):
+        arr = _job_array(jobs)
+        h = C.c_void_p()
+        N.check(N.lib().fsim_batch_graph_create(C.byref(h), arr, len(arr), C.c_void_p(workspace_ptr),
+                                                C.c_size_t(workspace_bytes),
+                                                C.c_void_p(stream_ptr) if stream_ptr else None))
+        self._h = h
+
+    def launch(self, stream_ptr: int = 0):
+        N.check(N.lib().fsim_batch_graph_launch(self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def info(self):
+        nj, nk = C.c_int(), C.c_int()
+        N.check(N.lib().fsim_batch_graph_info(self._h, C.byref(nj), C.byref(nk)))
+        return {"jobs": nj.value, "kernels": nk.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().fsim_batch_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:
@@ -108,17 +162,22 @@ class Server:
     def submit(self, channel: int, raw) -> int:
         raw = np.ascontiguousarray(raw, dtype=np.uint16 if self.input_type == N.INPUT_U16 else np.float32)
         t = C.c_uint64()
-        N.check(N.lib().fsim_serve_submit(self._h, int(channel), raw.ctypes.data_as(C.c_void_p), C.byref(t)))
+        N.check(N.lib().fsim_serve_submit(self._h, int(channel), raw.ctypes.data_as(C.c_void_p), raw.nbytes,
+                                          C.byref(t)))
         return t.value
 
     def try_submit(self, channel: int, raw):
+        """submit(), or None when admission refuses the stack (FSIM_EBUSY)."""
         raw = np.ascontiguousarray(raw, dtype=np.uint16 if self.input_type == N.INPUT_U16 else np.float32)
         t = C.c_uint64()
-        rc = N.lib().fsim_serve_submit(self._h, int(channel), raw.ctypes.data_as(C.c_void_p), C.byref(t))
+        rc = N.lib().fsim_serve_submit(self._h, int(channel), raw.ctypes.data_as(C.c_void_p), raw.nbytes, C.byref(t))
         if rc == N.FSIM_EBUSY:
             return None
         N.check(rc)
         return t.value
+
+    def cancel(self, ticket: int):
+        N.check(N.lib().fsim_serve_cancel(self._h, C.c_uint64(ticket)))
 
     def wait(self, ticket: int, out=None, timeout_ms=10000):
         n = None

@@ -155,9 +155,38 @@ typedef struct fsim_job {
   float* widefield; /* device, nullable: w x w mean of the damped raw frames (live path) */
 } fsim_job;
 /* Reconstruct n_jobs datasets (mixed sizes and plans allowed) with one set of launches per
- * size class. workspace: device memory of at least the sum of fsim_plan_workspace_bytes. */
+ * size class; the size classes run side by side on library-owned streams forked from and
+ * joined back into `stream`. workspace: device memory of at least the sum of
+ * fsim_plan_workspace_bytes plus 256 bytes per job. Not for use inside a caller's stream
+ * capture (its job table is staged through reused pinned buffers): record a batch with
+ * fsim_batch_graph_create instead. */
 int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t workspace_bytes,
                      void* stream);
+/* Host-buffer batch (replaces the per-op Java-array copies of the accel vectors,
+ * AccelVectorReal.java:218-247 / AccelVectorCplx.java:296-331, for whole stacks): uploads,
+ * passes and downloads of successive chunks of `chunk` jobs (0 = about 96 MiB of raw frames)
+ * overlap on three library-owned streams; returns when every output is in host memory.
+ * Page-locked host buffers are copied by DMA; pageable ones copy synchronously. One call
+ * runs at a time per process (others wait). */
+typedef struct fsim_host_job {
+  const fsim_plan* plan;
+  const void* raw_host;  /* nr_dirs*nr_phases frames, w*w each, f32 or u16 */
+  float* out_host;       /* 2w x 2w float32 */
+  float* widefield_host; /* nullable; live-path plans only: w x w */
+} fsim_host_job;
+int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int chunk);
+/* A fixed batch recorded once as a CUDA graph (no reference counterpart): the job-table
+ * copy and every size class's passes, with the classes on parallel branches. Replays
+ * (fsim_batch_graph_launch) reconstruct the same jobs' current raw buffers into the same
+ * outputs. Plans, raw/out buffers and the workspace must stay allocated while the graph
+ * exists; fsim_plan_update keeps a plan's table addresses, so replays pick up new
+ * parameters. n_kernels: kernel launches per replay. */
+typedef struct fsim_batch_graph fsim_batch_graph;
+int fsim_batch_graph_create(fsim_batch_graph** out, const fsim_job* jobs, int n_jobs, void* workspace,
+                            size_t workspace_bytes, void* stream);
+int fsim_batch_graph_launch(fsim_batch_graph* g, void* stream);
+int fsim_batch_graph_info(const fsim_batch_graph* g, int* n_jobs, int* n_kernels);
+int fsim_batch_graph_destroy(fsim_batch_graph* g);
 /* Kernel variant per image size (no reference counterpart), chosen by the project's
  * autotuner (fairsim-vigor_gb300/autotune.py, results in tuning.json): pass 0 = row pass
  * (elements per thread), pass 1 = column pass (elements per thread x interleaved columns).
@@ -191,6 +220,11 @@ int fsim_live_refit(fsim_sim_param* p, const uint16_t* raw_device, double* peaks
 int fsim_corr_grid_noalloc(const void* b0, const void* b1, int n, const double* kx, int nx, const double* ky,
                            int ny, double scal, double* out, void* stream);
 
+/* ---- test hook (no reference counterpart) ------------------------------------------------
+ * The nth next device allocation made by the library (nth >= 1) fails as out of memory;
+ * 0 disarms. Lets tests drive every FSIM_EOOM path without exhausting a shared GPU. */
+int fsim_debug_fail_alloc(int nth);
+
 /* ---- served form: continuous batching over channels (replaces ReconstructionRunner) --- */
 typedef struct fsim_server fsim_server;
 typedef struct fsim_serve_config {
@@ -207,11 +241,19 @@ typedef struct fsim_serve_stats {
   double p50_ms, p99_ms, mean_ms, max_ms;
   double recon_per_s;
   double wall_s;
+  uint64_t cancelled;
 } fsim_serve_stats;
 int fsim_serve_open(fsim_server** out, const fsim_serve_config* cfg, const fsim_sim_param* channels,
                     int n_channels);
-/* Copies the raw stack (host) into a staging slot; FSIM_EBUSY when no slot is free. */
-int fsim_serve_submit(fsim_server* s, int channel, const void* raw_host, uint64_t* ticket);
+/* Copies the raw stack (host, raw_bytes long) into a staging slot. FSIM_EBUSY when no slot
+ * is free (the reference's live queue drops and counts the frame instead,
+ * ReconstructionRunner.java:140-150); FSIM_EINVAL when raw_bytes is not the channel's
+ * nr_dirs*nr_phases*w*w*sample size (the reference throws from Vec.failSize). */
+int fsim_serve_submit(fsim_server* s, int channel, const void* raw_host, size_t raw_bytes, uint64_t* ticket);
+/* Gives a ticket up: a queued stack is dropped, a finished one released, and one on the GPU
+ * releases its slot when its batch completes. Waiting on it afterwards gives
+ * FSIM_ENOTFOUND. */
+int fsim_serve_cancel(fsim_server* s, uint64_t ticket);
 /* Waits up to timeout_ms for the ticket; copies the 2w x 2w result to out_host. */
 int fsim_serve_wait(fsim_server* s, uint64_t ticket, float* out_host, int timeout_ms, double* latency_ms);
 int fsim_serve_stats_get(fsim_server* s, fsim_serve_stats* out);

@@ -46,3 +46,11 @@ def rel_l2(a, b):
     a = np.asarray(a, dtype=np.float64) if not np.iscomplexobj(a) else np.asarray(a, dtype=np.complex128)
     b = np.asarray(b, dtype=np.float64) if not np.iscomplexobj(b) else np.asarray(b, dtype=np.complex128)
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+@pytest.fixture(scope="session")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch

@@ -13,14 +13,6 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def torch_cuda():
-    torch = pytest.importorskip("torch")
-    if not torch.cuda.is_available():
-        pytest.skip("no CUDA device")
-    return torch
-
-
 def make(fs, n, seed, **kw):
     raw, truth = fs.synth.make_dataset(n=n, seed=seed, **kw)
     sp = fs.synth.sim_param_for(truth, n, n_dirs=kw.get("n_dirs", 3), n_phases=kw.get("n_phases", 3),
@@ -178,3 +170,124 @@ def test_every_tuned_variant_matches_oracle(fs, oracle, n):
     finally:
         fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 0, saved[0][0]))
         fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 1, saved[1][0]))
+
+
+def test_batch_graph_replays_match_batch(fs, torch_cuda):
+    """A batch recorded as a CUDA graph gives the same bits as the direct batch call, reads
+    the raw buffers' current contents on each replay, and picks up plan updates."""
+    torch = torch_cuda
+    specs = [(256, 110), (512, 111), (384, 112), (256, 113)]
+    plans, raws = [], []
+    for n, seed in specs:
+        raw, truth, sp = make(fs, n, seed)
+        plans.append(fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10))
+        raws.append(raw)
+    d_raw = [torch.from_numpy(r).cuda() for r in raws]
+    d_out = [torch.empty((2 * p.w, 2 * p.w), dtype=torch.float32, device="cuda") for p in plans]
+    ws = torch.empty(fs.plan.batch_workspace_bytes(plans), dtype=torch.uint8, device="cuda")
+    jobs = [(p, r.data_ptr(), o.data_ptr()) for p, r, o in zip(plans, d_raw, d_out)]
+    fs.plan.recon_batch(jobs, ws.data_ptr(), ws.numel())
+    torch.cuda.synchronize()
+    direct = [o.cpu().numpy().copy() for o in d_out]
+    g = fs.plan.BatchGraph(jobs, ws.data_ptr(), ws.numel())
+    assert g.info() == {"jobs": 4, "kernels": 9}  # three size classes x passes A, B, C
+    for o in d_out:
+        o.zero_()
+    g.launch()
+    torch.cuda.synchronize()
+    for o, e in zip(d_out, direct):
+        assert np.array_equal(o.cpu().numpy(), e)
+    # new pixels in a raw buffer and new parameters in a plan reach the next replay
+    raw2, truth2, sp2 = make(fs, 256, 114)
+    d_raw[0].copy_(torch.from_numpy(raw2))
+    sp3 = plans[1].sp.duplicate()
+    for d in range(3):
+        sp3.dir(d).setPhaOff(sp3.dir(d).getPhaOff() + 0.2)
+    plans[1].update(sp3)
+    g.launch()
+    torch.cuda.synchronize()
+    ref0 = fs.plan.ReconPlan(sp2, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    assert np.array_equal(d_out[0].cpu().numpy(), ref0.reconstruct_host(raw2))
+    assert np.array_equal(d_out[1].cpu().numpy(), plans[1].reconstruct_host(raws[1]))
+    g.close()
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_recon_batch_host_matches_single(fs, torch_cuda, pinned):
+    """Host-buffer batches (overlapped upload / passes / download in chunks) give the same
+    bits as each stack reconstructed alone, for mixed sizes, paths and input types."""
+    torch = torch_cuda
+    specs = [(256, 120, "off"), (512, 121, "live"), (384, 122, "off"), (256, 123, "live"), (512, 124, "off")]
+    plans, raws, singles, wfs = [], [], [], []
+    for n, seed, kind in specs:
+        live = kind == "live"
+        raw, truth, sp = make(fs, n, seed, as_u16=live)
+        p = fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE if live else fs.native.PATH_OFFLINE,
+                              input_type=fs.native.INPUT_U16 if live else fs.native.INPUT_F32, fade_px=10)
+        plans.append(p)
+        raws.append(raw)
+        singles.append(p.reconstruct_host(raw))
+    if pinned:
+        h_raw = [torch.from_numpy(r.view(np.int16) if r.dtype == np.uint16 else r).pin_memory() for r in raws]
+        h_out = [torch.empty((2 * p.w, 2 * p.w), dtype=torch.float32).pin_memory() for p in plans]
+        ptr = lambda t: t.data_ptr()  # noqa: E731
+        get = lambda t: t.numpy()  # noqa: E731
+    else:
+        h_raw = [np.ascontiguousarray(r) for r in raws]
+        h_out = [np.empty((2 * p.w, 2 * p.w), np.float32) for p in plans]
+        ptr = lambda a: a.ctypes.data  # noqa: E731
+        get = lambda a: a  # noqa: E731
+    h_wf = [np.empty((p.w, p.w), np.float32) if p.path == fs.native.PATH_LIVE else None for p in plans]
+    jobs = [(p, ptr(r), ptr(o), w.ctypes.data if w is not None else None) for p, r, o, w in zip(plans, h_raw, h_out, h_wf)]
+    fs.plan.recon_batch_host(jobs, chunk=2)
+    for o, s in zip(h_out, singles):
+        assert np.array_equal(get(o), s)
+    for p, w, r in zip(plans, h_wf, raws):
+        if w is not None:
+            d_raw = torch.from_numpy(r.view(np.int16)).cuda()
+            d_out = torch.empty((2 * p.w, 2 * p.w), dtype=torch.float32, device="cuda")
+            d_wf = torch.empty((p.w, p.w), dtype=torch.float32, device="cuda")
+            ws = torch.empty(fs.plan.batch_workspace_bytes([p]), dtype=torch.uint8, device="cuda")
+            fs.plan.recon_batch([(p, d_raw.data_ptr(), d_out.data_ptr(), d_wf.data_ptr())], ws.data_ptr(), ws.numel())
+            torch.cuda.synchronize()
+            assert np.array_equal(w, d_wf.cpu().numpy())
+
+
+def test_offline_large_five_phase_vs_oracle(fs, oracle):
+    """2048^2, 3 angles x 5 phases (pseudo-inverse separation), |k0| = 0.9 cutoff,
+    modulation 0.6, 200 photons, reconstructed to 4096^2: within 1e-4 relative L2 of the
+    float oracle; the error against the FP64 oracle is recorded."""
+    n = 2048
+    raw, truth, sp = make(fs, n, seed=130, n_phases=5, k0_frac=0.9, modulation=0.6, photons=200.0)
+    plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    got = plan.reconstruct_host(raw)
+    exp32 = oracle.recon_raw(sp, raw, fade=10)
+    e32 = rel_l2(got, exp32)
+    exp64 = oracle.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+    e64 = rel_l2(got, exp64)
+    print("2048^2 3x5: rel-L2 vs float oracle %.3e, vs FP64 oracle %.3e (oracle float vs FP64 %.3e)"
+          % (e32, e64, rel_l2(exp32, exp64)))
+    assert e32 < 1e-4
+    assert e64 < 1e-4
+
+
+def test_estimate_raw_1024_vs_oracle(fs, oracle, torch_cuda):
+    """Full parameter fit at 1024^2 (locatePeak, fitPeak 3 x 10 x 10, getPeak): the fitted
+    shifts equal the oracle's and land on the generator's k0 pixel."""
+    import ctypes as C
+    torch = torch_cuda
+    n = 1024
+    raw, truth, sp = make(fs, n, seed=140)
+    sp.directions = [fs.Dir(2, 3) for _ in range(3)]
+    spec = oracle.prepare_raw(sp, raw)
+    est, peaks, _ = oracle.estimate(sp, spec, 1, 0.6)
+    c = fs.native.to_c_param(sp)
+    d_raw = torch.from_numpy(raw).cuda()
+    out = (C.c_double * 12)()
+    fs.native.check(fs.native.lib().fsim_estimate_raw(C.byref(c), C.c_void_p(d_raw.data_ptr()), fs.native.INPUT_F32,
+                                                      10, 1, C.c_double(0.6), out))
+    got = fs.native.from_c_param(c)
+    for d in range(3):
+        assert abs(got["pX"][d] - est["pX"][d]) < 1e-9 and abs(got["pY"][d] - est["pY"][d]) < 1e-9
+        assert abs(got["phaOff"][d] - est["phaOff"][d]) < 1e-4
+        assert abs(got["pX"][d] - truth["pxpy"][d][0]) < 0.1 and abs(got["pY"][d] - truth["pxpy"][d][1]) < 0.1
