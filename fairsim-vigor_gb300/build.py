@@ -72,6 +72,35 @@ def build(verbose: bool = False, jobs: int | None = None, ptxas_info: bool = Fal
     return LIB
 
 
+def find_jni_include():
+    """Include folders of a JDK's jni.h (JAVA_HOME, then /usr/lib/jvm), or None."""
+    cands = []
+    if os.environ.get("JAVA_HOME"):
+        cands.append(os.path.join(os.environ["JAVA_HOME"], "include"))
+    cands += sorted(glob.glob("/usr/lib/jvm/*/include"))
+    for inc in cands:
+        if os.path.exists(os.path.join(inc, "jni.h")):
+            return [inc] + [os.path.dirname(h) for h in glob.glob(os.path.join(inc, "*", "jni_md.h"))]
+    return None
+
+
+def build_jni(verbose: bool = False):
+    """Builds lib/libfairsim_gb300_jni.so (jni/fsim_jni.cpp) when a JDK is installed; returns
+    its path, or None without a jni.h (the C ABI library is complete without it)."""
+    inc = find_jni_include()
+    if not inc:
+        return None
+    lib = build(verbose)
+    out = os.path.join(LIBDIR, "libfairsim_gb300_jni.so")
+    cmd = (["g++", "-O2", "-std=c++17", "-shared", "-fPIC"] + ["-I" + i for i in inc]
+           + [os.path.join(HERE, "jni", "fsim_jni.cpp"), "-L" + LIBDIR, "-lfairsim_gb300",
+              "-Wl,-rpath,$ORIGIN", "-o", out])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("JNI shim build failed:\n" + r.stderr[-4000:])
+    return out if lib else None
+
+
 if __name__ == "__main__":
     import time
 

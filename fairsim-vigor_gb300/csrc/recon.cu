@@ -21,6 +21,7 @@
 // OTF lookup.
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -149,6 +150,32 @@ int Plan::build(cudaStream_t st) {
       win[2 * (a * nC + c)] = xs;
       win[2 * (a * nC + c) + 1] = ys;
     }
+  // Nyquist response of each pair's pos component: FFT_N((-1)^n ro_pos[n]) with
+  // ro_pos[n] = exp(+2 pi i kx (2n+1)/W)/W, i.e. exp(i phi0)/W * sum_n exp(i theta n),
+  // theta = 4 pi kx/W + pi - 2 pi m/N, summed in closed form in double
+  const int nPair = prm.nr_bands - 1;
+  std::vector<float2> nyq((size_t)nA * nPair * N);
+  for (int a = 0; a < nA; a++)
+    for (int b = 1; b <= nPair; b++) {
+      double kx, ky;
+      comp_shift(&prm, a, 2 * b, &kx, &ky);
+      const double f0 = kx / W - std::floor(kx / W), f1 = 2 * kx / W - std::floor(2 * kx / W);
+      const std::complex<double> e0 = std::polar(1.0 / W, 2 * M_PI * f0);
+      for (int m = 0; m < N; m++) {
+        double th = 2 * M_PI * f1 + M_PI - 2 * M_PI * (double)m / N;
+        th -= 2 * M_PI * std::floor(th / (2 * M_PI) + 0.5);  // (-pi, pi]
+        std::complex<double> S;
+        if (std::fabs(th) < 1e-14) {
+          S = (double)N;
+        } else {
+          double fn = (double)N * th / (2 * M_PI);
+          fn -= std::floor(fn);
+          S = (1.0 - std::polar(1.0, 2 * M_PI * fn)) / (1.0 - std::polar(1.0, th));
+        }
+        const std::complex<double> q = e0 * S;
+        nyq[((size_t)a * nPair + (b - 1)) * N + m] = make_float2((float)q.real(), (float)q.imag());
+      }
+    }
   // device layout: one allocation
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t off_coef = 0, off_ramp = off_coef + al(coef.size() * sizeof(float2));
@@ -157,7 +184,8 @@ int Plan::build(cudaStream_t st) {
   size_t off_damp = off_otf + al(sizeof(OtfTable));
   size_t off_mask = off_damp + al((size_t)N * N * sizeof(float));
   size_t off_wa = off_mask + al((size_t)nA * nC * nwin * nwin * sizeof(float));
-  size_t total = off_wa + al((size_t)W * W * sizeof(float));
+  size_t off_nyq = off_wa + al((size_t)W * W * sizeof(float));
+  size_t total = off_nyq + al(nyq.size() * sizeof(float2));
   if (total > dev_bytes) {
     if (dev) cudaFree(dev);
     dev = nullptr;
@@ -165,6 +193,7 @@ int Plan::build(cudaStream_t st) {
     dev_bytes = total;
   }
   char* b = (char*)dev;
+  d_nyq = (float2*)(b + off_nyq);
   d_coef = (float2*)(b + off_coef);
   d_ramps = (float2*)(b + off_ramp);
   d_win = (int*)(b + off_win);
@@ -177,6 +206,7 @@ int Plan::build(cudaStream_t st) {
   FSIM_CUDA(cudaMemcpyAsync(d_ramps, ramps.data(), ramps.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
   FSIM_CUDA(cudaMemcpyAsync(d_win, win.data(), win.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   FSIM_CUDA(cudaMemcpyAsync(d_otf, &ht, sizeof(OtfTable), cudaMemcpyHostToDevice, st));
+  FSIM_CUDA(cudaMemcpyAsync(d_nyq, nyq.data(), nyq.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
   if (d_damp) {
     std::vector<float> dv = fade_vector(N, N, fade_px);
     FSIM_CUDA(cudaMemcpyAsync(d_damp, dv.data(), dv.size() * sizeof(float), cudaMemcpyHostToDevice, st));
@@ -227,6 +257,7 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws
   j.win = d_win;
   j.masks = d_masks;
   j.wa = d_wa;
+  j.nyq = d_nyq;
   size_t I = (size_t)prm.nr_dirs * nC * nwin * N * sizeof(float2);
   j.I = (float2*)ws;
   j.O = (float2*)(ws + ((I + 255) & ~(size_t)255));

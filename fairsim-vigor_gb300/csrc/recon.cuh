@@ -19,6 +19,7 @@ struct JobDesc {
   const int* win;       // [a][c] {Xs, Ys} window origins (offline) / {xInt, yInt} paste offsets (live)
   const float* masks;   // [a][c] OTF masks (offline) / N*N conj-OTF vector (live)
   const float* wa;      // Wiener x apodization, quad layout [X/4][Y][X%4]
+  const float2* nyq;    // offline: [a][b-1][N] FFT_N((-1)^n ro_pos[n]), the Nyquist term of a pair's pos component
   float2* I;            // workspace: intermediate after the row pass
   float2* O;            // workspace: W*W after the column pass
 };
@@ -40,6 +41,7 @@ struct Plan {
   float* d_damp = nullptr;
   float* d_masks = nullptr;
   float* d_wa = nullptr;
+  float2* d_nyq = nullptr;
   // host-call convenience buffers (fsim_recon_host)
   void* h_ws = nullptr;
   size_t h_ws_bytes = 0;

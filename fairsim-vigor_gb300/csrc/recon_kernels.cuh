@@ -62,7 +62,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
   constexpr int W = P::W, T = P::T, EN = P::EN;
   const int y = blockIdx.x, a = blockIdx.y, t = threadIdx.x;
   __shared__ JobDesc J;
-  __shared__ float2 bz[smem_line_elems(N, 1)], bh[smem_line_elems(N, 1)], sv[N];
+  __shared__ float2 bz[smem_line_elems(N, 1)], bh[smem_line_elems(N, 1)];
+  __shared__ float2 nyqz;  // Z_neg[N/2] of the current pair
   __shared__ float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
   extern __shared__ float rows[];  // nP raw rows of this image row (background clip, damping)
   const float2* twN = g_stw + stw_offset(N, EN);  // stage table, read through L1
@@ -99,8 +100,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
     return z;
   };
   // Components: band 0, then per band b the pair neg = 2b-1, pos = 2b. The separation
-  // coefficients of a pair are exact complex conjugates in float, so z_pos = conj(z_neg)
-  // and FFT(z_pos)[m] = conj(FFT(z_neg)[-m]): one forward FFT serves both.
+  // coefficients of a pair are complex conjugates, so z_pos = conj(z_neg): the pos
+  // component's row transform follows from the neg one's (below).
   for (int b = 0; b < (nC + 1) / 2; b++) {
     const int cm = b == 0 ? 0 : 2 * b - 1;
 #pragma unroll
@@ -125,42 +126,38 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
       __syncthreads();
       continue;
     }
+    // pair (neg, pos): only the neg component is transformed. With z_pos = conj(z_neg),
+    // ro_pos = conj(ro_neg), re_pos = conj(re_neg) (opposite shifts):
+    //   E_pos[m] = conj(E_neg[-m]),
+    //   O_pos[m] = conj(O_neg[-m]) + d * Q[m],  d = -2i conj(Z_neg[N/2]),
+    // where the d term is the pasted Nyquist bin, whose half-sample phase s(N/2) = -i is
+    // not conjugate-symmetric, and Q = FFT_N((-1)^n ro_pos[n]) is a plan table.
+    const int cn = 2 * b - 1, cp = 2 * b;
+    if (t == (N / 2) % T) nyqz = bh[sidx(N / 2)];
+    // odd samples of the upsampled line: iFFT_N(Z * s)
 #pragma unroll
-    for (int i = 0; i < EN; i++) sv[t + i * T] = bh[sidx(t + i * T)];
-    for (int k = 0; k < 2; k++) {
-      const int c = 2 * b - 1 + k;
-      if (k == 1) {  // pos: z = conj(z_neg), Z = mirrored conj(Z_neg)
-        __syncthreads();
+    for (int i = 0; i < EN; i++) {
+      const int m = t + i * T;
+      bh[sidx(m)] = cmul(bh[sidx(m)], half_shift<N>(twW, m));
+    }
+    __syncthreads();
+    line_fft_st<N, T, 1, true>(bh, t, twN);
+    // times the even/odd ramp samples, forward transforms
+    const float2* re = J.ramps + (size_t)(a * nC + cn) * 2 * W;
+    const float2* ro = re + N;
 #pragma unroll
-        for (int i = 0; i < EN; i++) {
-          const int m = t + i * T;
-          bz[sidx(m)] = cconjf(mix(cm, m));
-          bh[sidx(m)] = cconjf(sv[m == 0 ? 0 : N - m]);
-        }
-      }
-      // odd samples of the upsampled line: iFFT_N(Z * s)
-#pragma unroll
-      for (int i = 0; i < EN; i++) {
-        const int m = t + i * T;
-        bh[sidx(m)] = cmul(bh[sidx(m)], half_shift<N>(twW, m));
-      }
-      __syncthreads();
-      line_fft_st<N, T, 1, true>(bh, t, twN);
-      // times the even/odd ramp samples, forward transforms
-      const float2* re = J.ramps + (size_t)(a * nC + c) * 2 * W;
-      const float2* ro = re + N;
-#pragma unroll
-      for (int i = 0; i < EN; i++) {
-        const int m = t + i * T;
-        bz[sidx(m)] = cmul(bz[sidx(m)], __ldg(re + m));
-        bh[sidx(m)] = cmul(bh[sidx(m)], __ldg(ro + m));
-      }
-      __syncthreads();
-      line_fft_st<N, T, 1, false>(bz, t, twN);
-      line_fft_st<N, T, 1, false>(bh, t, twN);
-      // window of the shifted spectrum: E[X mod N] + exp(-2 pi i X/W) O[X mod N]
-      const int Xs = J.win[2 * (a * nC + c)];
-      float2* I = J.I + (size_t)(a * nC + c) * J.nWin * N;
+    for (int i = 0; i < EN; i++) {
+      const int m = t + i * T;
+      bz[sidx(m)] = cmul(bz[sidx(m)], __ldg(re + m));
+      bh[sidx(m)] = cmul(bh[sidx(m)], __ldg(ro + m));
+    }
+    __syncthreads();
+    line_fft_st<N, T, 1, false>(bz, t, twN);
+    line_fft_st<N, T, 1, false>(bh, t, twN);
+    // neg window of the shifted spectrum: E[X mod N] + exp(-2 pi i X/W) O[X mod N]
+    {
+      const int Xs = J.win[2 * (a * nC + cn)];
+      float2* I = J.I + (size_t)(a * nC + cn) * J.nWin * N;
       for (int xl = t; xl < J.nWin; xl += T) {
         int X = Xs + xl;
         if (X >= W) X -= W;
@@ -168,8 +165,24 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
         const float2 e = bz[sidx(m)], o = bh[sidx(m)];
         I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(e, cmul(twW[X], o));
       }
-      __syncthreads();
     }
+    // pos window from the mirrored neg transforms
+    {
+      const float2 d = make_float2(-2.f * nyqz.y, -2.f * nyqz.x);
+      const float2* Q = J.nyq + (size_t)(a * ((nC - 1) / 2) + (b - 1)) * N;
+      const int Xs = J.win[2 * (a * nC + cp)];
+      float2* I = J.I + (size_t)(a * nC + cp) * J.nWin * N;
+      for (int xl = t; xl < J.nWin; xl += T) {
+        int X = Xs + xl;
+        if (X >= W) X -= W;
+        const int m = X < N ? X : X - N;
+        const int mm = m == 0 ? 0 : N - m;
+        const float2 e = cconjf(bz[sidx(mm)]);
+        const float2 o = cadd(cconjf(bh[sidx(mm)]), cmul(d, __ldg(Q + m)));
+        I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(e, cmul(twW[X], o));
+      }
+    }
+    __syncthreads();
   }
 }
 

@@ -9,7 +9,11 @@
 #include "fft_line.cuh"
 #include "runtime.cuh"
 
+#include <cuda_profiler_api.h>
+
 namespace fsim {
+
+bool fft2d_supported(int w, int h);  // fft2d.cu
 
 static thread_local char g_errbuf[1024] = "";
 
@@ -165,6 +169,43 @@ int fsim_sync(void) {
 }
 
 int fsim_version(void) { return 10000; }
+
+int fsim_buffer_alloc(size_t bytes, int host, void** out) {
+  FSIM_REQUIRE(out && bytes > 0, FSIM_EINVAL, "buffer_alloc: bad arguments");
+  *out = nullptr;
+  int rc = fsim::ensure_init();
+  if (rc) return rc;
+  if (host) {
+    FSIM_CUDA(cudaMallocHost(out, bytes));
+  } else {
+    FSIM_CUDA(fsim::dev_alloc(out, bytes));
+  }
+  return FSIM_OK;
+}
+
+int fsim_buffer_free(void* p, int host) {
+  if (!p) return FSIM_OK;
+  FSIM_CUDA(host ? cudaFreeHost(p) : cudaFree(p));
+  return FSIM_OK;
+}
+
+int fsim_profiler(int start) {
+  int rc = fsim::ensure_init();
+  if (rc) return rc;
+  FSIM_CUDA(start ? cudaProfilerStart() : cudaProfilerStop());
+  return FSIM_OK;
+}
+
+int fsim_fft_plan_2d(int w, int h, int64_t* plan) {
+  FSIM_REQUIRE(plan, FSIM_EINVAL, "fft_plan_2d: null output");
+  *plan = 0;
+  FSIM_REQUIRE(fsim::fft2d_supported(w, h), FSIM_EINVAL,
+               "fft_plan_2d: no line FFT for %d x %d", w, h);
+  // nothing to build: the line FFTs use the resident twiddle tables; the handle carries
+  // the shape for the vector that is transformed with it
+  *plan = ((int64_t)w << 32) | (int64_t)(uint32_t)h;
+  return FSIM_OK;
+}
 
 int fsim_debug_fail_alloc(int nth) {
   FSIM_REQUIRE(nth >= 0, FSIM_EINVAL, "debug_fail_alloc: nth must be >= 0");

@@ -20,6 +20,7 @@
 #include <deque>
 #include <string>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -33,6 +34,82 @@
 
 using namespace fsim;
 using clk = std::chrono::steady_clock;
+
+// Host copies of whole stacks and images (megabytes each) split over a few threads: with
+// one thread, memcpy bandwidth of a single core bounds the served throughput.
+class CopyPool {
+ public:
+  explicit CopyPool(int n) {
+    for (int i = 0; i < n; i++) th_.emplace_back([this] { loop(); });
+  }
+  ~CopyPool() {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  void copy(void* dst, const void* src, size_t bytes) {
+    constexpr size_t kMin = (size_t)1 << 20;
+    const size_t parts = std::min(th_.size() + 1, (bytes + kMin - 1) / kMin);
+    if (parts <= 1) {
+      std::memcpy(dst, src, bytes);
+      return;
+    }
+    const size_t per = ((bytes / parts) + 63) & ~(size_t)63;
+    Latch latch;
+    latch.left = (int)parts - 1;
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      for (size_t k = 1; k < parts; k++) {
+        const size_t off = k * per;
+        if (off >= bytes) {
+          latch.left--;
+          continue;
+        }
+        q_.push_back(Task{(char*)dst + off, (const char*)src + off, std::min(per, bytes - off), &latch});
+      }
+    }
+    cv_.notify_all();
+    std::memcpy(dst, src, std::min(per, bytes));
+    std::unique_lock<std::mutex> lk(latch.mu);
+    latch.cv.wait(lk, [&] { return latch.left == 0; });
+  }
+
+ private:
+  struct Latch {
+    std::mutex mu;
+    std::condition_variable cv;
+    int left = 0;
+  };
+  struct Task {
+    char* dst;
+    const char* src;
+    size_t n;
+    Latch* latch;
+  };
+  void loop() {
+    for (;;) {
+      Task t;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return stop_ || !q_.empty(); });
+        if (q_.empty()) return;
+        t = q_.front();
+        q_.pop_front();
+      }
+      std::memcpy(t.dst, t.src, t.n);
+      std::lock_guard<std::mutex> g(t.latch->mu);
+      if (--t.latch->left == 0) t.latch->cv.notify_all();
+    }
+  }
+  std::vector<std::thread> th_;
+  std::deque<Task> q_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  bool stop_ = false;
+};
 
 static double now_ms() {
   return std::chrono::duration<double, std::milli>(clk::now().time_since_epoch()).count();
@@ -49,7 +126,7 @@ struct fsim_server {
     void* d_refit_raw = nullptr;
     size_t raw_bytes = 0;
   };
-  enum { FREE = 0, FILLING, PENDING, RUNNING, DONE };
+  enum { FREE = 0, FILLING, PENDING, RUNNING, DONE, COLLECTING };
   struct Slot {
     void* h_raw = nullptr;
     void* d_raw = nullptr;
@@ -83,6 +160,7 @@ struct fsim_server {
   std::mutex mu;
   std::condition_variable cv_work, cv_done, cv_refit;
   std::thread worker, refitter;
+  std::unique_ptr<CopyPool> copier;
   std::deque<int> refit_queue;
   bool stop = false;
   // stats
@@ -352,6 +430,8 @@ static int serve_setup(fsim_server* s, const fsim_serve_config* cfg, const fsim_
   }
   FSIM_CUDA(cudaStreamCreateWithFlags(&s->refit_stream, cudaStreamNonBlocking));
   FSIM_CUDA(cudaDeviceSynchronize());
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  s->copier.reset(new CopyPool((int)std::min(7u, std::max(1u, hw / 4))));
   return FSIM_OK;
 }
 
@@ -382,7 +462,7 @@ int fsim_serve_submit(fsim_server* s, int channel, const void* raw_host, size_t 
     s->by_ticket[sl.ticket] = i;
     *ticket = sl.ticket;
   }
-  std::memcpy(s->slots[i].h_raw, raw_host, s->ch[channel].raw_bytes);
+  s->copier->copy(s->slots[i].h_raw, raw_host, s->ch[channel].raw_bytes);
   {
     std::lock_guard<std::mutex> g(s->mu);
     s->slots[i].state = fsim_server::PENDING;
@@ -409,11 +489,17 @@ int fsim_serve_wait(fsim_server* s, uint64_t ticket, float* out_host, int timeou
   }
   FSIM_REQUIRE(mine(), FSIM_ENOTFOUND, "serve_wait: ticket %llu was cancelled while waiting",
                (unsigned long long)ticket);
+  // copy out without the server lock: the ticket is retired first, so no other call
+  // (wait, cancel) can reach this slot until it is back on the free list
   const size_t W = 2 * (size_t)s->ch[sl.channel].prm.w;
-  std::memcpy(out_host, sl.h_out, W * W * sizeof(float));
   if (latency_ms) *latency_ms = sl.t_done - sl.t_submit;
-  sl.state = fsim_server::FREE;
+  sl.state = fsim_server::COLLECTING;
   s->by_ticket.erase(ticket);
+  lk.unlock();
+  s->copier->copy(out_host, sl.h_out, W * W * sizeof(float));
+  lk.lock();
+  sl.state = fsim_server::FREE;
+  sl.ticket = 0;
   s->free_list.push_back(i);
   return FSIM_OK;
 }

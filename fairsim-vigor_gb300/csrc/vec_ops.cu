@@ -371,6 +371,40 @@ int fsim_vec_info(const fsim_vec* v, int* w, int* h, int* is_complex, void** dev
   return FSIM_OK;
 }
 
+int fsim_vec_reshape(fsim_vec* v, int w, int h) {
+  NEED_VEC(v);
+  FSIM_REQUIRE(w > 0 && h > 0 && (size_t)w * h == v->n, FSIM_EINVAL,
+               "fsim_vec_reshape: %d x %d does not hold %zu elements", w, h, v->n);
+  v->w = w;
+  v->h = h;
+  return FSIM_OK;
+}
+
+int fsim_vec_set_elem(fsim_vec* v, size_t index, float re, float im) {
+  NEED_INIT();
+  NEED_VEC(v);
+  FSIM_REQUIRE(index < v->n, FSIM_EINVAL, "fsim_vec_set_elem: index %zu of %zu", index, v->n);
+  const float val[2] = {re, im};
+  // ordered after earlier work on the vector; the value is copied before the call returns
+  FSIM_CUDA(cudaMemcpyAsync(v->d + (v->cplx ? 2 * index : index), val, (v->cplx ? 2 : 1) * sizeof(float),
+                            cudaMemcpyHostToDevice, ctx().stream));
+  FSIM_CUDA(cudaStreamSynchronize(ctx().stream));
+  return FSIM_OK;
+}
+
+int fsim_vec_get_elem(const fsim_vec* v, size_t index, float* re, float* im) {
+  NEED_INIT();
+  NEED_VEC(v);
+  FSIM_REQUIRE(index < v->n && re, FSIM_EINVAL, "fsim_vec_get_elem: index %zu of %zu", index, v->n);
+  float val[2] = {0.f, 0.f};
+  FSIM_CUDA(cudaMemcpyAsync(val, v->d + (v->cplx ? 2 * index : index), (v->cplx ? 2 : 1) * sizeof(float),
+                            cudaMemcpyDeviceToHost, ctx().stream));
+  FSIM_CUDA(cudaStreamSynchronize(ctx().stream));
+  *re = val[0];
+  if (im) *im = val[1];
+  return FSIM_OK;
+}
+
 int fsim_vec_upload(fsim_vec* v, const float* host) {
   NEED_INIT();
   NEED_VEC(v);

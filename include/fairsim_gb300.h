@@ -51,6 +51,16 @@ int fsim_sync(void);                     /* AccelVectorFactory.nativeSync (cudaD
 int fsim_version(void);
 int fsim_set_stream(void* stream);       /* stream used by the vector API (NULL = own stream) */
 
+/* AccelVectorFactory.nativeAllocMemory / nativeAllocMemoryHost (AccelVectorFactory.java:140-141):
+ * raw device (host == 0) or page-locked host (host != 0) buffers, and their release. */
+int fsim_buffer_alloc(size_t bytes, int host, void** out);
+int fsim_buffer_free(void* p, int host);
+/* AccelVectorFactory.startProfiler / stopProfiler (AccelVectorFactory.java:143-146). */
+int fsim_profiler(int start);
+/* FFTProvider.nativeCreatePlan2d (FFTProvider.java:105): checks that w x h has line FFTs and
+ * returns a handle carrying the shape (no plan object is built; nothing to free). */
+int fsim_fft_plan_2d(int w, int h, int64_t* plan);
+
 /* ---- SimParam (+ OtfProvider.fromEstimate) as a flat record ------------------------
  * org/fairsim/sim_algorithm/SimParam.java:31-615, OtfProvider.java:96-127.
  * px/py: Dir.pX/pY (band-1 shift; setPxPy divides the highest-band shift by nBands-1),
@@ -78,6 +88,14 @@ int fsim_vec_info(const fsim_vec* v, int* w, int* h, int* is_complex, void** dev
 /* copyBuffer (AccelVectorCplx.java:311): host <-> device, n floats of the vector */
 int fsim_vec_upload(fsim_vec* v, const float* host);
 int fsim_vec_download(const fsim_vec* v, float* host);
+/* The accel vectors are allocated by element count (AccelVectorCplx.java:305) and learn
+ * their 2D shape from the call that needs it (FFT plan, nativeFourierShift's N,
+ * nativePasteFreq's wo/ho): reshape sets w x h with w*h equal to the element count. */
+int fsim_vec_reshape(fsim_vec* v, int w, int h);
+/* nativeSet / nativeGet (AccelVectorCplx.java:486-487, AccelVectorReal.java:332-333):
+ * element index = x + y*width; im is ignored (set) or not written (get) for real vectors. */
+int fsim_vec_set_elem(fsim_vec* v, size_t index, float re, float im);
+int fsim_vec_get_elem(const fsim_vec* v, size_t index, float* re, float* im);
 /* nativeCOPYSHORT (AccelVectorCplx.java:483, AccelVectorReal.java:330): unsigned 16-bit pixels */
 int fsim_vec_upload_u16(fsim_vec* v, const uint16_t* host);
 /* elementwise ops (AccelVectorCplx.java:314-331, AccelVectorReal.java:235-247) */

@@ -32,3 +32,28 @@ def test_calls_without_device_return_status(fs):
     rc = lib.fsim_init(0)
     assert rc == fs.native.FSIM_ENODEV
     assert b"device" in lib.fsim_last_error()
+
+
+def test_jni_shim_defines_every_reference_native():
+    """The JNI shim must export the symbol of every `native` method the reference's accel
+    classes declare (list in tests/golden/jni_natives.txt, made by make_jni_natives.py), so
+    that those classes load the GB300 library unchanged. Checked on the source: no jni.h
+    is installed here to compile it."""
+    import re
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    want = open(os.path.join(root, "tests", "golden", "jni_natives.txt")).read().split()
+    src = open(os.path.join(root, "fairsim-vigor_gb300", "jni", "fsim_jni.cpp")).read()
+    have = {"Java_org_fairsim_accel_%s_%s" % m for m in re.findall(r"JFN\(\w+,\s*(\w+),\s*(\w+)\)", src)}
+    assert len(want) == 38
+    assert sorted(set(want) - have) == []
+
+
+def test_jni_shim_calls_only_declared_functions(fs):
+    import re
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = open(os.path.join(root, "fairsim-vigor_gb300", "jni", "fsim_jni.cpp")).read()
+    declared = set(fs.native.header_functions())
+    used = set(re.findall(r"\b(fsim_\w+)\(", src))
+    assert used and used <= declared, sorted(used - declared)

@@ -213,3 +213,36 @@ def test_run_reconstruction_op_by_op_vs_oracle(V, oracle, fs, n):
     out = fs.algorithm.SimAlgorithm.runReconstruction(sp, inFFT, False, 0).vectorData()
     assert rel_l2(out, exp32) < 1e-4   # vs the reference's float semantics
     assert rel_l2(out, exp64) < 1e-5   # vs the FP64 oracle
+
+
+def test_accel_natives_set_get_reshape_plan_buffers(fs, V):
+    """The remaining accel natives: nativeSet/nativeGet (element access), vectors allocated
+    by element count and shaped by the call that needs a shape, nativeCreatePlan2d, and
+    the factory's raw device / pinned host buffers."""
+    import ctypes as C
+
+    lib = fs.native.lib()
+    rng = np.random.default_rng(9)
+    z = (rng.standard_normal((64, 32)) + 1j * rng.standard_normal((64, 32))).astype(np.complex64)
+    v = V.Vec2dCplx(64 * 32, 1)  # allocated by element count, like AccelVectorCplx.alloc
+    fs.native.check(lib.fsim_vec_reshape(v.handle, 32, 64))
+    v.setData(z)
+    re, im = C.c_float(), C.c_float()
+    fs.native.check(lib.fsim_vec_get_elem(v.handle, 5 + 7 * 32, C.byref(re), C.byref(im)))
+    assert (re.value, im.value) == (float(z[7, 5].real), float(z[7, 5].imag))
+    fs.native.check(lib.fsim_vec_set_elem(v.handle, 3 + 2 * 32, 1.5, -2.25))
+    z[2, 3] = 1.5 - 2.25j
+    plan = C.c_int64()
+    fs.native.check(lib.fsim_fft_plan_2d(32, 64, C.byref(plan)))
+    assert (plan.value >> 32, plan.value & 0xffffffff) == (32, 64)
+    v.fft2d(False)
+    assert rel_l2(v.vectorData(), np.fft.fft2(z.astype(np.complex128))) < 3e-6
+    assert lib.fsim_vec_reshape(v.handle, 33, 64) == fs.native.FSIM_EINVAL
+    assert lib.fsim_vec_set_elem(v.handle, 64 * 32, 0.0, 0.0) == fs.native.FSIM_EINVAL
+    for host in (0, 1):
+        p = C.c_void_p()
+        fs.native.check(lib.fsim_buffer_alloc(8 << 20, host, C.byref(p)))
+        assert p.value
+        fs.native.check(lib.fsim_buffer_free(p, host))
+    fs.native.check(lib.fsim_profiler(1))
+    fs.native.check(lib.fsim_profiler(0))

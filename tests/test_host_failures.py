@@ -101,3 +101,11 @@ def test_status_codes_map_to_exception_types(fs):
         N.check(N.FSIM_EBUSY)
     with pytest.raises(N.FsimError):
         N.check(N.FSIM_ECUDA)
+
+
+def test_fft_plan_checks_sizes_without_a_device(fs):
+    lib = fs.native.lib()
+    h = C.c_int64()
+    assert lib.fsim_fft_plan_2d(100, 64, C.byref(h)) == fs.native.FSIM_EINVAL
+    assert lib.fsim_fft_plan_2d(512, 384, C.byref(h)) == fs.native.FSIM_OK
+    assert (h.value >> 32, h.value & 0xffffffff) == (512, 384)
