@@ -179,18 +179,31 @@ TRAFFIC_PER_DATASET = {}
 
 
 def pass_bytes(n=N, n_dirs=NA, n_phases=NP, n_bands=NB, na=1.4, lam=525.0, pxl=0.08):
-    """Algorithmic bytes per dataset of the offline passes A, B, C (each input read once,
-    each output written once): A reads the raw frames and writes the row-transformed OTF
-    support windows I; B reads I, the masks and Wiener x apodization and writes the
-    column-transformed W x W plane O; C reads O and writes the W x W image."""
-    nc = 2 * n_bands - 1
+    """Algorithmic bytes per dataset of the offline passes (each input read once, each output
+    written once):
+      A      raw frames in; row-transformed OTF-support windows I of band 0 and of each pair's
+             neg component out, plus one Nyquist term per row (D)
+      G+B1   D in, one column per angle and pair out (G); I in, the column-transformed windows
+             Tw (band 0, neg of every pair) and one Nyquist term per neg column (Dy) out
+      B2     Tw (read for the neg and, mirrored, for the pos component), OTF masks (band 0
+             once, neg and pos of every pair), Wiener x apodization, G, Dy in; the W x W
+             column-transformed plane O out
+      C      O in, the W x W image out"""
+    npair = n_bands - 1
     W = 2 * n
     R = (2 * na / (lam / 1000.0)) / (1.0 / (n * pxl))
     nwin = min(W, ((2 * int(np.ceil(R)) + 6) // 4) * 4 + 4)
-    a = n_dirs * n_phases * n * n * 4 + n_dirs * nc * nwin * n * 8
-    b = n_dirs * nc * nwin * n * 8 + n_dirs * nc * nwin * nwin * 4 + W * W * 4 + W * W * 8
+    I = n_dirs * (1 + npair) * nwin * n * 8
+    D = n_dirs * npair * n * 8
+    G = n_dirs * npair * nwin * 8
+    Tw = (1 + n_dirs * npair) * nwin * nwin * 8
+    Dy = n_dirs * npair * nwin * 8
+    masks = (1 + 2 * n_dirs * npair) * nwin * nwin * 4
+    a = n_dirs * n_phases * n * n * 4 + I + D
+    b1 = D + G + I + Tw + Dy
+    b2 = Tw + n_dirs * npair * nwin * nwin * 8 + masks + W * W * 4 + G + Dy + W * W * 8
     c = W * W * 8 + W * W * 4
-    return [a, b, c]
+    return [a, b1, b2, c]
 
 
 def main():
@@ -319,7 +332,7 @@ def main():
     N_.check(N_.lib().fsim_profile_enable(0))
     pm = np.median(np.array(pass_ms), axis=0)
     algo = pass_bytes()
-    names = ["k_pass_a<512>", "k_pass_b<512>", "k_pass_c<512>"]
+    names = ["k_pass_a<512>", "k_pass_g+k_pass_b1<512>", "k_pass_b2<512>", "k_pass_c<512>"]
     dom = int(np.argmax(pm))
     peak, peak_kind = peaks()
     achieved = algo[dom] * B / (pm[dom] / 1000.0) / 1e9
@@ -342,6 +355,7 @@ def main():
         extras["mixed_batch"] = mixed_leg(fs, torch, stream, timed)
         extras["large_3x5_2048"] = large_leg(fs, torch, stream, timed)
         extras["estimate_1024"] = estimate_leg(fs, torch)
+        extras["fft2d_vs_cufft"] = [fft_leg(fs, torch, stream, timed, n, b) for n, b in ((512, 64), (1024, 16))]
         rate, cores, n, dt = cpu_recon_rate(fs, datasets)
         extras["cpu_baseline"] = {"value": rate, "unit": "recon/s", "cores": cores, "kind": "port",
                                   "sample": "%d reconstructions of one 512x512 3x3 dataset in %.1f s (oracle: C++ "
@@ -486,6 +500,36 @@ def large_leg(fs, torch, stream, timed, steps=5):
             "host_call_ms": host_ms, "stream_target_stacks_per_s": 20.0,
             "rel_l2_vs_oracle_f32": rl(got, exp32), "rel_l2_vs_oracle_f64": rl(got, exp64),
             "oracle_f32_vs_f64": rl(exp32, exp64), "device_vs_host_call_identical": bool(np.array_equal(got, got_host))}
+
+
+def fft_leg(fs, torch, stream, timed, n, batch, steps=10):
+    """The library's 2D FFT (fsim_fft2d_batch: row pass + column pass, Stockham line FFTs)
+    against cuFFT (torch.fft.fft2), as a comparator only, on `batch` n x n complex64 planes."""
+    import ctypes as C
+
+    lib = fs.native.lib()
+    g = torch.Generator(device="cuda").manual_seed(n)
+    x = torch.randn((batch, n, n), dtype=torch.complex64, device="cuda", generator=g)
+    y = x.clone()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def ours():
+        fs.native.check(lib.fsim_fft2d_batch(C.c_void_p(y.data_ptr()), n, n, batch, 0, sp))
+
+    with torch.cuda.stream(stream):
+        ours()
+        ref = torch.fft.fft2(x)
+        torch.cuda.synchronize()
+        err = float((torch.linalg.vector_norm(y - ref) / torch.linalg.vector_norm(ref)).item())
+        for _ in range(3):
+            ours()
+            torch.fft.fft2(x)
+    ms_ours = timed(ours, steps) / steps
+    with torch.cuda.stream(stream):
+        ms_cufft = timed(lambda: torch.fft.fft2(x), steps) / steps
+    byts = 16.0 * batch * n * n  # one read and one write of every complex64 element
+    return {"n": n, "batch": batch, "ms": ms_ours, "cufft_ms": ms_cufft, "rel_l2_vs_cufft": err,
+            "GB_per_s": byts / (ms_ours / 1000) / 1e9, "cufft_GB_per_s": byts / (ms_cufft / 1000) / 1e9}
 
 
 def estimate_leg(fs, torch, reps=3):

@@ -1,7 +1,7 @@
 """Autotuner for the fused reconstruction's launch shapes.
 
 For every image size it times each variant of the row pass (elements per thread, i.e. the
-radix plan and threads per line) and of the column pass (elements per thread x interleaved
+radix plan and threads per line) and of the column passes (elements per thread x interleaved
 columns per block) with the library's per-pass CUDA events on a batch of datasets larger
 than L2, picks the fastest of each, and writes ``tuning.json`` next to this file.
 ``native.init()`` applies the table (fsim_tune_set). Variants change launch shapes only;
@@ -79,7 +79,8 @@ def tune(sizes=(256, 384, 512, 768, 1024), reps=5, target_bytes=1 << 30, verbose
         N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, 0, best_a))
         for vb in range(nvb):
             N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, 1, vb))
-            b_ms.append(float(measure()[1]))
+            m = measure()
+            b_ms.append(float(sum(m[1:-1])))  # the column passes (G+B1, B2)
         best_b = int(np.argmin(b_ms))
         N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, 1, best_b))
         result[str(n)] = {"a": best_a, "b": best_b, "batch": B, "a_ms": a_ms, "b_ms": b_ms,

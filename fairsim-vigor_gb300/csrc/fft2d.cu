@@ -153,3 +153,12 @@ extern "C" int fsim_vec_fft2d(fsim_vec* v, int inverse) {
   FSIM_REQUIRE(v && v->d && v->cplx, FSIM_EINVAL, "fft2d: complex vector required");
   return fsim::fft2d_device(reinterpret_cast<float2*>(v->d), v->w, v->h, inverse != 0, fsim::ctx().stream, 1);
 }
+
+extern "C" int fsim_fft2d_batch(void* data, int w, int h, int batch, int inverse, void* stream) {
+  FSIM_REQUIRE(data && batch > 0, FSIM_EINVAL, "fft2d_batch: bad arguments");
+  FSIM_REQUIRE(fsim::fft2d_supported(w, h), FSIM_EINVAL, "fft2d_batch: unsupported size %d x %d", w, h);
+  int rc = fsim::ensure_init();
+  if (rc) return rc;
+  cudaStream_t st = stream ? (cudaStream_t)stream : fsim::ctx().stream;
+  return fsim::fft2d_device(static_cast<float2*>(data), w, h, inverse != 0, st, batch);
+}

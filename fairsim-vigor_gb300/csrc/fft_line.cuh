@@ -222,6 +222,26 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2*
   // TS > 0: plain table exp(-2 pi i m/(L*TS)) read at stride TS; TS == 0: stage table
   // [r-1][k] of this stage (tw points at the stage's first entry)
   constexpr int E = L / T, NB = E / R, LR = L / R;
+  // The twiddle loads depend only on the thread's index: issue them first, so that their
+  // latency overlaps the shared-memory reads and the barrier.
+  constexpr int NT = NS > 1 ? (TS > 0 ? R - 1 : (R == 16 ? 3 : (R >= 8 || R == 3 ? 2 : 1))) : 1;
+  float2 tl[NB][NT];
+  if constexpr (NS > 1) {
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+      const int k = (t + b * T) % NS;
+      if constexpr (TS > 0) {
+#pragma unroll
+        for (int r = 1; r < R; r++) tl[b][r - 1] = tw[r * k * (L / (NS * R)) * TS];
+      } else {
+        // stage table [r-1][k]: W^k, W^2k (radix 3), W^4k (radix 8/16), W^8k (radix 16)
+        tl[b][0] = tw[k];
+        if constexpr (R == 3) tl[b][1] = tw[NS + k];
+        if constexpr (R >= 8) tl[b][1] = tw[3 * NS + k];
+        if constexpr (R == 16) tl[b][2] = tw[7 * NS + k];
+      }
+    }
+  }
   float2 v[NB][R];
 #pragma unroll
   for (int b = 0; b < NB; b++) {
@@ -238,25 +258,24 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2*
       float2 w[R];
       if constexpr (TS > 0) {
 #pragma unroll
-        for (int r = 1; r < R; r++) w[r] = tw[r * k * (L / (NS * R)) * TS];
+        for (int r = 1; r < R; r++) w[r] = tl[b][r - 1];
       } else {
-        // stage table [r-1][k]: load W^k (and W^4k for radix 8/16), the rest by products
-        // (at most three roundings beyond the table's)
-        w[1] = tw[k];
-        if constexpr (R == 3) w[2] = tw[NS + k];
+        // the remaining powers by products (at most three roundings beyond the table's)
+        w[1] = tl[b][0];
+        if constexpr (R == 3) w[2] = tl[b][1];
         if constexpr (R == 4) {
           w[2] = cmul(w[1], w[1]);
           w[3] = cmul(w[2], w[1]);
         }
         if constexpr (R >= 8) {
-          w[4] = tw[3 * NS + k];
+          w[4] = tl[b][1];
           w[2] = cmul(w[1], w[1]);
           w[3] = cmul(w[2], w[1]);
 #pragma unroll
           for (int r = 5; r < 8; r++) w[r] = cmul(w[4], w[r - 4]);
         }
         if constexpr (R == 16) {
-          w[8] = tw[7 * NS + k];
+          w[8] = tl[b][2];
 #pragma unroll
           for (int r = 9; r < 16; r++) w[r] = cmul(w[8], w[r - 8]);
         }

@@ -380,6 +380,10 @@ void Plan::fill_job_live(JobDesc& j, const void* raw, float* out, float* wf, cha
   j.masks = d_masks;
   j.wa = d_wa;
   j.nyq = nullptr;
+  j.D = nullptr;
+  j.G = nullptr;
+  j.Tw = nullptr;
+  j.Dy = nullptr;
   size_t I = (size_t)prm.nr_dirs * nC * N * N * sizeof(float2);
   j.I = (float2*)ws;
   j.O = (float2*)(ws + ((I + 255) & ~(size_t)255));

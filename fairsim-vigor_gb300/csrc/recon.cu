@@ -150,30 +150,42 @@ int Plan::build(cudaStream_t st) {
       win[2 * (a * nC + c)] = xs;
       win[2 * (a * nC + c) + 1] = ys;
     }
-  // Nyquist response of each pair's pos component: FFT_N((-1)^n ro_pos[n]) with
-  // ro_pos[n] = exp(+2 pi i kx (2n+1)/W)/W, i.e. exp(i phi0)/W * sum_n exp(i theta n),
-  // theta = 4 pi kx/W + pi - 2 pi m/N, summed in closed form in double
+  // The neg component of each pair uses the mirror image of its pos window (columns and
+  // rows), so that pos values can be formed from the neg transforms at (-X, -Y). The pos
+  // window has slack on both sides of the OTF support, so the mirror covers the neg support.
   const int nPair = prm.nr_bands - 1;
-  std::vector<float2> nyq((size_t)nA * nPair * N);
+  for (int a = 0; a < nA; a++)
+    for (int b = 1; b <= nPair; b++) {
+      const int cp = 2 * b, cn = 2 * b - 1;
+      win[2 * (a * nC + cn)] = ((W - win[2 * (a * nC + cp)] - nwin + 1) % W + W) % W;
+      win[2 * (a * nC + cn) + 1] = ((W - win[2 * (a * nC + cp) + 1] - nwin + 1) % W + W) % W;
+    }
+  // Nyquist response of each pair's pos component along x and along y:
+  // FFT_N((-1)^n ro[n]) with ro[n] = exp(+2 pi i k (2n+1)/W)/W (k = kx, resp. -ky), i.e.
+  // exp(i phi0)/W * sum_n exp(i theta n), theta = 4 pi k/W + pi - 2 pi m/N, in closed form
+  std::vector<float2> nyq((size_t)nA * nPair * 2 * N);
   for (int a = 0; a < nA; a++)
     for (int b = 1; b <= nPair; b++) {
       double kx, ky;
       comp_shift(&prm, a, 2 * b, &kx, &ky);
-      const double f0 = kx / W - std::floor(kx / W), f1 = 2 * kx / W - std::floor(2 * kx / W);
-      const std::complex<double> e0 = std::polar(1.0 / W, 2 * M_PI * f0);
-      for (int m = 0; m < N; m++) {
-        double th = 2 * M_PI * f1 + M_PI - 2 * M_PI * (double)m / N;
-        th -= 2 * M_PI * std::floor(th / (2 * M_PI) + 0.5);  // (-pi, pi]
-        std::complex<double> S;
-        if (std::fabs(th) < 1e-14) {
-          S = (double)N;
-        } else {
-          double fn = (double)N * th / (2 * M_PI);
-          fn -= std::floor(fn);
-          S = (1.0 - std::polar(1.0, 2 * M_PI * fn)) / (1.0 - std::polar(1.0, th));
+      for (int dim = 0; dim < 2; dim++) {
+        const double k = dim == 0 ? kx : -ky;
+        const double f0 = k / W - std::floor(k / W), f1 = 2 * k / W - std::floor(2 * k / W);
+        const std::complex<double> e0 = std::polar(1.0 / W, 2 * M_PI * f0);
+        for (int m = 0; m < N; m++) {
+          double th = 2 * M_PI * f1 + M_PI - 2 * M_PI * (double)m / N;
+          th -= 2 * M_PI * std::floor(th / (2 * M_PI) + 0.5);  // (-pi, pi]
+          std::complex<double> S;
+          if (std::fabs(th) < 1e-14) {
+            S = (double)N;
+          } else {
+            double fn = (double)N * th / (2 * M_PI);
+            fn -= std::floor(fn);
+            S = (1.0 - std::polar(1.0, 2 * M_PI * fn)) / (1.0 - std::polar(1.0, th));
+          }
+          const std::complex<double> q = e0 * S;
+          nyq[(((size_t)a * nPair + (b - 1)) * 2 + dim) * N + m] = make_float2((float)q.real(), (float)q.imag());
         }
-        const std::complex<double> q = e0 * S;
-        nyq[((size_t)a * nPair + (b - 1)) * N + m] = make_float2((float)q.real(), (float)q.imag());
       }
     }
   // device layout: one allocation
@@ -233,11 +245,22 @@ int Plan::build(cudaStream_t st) {
   return FSIM_OK;
 }
 
+// workspace of one dataset: I | D | G | Tw | Dy | O (each 256-byte aligned)
+static void ws_parts(const fsim_sim_param& p, int nwin, size_t part[6]) {
+  const int N = p.w, W = 2 * N, nPair = p.nr_bands - 1;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  part[0] = al((size_t)p.nr_dirs * (1 + nPair) * nwin * N * sizeof(float2));
+  part[1] = al((size_t)p.nr_dirs * nPair * N * sizeof(float2));
+  part[2] = al((size_t)p.nr_dirs * nPair * nwin * sizeof(float2));
+  part[3] = al((size_t)(1 + p.nr_dirs * nPair) * nwin * nwin * sizeof(float2));
+  part[4] = al((size_t)p.nr_dirs * nPair * nwin * sizeof(float2));
+  part[5] = al((size_t)W * W * sizeof(float2));
+}
+
 size_t Plan::workspace_bytes() const {
-  const int N = prm.w, W = 2 * N, nC = 2 * prm.nr_bands - 1;
-  size_t I = (size_t)prm.nr_dirs * nC * nwin * N * sizeof(float2);
-  size_t O = (size_t)W * W * sizeof(float2);
-  return ((I + 255) & ~(size_t)255) + ((O + 255) & ~(size_t)255);
+  size_t part[6];
+  ws_parts(prm, nwin, part);
+  return part[0] + part[1] + part[2] + part[3] + part[4] + part[5];
 }
 
 void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws) const {
@@ -258,9 +281,15 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws
   j.masks = d_masks;
   j.wa = d_wa;
   j.nyq = d_nyq;
-  size_t I = (size_t)prm.nr_dirs * nC * nwin * N * sizeof(float2);
-  j.I = (float2*)ws;
-  j.O = (float2*)(ws + ((I + 255) & ~(size_t)255));
+  size_t part[6];
+  ws_parts(prm, nwin, part);
+  char* w = ws;
+  j.I = (float2*)w;
+  j.D = (float2*)(w += part[0]);
+  j.G = (float2*)(w += part[1]);
+  j.Tw = (float2*)(w += part[2]);
+  j.Dy = (float2*)(w += part[3]);
+  j.O = (float2*)(w += part[4]);
 }
 
 // ---- autotuned variants ------------------------------------------------------------------------

@@ -19,8 +19,13 @@ struct JobDesc {
   const int* win;       // [a][c] {Xs, Ys} window origins (offline) / {xInt, yInt} paste offsets (live)
   const float* masks;   // [a][c] OTF masks (offline) / N*N conj-OTF vector (live)
   const float* wa;      // Wiener x apodization, quad layout [X/4][Y][X%4]
-  const float2* nyq;    // offline: [a][b-1][N] FFT_N((-1)^n ro_pos[n]), the Nyquist term of a pair's pos component
-  float2* I;            // workspace: intermediate after the row pass
+  const float2* nyq;    // offline: [a][b-1][x, y][N] FFT_N((-1)^n ro_pos[n]) of the pos component's x and y
+                        // odd-sample ramps (the Nyquist response, see pass A)
+  float2* I;            // workspace: row-transformed windows [a][band 0, neg of each pair][nWin/4][N][4]
+  float2* D;            // workspace: [a][b-1][N] Nyquist term d of every row's neg component (pass A)
+  float2* G;            // workspace: [a][b-1][nWin] column transform of D with the pos y shift (pass G)
+  float2* Tw;           // workspace: column-transformed windows [band 0, neg of (a, b)][nWin/4][nWin][4] (pass B1)
+  float2* Dy;           // workspace: [a][b-1][nWin] Nyquist term d' of every neg window column (pass B1)
   float2* O;            // workspace: W*W after the column pass
 };
 

@@ -63,7 +63,6 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
   const int y = blockIdx.x, a = blockIdx.y, t = threadIdx.x;
   __shared__ JobDesc J;
   __shared__ float2 bz[smem_line_elems(N, 1)], bh[smem_line_elems(N, 1)];
-  __shared__ float2 nyqz;  // Z_neg[N/2] of the current pair
   __shared__ float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
   extern __shared__ float rows[];  // nP raw rows of this image row (background clip, damping)
   const float2* twN = g_stw + stw_offset(N, EN);  // stage table, read through L1
@@ -71,7 +70,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
   load_job(&J, jobs + blockIdx.z, t, T);
   __syncthreads();
   if (a >= J.nA) return;  // uniform per block
-  const int nP = J.nP, nC = J.nC;
+  const int nP = J.nP, nC = J.nC, nPair = (nC - 1) / 2, nS = 1 + nPair;  // I slots per angle
   for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
   const size_t frame = (size_t)N * N, row = (size_t)y * N;
   for (int p = 0; p < nP; p++) {
@@ -116,7 +115,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
     if (b == 0) {
       // band 0: pasteFreq only; keep the OTF-support window in quad layout
       const int Xs = J.win[2 * (a * nC)];
-      float2* I = J.I + (size_t)(a * nC) * J.nWin * N;
+      float2* I = J.I + (size_t)(a * nS) * J.nWin * N;
       for (int xl = t; xl < J.nWin; xl += T) {
         int X = Xs + xl;
         if (X >= W) X -= W;
@@ -126,14 +125,19 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
       __syncthreads();
       continue;
     }
-    // pair (neg, pos): only the neg component is transformed. With z_pos = conj(z_neg),
-    // ro_pos = conj(ro_neg), re_pos = conj(re_neg) (opposite shifts):
+    // pair (neg, pos): only the neg component is transformed and stored. With
+    // z_pos = conj(z_neg) and opposite shifts (ro_pos = conj(ro_neg), re_pos = conj(re_neg)):
     //   E_pos[m] = conj(E_neg[-m]),
     //   O_pos[m] = conj(O_neg[-m]) + d * Q[m],  d = -2i conj(Z_neg[N/2]),
     // where the d term is the pasted Nyquist bin, whose half-sample phase s(N/2) = -i is
-    // not conjugate-symmetric, and Q = FFT_N((-1)^n ro_pos[n]) is a plan table.
-    const int cn = 2 * b - 1, cp = 2 * b;
-    if (t == (N / 2) % T) nyqz = bh[sidx(N / 2)];
+    // not conjugate-symmetric, and Q = FFT_N((-1)^n ro_pos[n]) is a plan table. So the pos
+    // row spectrum is conj(F_neg[-X]) + exp(-2 pi i X/W) Q[X mod N] d: the column pass
+    // forms it from the neg windows (mirror images of the pos windows) and d, kept here.
+    const int cn = 2 * b - 1;
+    if (t == (N / 2) % T) {
+      const float2 zn = bh[sidx(N / 2)];
+      J.D[(size_t)(a * nPair + (b - 1)) * N + y] = make_float2(-2.f * zn.y, -2.f * zn.x);
+    }
     // odd samples of the upsampled line: iFFT_N(Z * s)
 #pragma unroll
     for (int i = 0; i < EN; i++) {
@@ -155,138 +159,264 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
     line_fft_st<N, T, 1, false>(bz, t, twN);
     line_fft_st<N, T, 1, false>(bh, t, twN);
     // neg window of the shifted spectrum: E[X mod N] + exp(-2 pi i X/W) O[X mod N]
-    {
-      const int Xs = J.win[2 * (a * nC + cn)];
-      float2* I = J.I + (size_t)(a * nC + cn) * J.nWin * N;
-      for (int xl = t; xl < J.nWin; xl += T) {
-        int X = Xs + xl;
-        if (X >= W) X -= W;
-        const int m = X < N ? X : X - N;
-        const float2 e = bz[sidx(m)], o = bh[sidx(m)];
-        I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(e, cmul(twW[X], o));
-      }
-    }
-    // pos window from the mirrored neg transforms
-    {
-      const float2 d = make_float2(-2.f * nyqz.y, -2.f * nyqz.x);
-      const float2* Q = J.nyq + (size_t)(a * ((nC - 1) / 2) + (b - 1)) * N;
-      const int Xs = J.win[2 * (a * nC + cp)];
-      float2* I = J.I + (size_t)(a * nC + cp) * J.nWin * N;
-      for (int xl = t; xl < J.nWin; xl += T) {
-        int X = Xs + xl;
-        if (X >= W) X -= W;
-        const int m = X < N ? X : X - N;
-        const int mm = m == 0 ? 0 : N - m;
-        const float2 e = cconjf(bz[sidx(mm)]);
-        const float2 o = cadd(cconjf(bh[sidx(mm)]), cmul(d, __ldg(Q + m)));
-        I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(e, cmul(twW[X], o));
-      }
+    const int Xs = J.win[2 * (a * nC + cn)];
+    float2* I = J.I + (size_t)(a * nS + b) * J.nWin * N;
+    for (int xl = t; xl < J.nWin; xl += T) {
+      int X = Xs + xl;
+      if (X >= W) X -= W;
+      const int m = X < N ? X : X - N;
+      const float2 e = bz[sidx(m)], o = bh[sidx(m)];
+      I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(e, cmul(twW[X], o));
     }
     __syncthreads();
   }
 }
 
-// ---- pass B: columns ---------------------------------------------------------------------------
+// ---- pass G: the pos components' Nyquist columns ----------------------------------------------
+// The pos row spectrum of a pair differs from the mirrored neg one by exp(-2 pi i X/W) Qx[X]
+// times d(y) (pass A). Along y that column d is transformed once per angle and pair with the
+// pos component's y shift; pass B adds it scaled by exp(-2 pi i X/W) Qx[X mod N].
+template <int N, int ENV>
+__global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_g(const JobDesc* __restrict__ jobs) {
+  using P = Cfg<N, ENV>;
+  constexpr int W = P::W, T = P::T, EN = P::EN;
+  const int t = threadIdx.x, ab = blockIdx.x;
+  __shared__ JobDesc J;
+  __shared__ float2 bz[smem_line_elems(N, 1)], bh[smem_line_elems(N, 1)];
+  const float2* twN = g_stw + stw_offset(N, EN);
+  const float2* twW = g_tw + tw_offset(W);
+  load_job(&J, jobs + blockIdx.y, t, T);
+  __syncthreads();
+  const int nC = J.nC, nPair = (nC - 1) / 2;
+  if (ab >= J.nA * nPair) return;  // uniform per block
+  const int a = ab / nPair, cp = 2 * (1 + ab % nPair);
+  const float2* d = J.D + (size_t)ab * N;
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int k = t + i * T;
+    const float2 v = d[k];
+    bz[sidx(k)] = v;
+    bh[sidx(k)] = v;
+  }
+  __syncthreads();
+  line_fft_st<N, T, 1, false>(bh, t, twN);
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int m = t + i * T;
+    bh[sidx(m)] = cmul(bh[sidx(m)], half_shift<N>(twW, m));
+  }
+  __syncthreads();
+  line_fft_st<N, T, 1, true>(bh, t, twN);
+  const float2* re = J.ramps + (size_t)(a * nC + cp) * 2 * W + W;  // y ramps
+  const float2* ro = re + N;
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int m = t + i * T;
+    bz[sidx(m)] = cmul(bz[sidx(m)], __ldg(re + m));
+    bh[sidx(m)] = cmul(bh[sidx(m)], __ldg(ro + m));
+  }
+  __syncthreads();
+  line_fft_st<N, T, 1, false>(bz, t, twN);
+  line_fft_st<N, T, 1, false>(bh, t, twN);
+  const int Ys = J.win[2 * (a * nC + cp) + 1];
+  for (int yl = t; yl < J.nWin; yl += T) {
+    int Y = Ys + yl;
+    if (Y >= W) Y -= W;
+    const int m = Y < N ? Y : Y - N;
+    J.G[(size_t)ab * J.nWin + yl] = cadd(bz[sidx(m)], cmul(twW[Y], bh[sidx(m)]));
+  }
+}
+
+// ---- pass B1: column transforms of band 0 and of the neg components ----------------------------
+// One block per CB window columns of one component: band 0 (the windows of all angles summed:
+// they share one unshifted mask) is transformed along y and pasted; each pair's neg
+// component gets the full y shift (even/odd split). The results over the component's
+// row window go to Tw in quad layout; for neg columns also d' = -2i conj(Z[N/2]).
 template <int N, int ENV, int CBV>
-__global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_pass_b(const JobDesc* __restrict__ jobs) {
+__global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_pass_b1(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N, ENV, CBV>;
   constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN;
-  const int q = blockIdx.x;  // column group: X = q*CB + lane
   const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
   __shared__ JobDesc J;
   extern __shared__ float2 sm[];
-  float2* acc = sm;                                // W x CB
-  float2* bz = acc + smem_line_elems(W, CB);       // N x CB
-  float2* bh = bz + smem_line_elems(N, CB);        // N x CB
+  float2* bz = sm;                           // N x CB
+  float2* bh = bz + smem_line_elems(N, CB);  // N x CB
+  const float2* twN = g_stw + stw_offset(N, EN);
+  const float2* twW = g_tw + tw_offset(W);
+  load_job(&J, jobs + blockIdx.z, lt, CB * T);
+  __syncthreads();
+  const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2, nS = 1 + nPair;
+  const int comp = blockIdx.y;  // 0: band 0; 1 + a*nPair + (b-1): neg of (a, b)
+  if (comp > J.nA * nPair || (int)blockIdx.x * CB >= nWin) return;  // uniform per block
+  const int xl = blockIdx.x * CB + lane;  // nWin is a multiple of 4: every lane is inside
+  const size_t quad = ((size_t)(xl >> 2) * N) * 4 + (xl & 3);
+  float2* out = J.Tw + (size_t)comp * nWin * nWin + ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3);
+  if (comp == 0) {
+#pragma unroll
+    for (int i = 0; i < EN; i++) {
+      const int k = t + i * T;
+      float2 v = make_float2(0.f, 0.f);
+      for (int a = 0; a < J.nA; a++) {
+        const float2 u = J.I[(size_t)a * nS * nWin * N + quad + (size_t)k * 4];
+        v.x += u.x;
+        v.y += u.y;
+      }
+      bh[sidx(k * CB + lane)] = v;
+    }
+    __syncthreads();
+    line_fft_st<N, T, CB, false>(bh, lt, twN);
+    const int Ys = J.win[1];
+    for (int yl = t; yl < nWin; yl += T) {
+      int Y = Ys + yl;
+      if (Y >= W) Y -= W;
+      const int m = paste_src<N>(Y);
+      out[(size_t)yl * 4] = m >= 0 ? bh[sidx(m * CB + lane)] : make_float2(0.f, 0.f);
+    }
+    return;
+  }
+  const int a = (comp - 1) / nPair, b = 1 + (comp - 1) % nPair, cn = 2 * b - 1;
+  const float2* I = J.I + (size_t)(a * nS + b) * nWin * N + quad;
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int k = t + i * T;
+    const float2 v = I[(size_t)k * 4];
+    bz[sidx(k * CB + lane)] = v;
+    bh[sidx(k * CB + lane)] = v;
+  }
+  __syncthreads();
+  line_fft_st<N, T, CB, false>(bh, lt, twN);  // Z along y
+  if (t == (N / 2) % T) {
+    const float2 z = bh[sidx((N / 2) * CB + lane)];
+    J.Dy[(size_t)(comp - 1) * nWin + xl] = make_float2(-2.f * z.y, -2.f * z.x);
+  }
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int m = t + i * T;
+    bh[sidx(m * CB + lane)] = cmul(bh[sidx(m * CB + lane)], half_shift<N>(twW, m));
+  }
+  __syncthreads();
+  line_fft_st<N, T, CB, true>(bh, lt, twN);
+  const float2* re = J.ramps + (size_t)(a * nC + cn) * 2 * W + W;  // y ramps
+  const float2* ro = re + N;
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int m = t + i * T;
+    bz[sidx(m * CB + lane)] = cmul(bz[sidx(m * CB + lane)], __ldg(re + m));
+    bh[sidx(m * CB + lane)] = cmul(bh[sidx(m * CB + lane)], __ldg(ro + m));
+  }
+  __syncthreads();
+  line_fft_st<N, T, CB, false>(bz, lt, twN);
+  line_fft_st<N, T, CB, false>(bh, lt, twN);
+  const int Yn = J.win[2 * (a * nC + cn) + 1];
+  for (int yl = t; yl < nWin; yl += T) {
+    int Y = Yn + yl;
+    if (Y >= W) Y -= W;
+    const int m = Y < N ? Y : Y - N;
+    out[(size_t)yl * 4] = cadd(bz[sidx(m * CB + lane)], cmul(twW[Y], bh[sidx(m * CB + lane)]));
+  }
+}
+
+// ---- pass B2: masked sum over components, Wiener x apodization, inverse FFT_W along y ------------
+// CB output columns per block; each thread keeps the 2*EN rows Y = t + i*T of its column in
+// registers. The pos component of a pair at (X, Y) comes from the neg transform at (-X, -Y),
+// stored at the mirrored window position (the neg window is the pos window's mirror image):
+//   F_pos[X][Y] = conj(F_neg[-X][-Y]) + exp(-2 pi i Y/W) d'(-X) Qy[Y mod N]
+//                 + exp(-2 pi i X/W) Qx[X mod N] G[Y]
+// (the identity of pass A along y, plus pass G's column for the x term).
+template <int N, int ENV, int CBV>
+__global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_pass_b2(const JobDesc* __restrict__ jobs) {
+  using P = Cfg<N, ENV, CBV>;
+  constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN;
+  const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
+  const int X = blockIdx.x * CB + lane;
+  __shared__ JobDesc J;
+  extern __shared__ float2 sm[];
+  float2* bz = sm;                           // N x CB
+  float2* bh = bz + smem_line_elems(N, CB);  // N x CB
   const float2* twN = g_stw + stw_offset(N, EN);
   const float2* twW = g_tw + tw_offset(W);
   load_job(&J, jobs + blockIdx.y, lt, CB * T);
-#pragma unroll
-  for (int i = 0; i < 2 * EN; i++) acc[sidx((t + i * T) * CB + lane)] = make_float2(0.f, 0.f);
   __syncthreads();
-  const int nC = J.nC, nWin = J.nWin;
-  // components: band 0 of all angles shares the unshifted mask and is summed before its
-  // FFT; every shifted component is transformed on its own.
-  for (int a = -1; a < J.nA; a++) {
-    for (int c = (a < 0 ? 0 : 1); c < (a < 0 ? 1 : nC); c++) {
-      const int aw = a < 0 ? 0 : a;
-      int xl = q * CB - J.win[2 * (aw * nC + c)];
-      if (xl < 0) xl += W;
-      if (xl >= nWin) continue;  // uniform: the whole group is outside this window
-      const int qi = xl / 4, sub = xl & 3;
+  const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2;
+  auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
+  float2 acc[2 * EN];
 #pragma unroll
-      for (int i = 0; i < EN; i++) {
-        const int k = t + i * T;
-        float2 v = make_float2(0.f, 0.f);
-        const int a0 = a < 0 ? 0 : a, a1 = a < 0 ? J.nA : a + 1;
-        for (int aa = a0; aa < a1; aa++) {
-          const float2 u = J.I[(size_t)(aa * nC + c) * nWin * N + ((size_t)qi * N + k) * 4 + sub + lane];
-          v.x += u.x;
-          v.y += u.y;
+  for (int i = 0; i < 2 * EN; i++) acc[i] = make_float2(0.f, 0.f);
+  // window position (xl, yl) -> offset in a quad-layout nWin x nWin window
+  auto qoff = [&](int xl) { return ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3); };
+  {  // band 0
+    const int xl = wrap(X - J.win[0]), Ys = J.win[1];
+    if (xl < nWin) {
+      const float* mk = J.masks + qoff(xl);
+      const float2* tv = J.Tw + qoff(xl);
+#pragma unroll
+      for (int i = 0; i < 2 * EN; i++) {
+        const int yl = wrap(t + i * T - Ys);
+        if (yl < nWin) {
+          const float f = __ldg(mk + (size_t)yl * 4);
+          const float2 u = tv[(size_t)yl * 4];
+          acc[i].x += f * u.x;
+          acc[i].y += f * u.y;
         }
-        bz[sidx(k * CB + lane)] = v;
-        bh[sidx(k * CB + lane)] = v;
       }
-      __syncthreads();
-      line_fft_st<N, T, CB, false>(bh, lt, twN);  // Z along y
-      const int Ys = J.win[2 * (aw * nC + c) + 1];
-      const float* mk = J.masks + (size_t)(aw * nC + c) * nWin * nWin + (size_t)qi * nWin * 4 + sub + lane;
-      if (c == 0) {
-        for (int yl = t; yl < nWin; yl += T) {
-          int Y = Ys + yl;
-          if (Y >= W) Y -= W;
-          const int m = paste_src<N>(Y);
-          if (m >= 0) {
+    }
+  }
+  for (int a = 0; a < J.nA; a++) {
+    for (int b = 1; b <= nPair; b++) {
+      const int cn = 2 * b - 1, cp = 2 * b, ab = a * nPair + (b - 1);
+      const float2* Tc = J.Tw + (size_t)(1 + ab) * nWin * nWin;
+      const int xn = wrap(X - J.win[2 * (a * nC + cn)]);
+      if (xn < nWin) {
+        const int Yn = J.win[2 * (a * nC + cn) + 1];
+        const float* mk = J.masks + (size_t)(a * nC + cn) * nWin * nWin + qoff(xn);
+        const float2* tv = Tc + qoff(xn);
+#pragma unroll
+        for (int i = 0; i < 2 * EN; i++) {
+          const int yl = wrap(t + i * T - Yn);
+          if (yl < nWin) {
             const float f = __ldg(mk + (size_t)yl * 4);
-            const float2 u = bh[sidx(m * CB + lane)];
-            float2& o = acc[sidx(Y * CB + lane)];
-            o.x += f * u.x;
-            o.y += f * u.y;
+            const float2 u = tv[(size_t)yl * 4];
+            acc[i].x += f * u.x;
+            acc[i].y += f * u.y;
           }
         }
-      } else {
+      }
+      const int xp = wrap(X - J.win[2 * (a * nC + cp)]);
+      if (xp < nWin) {
+        const int Yp = J.win[2 * (a * nC + cp) + 1];
+        const int xm = nWin - 1 - xp;  // window column of -X in the neg window
+        const float* mk = J.masks + (size_t)(a * nC + cp) * nWin * nWin + qoff(xp);
+        const float2* tv = Tc + qoff(xm);
+        const float2* Qx = J.nyq + (size_t)(ab * 2) * N;
+        const float2* Qy = Qx + N;
+        const float2 dp = J.Dy[(size_t)ab * nWin + xm];
+        const float2 cx = cmul(twW[X], __ldg(Qx + (X < N ? X : X - N)));
+        const float2* G = J.G + (size_t)ab * nWin;
 #pragma unroll
-        for (int i = 0; i < EN; i++) {
-          const int m = t + i * T;
-          bh[sidx(m * CB + lane)] = cmul(bh[sidx(m * CB + lane)], half_shift<N>(twW, m));
-        }
-        __syncthreads();
-        line_fft_st<N, T, CB, true>(bh, lt, twN);
-        const float2* re = J.ramps + (size_t)(a * nC + c) * 2 * W + W;  // y ramps
-        const float2* ro = re + N;
-#pragma unroll
-        for (int i = 0; i < EN; i++) {
-          const int m = t + i * T;
-          bz[sidx(m * CB + lane)] = cmul(bz[sidx(m * CB + lane)], __ldg(re + m));
-          bh[sidx(m * CB + lane)] = cmul(bh[sidx(m * CB + lane)], __ldg(ro + m));
-        }
-        __syncthreads();
-        line_fft_st<N, T, CB, false>(bz, lt, twN);
-        line_fft_st<N, T, CB, false>(bh, lt, twN);
-        for (int yl = t; yl < nWin; yl += T) {
-          int Y = Ys + yl;
-          if (Y >= W) Y -= W;
-          const int m = Y < N ? Y : Y - N;
-          const float f = __ldg(mk + (size_t)yl * 4);
-          const float2 u = cadd(bz[sidx(m * CB + lane)], cmul(twW[Y], bh[sidx(m * CB + lane)]));
-          float2& o = acc[sidx(Y * CB + lane)];
-          o.x += f * u.x;
-          o.y += f * u.y;
+        for (int i = 0; i < 2 * EN; i++) {
+          const int Y = t + i * T;
+          const int yl = wrap(Y - Yp);
+          if (yl < nWin) {
+            const int m = Y < N ? Y : Y - N;
+            const float f = __ldg(mk + (size_t)yl * 4);
+            const float2 e = cconjf(tv[(size_t)(nWin - 1 - yl) * 4]);
+            const float2 u = cadd(cadd(e, cmul(twW[Y], cmul(dp, __ldg(Qy + m)))), cmul(cx, G[yl]));
+            acc[i].x += f * u.x;
+            acc[i].y += f * u.y;
+          }
         }
       }
-      __syncthreads();
     }
   }
   // Wiener denominator x apodization, then iFFT_W along y as two N-point inverse FFTs:
   //   out[2n] = iFFT_N(A[k] + A[k+N]),  out[2n+1] = iFFT_N((A[k] - A[k+N]) exp(i pi k/N))
-  const int X0 = q * CB;
-  const float* wa = J.wa + (size_t)(X0 / 4) * W * 4 + (X0 & 3) + lane;
+  const float* wa = J.wa + (size_t)(X >> 2) * W * 4 + (X & 3);
 #pragma unroll
   for (int i = 0; i < EN; i++) {
     const int k = t + i * T;
     const float f0 = __ldg(wa + (size_t)k * 4), f1 = __ldg(wa + (size_t)(k + N) * 4);
-    const float2 a0 = acc[sidx(k * CB + lane)], a1 = acc[sidx((k + N) * CB + lane)];
-    const float2 u0 = make_float2(a0.x * f0, a0.y * f0), u1 = make_float2(a1.x * f1, a1.y * f1);
+    const float2 u0 = make_float2(acc[i].x * f0, acc[i].y * f0);
+    const float2 u1 = make_float2(acc[i + EN].x * f1, acc[i + EN].y * f1);
     bz[sidx(k * CB + lane)] = cadd(u0, u1);
     bh[sidx(k * CB + lane)] = cmul(csub(u0, u1), cconjf(twW[k]));
   }
@@ -296,8 +426,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_p
 #pragma unroll
   for (int i = 0; i < EN; i++) {
     const int k = t + i * T;
-    J.O[(size_t)(2 * k) * W + X0 + lane] = bz[sidx(k * CB + lane)];
-    J.O[(size_t)(2 * k + 1) * W + X0 + lane] = bh[sidx(k * CB + lane)];
+    J.O[(size_t)(2 * k) * W + X] = bz[sidx(k * CB + lane)];
+    J.O[(size_t)(2 * k + 1) * W + X] = bh[sidx(k * CB + lane)];
   }
 }
 
@@ -333,9 +463,10 @@ static int launch_offline_v(const JobDesc* d_jobs, int njobs, int maxA, int maxP
   constexpr int W = PC::W;
   cudaEvent_t* ev = profile_events();
   static bool attr = false;
-  const size_t smem_b = sizeof(float2) * (smem_line_elems(W, PB::CB) + 2 * smem_line_elems(N, PB::CB));
+  const size_t smem_b = sizeof(float2) * 2 * smem_line_elems(N, PB::CB);
   if (!attr) {
-    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
+    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b1<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
+    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b2<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
     FSIM_CUDA(cudaFuncSetAttribute(k_pass_a<N, ENA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(sizeof(float) * FSIM_MAX_PHASES * N)));
     attr = true;
@@ -343,12 +474,16 @@ static int launch_offline_v(const JobDesc* d_jobs, int njobs, int maxA, int maxP
   if (ev) cudaEventRecord(ev[0], st);
   k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, sizeof(float) * maxP * N, st>>>(d_jobs);
   if (ev) cudaEventRecord(ev[1], st);
-  k_pass_b<N, ENB, CBB><<<dim3(W / PB::CB, njobs), PB::CB * PB::T, smem_b, st>>>(d_jobs);
+  k_pass_g<N, ENA><<<dim3(maxA * (FSIM_MAX_BANDS - 1), njobs), PA::T, 0, st>>>(d_jobs);
+  k_pass_b1<N, ENB, CBB><<<dim3(W / PB::CB, 1 + maxA * (FSIM_MAX_BANDS - 1), njobs), PB::CB * PB::T, smem_b, st>>>(
+      d_jobs);
   if (ev) cudaEventRecord(ev[2], st);
+  k_pass_b2<N, ENB, CBB><<<dim3(W / PB::CB, njobs), PB::CB * PB::T, smem_b, st>>>(d_jobs);
+  if (ev) cudaEventRecord(ev[3], st);
   k_pass_c<N><<<dim3(W / PC::GC, njobs), PC::GC * PC::TC, 0, st>>>(d_jobs);
   if (ev) {
-    cudaEventRecord(ev[3], st);
-    profile_mark(3);
+    cudaEventRecord(ev[4], st);
+    profile_mark(4);
   }
   FSIM_CHECK_LAUNCH();
   return FSIM_OK;
@@ -371,7 +506,7 @@ __host__ inline int size_slot(int n) {
   return -1;
 }
 
-// variant lists: pass A elements/thread {E0, E1}; pass B (elements, columns)
+// variant lists: pass A elements/thread {E0, E1}; passes B1/B2 (elements, columns per block)
 // {(E0,4), (E0,2), (E1,4), (E1,2)} with E0 = 8, E1 = 16 (3*2^k sizes: 12, 24)
 template <int N>
 int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st) {

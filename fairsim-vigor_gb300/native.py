@@ -154,6 +154,7 @@ _SIGS = {
     "fsim_profiler": (I32, [I32]),
     "fsim_fft_plan_2d": (I32, [I32, I32, C.POINTER(C.c_int64)]),
     "fsim_vec_reshape": (I32, [VP, I32, I32]),
+    "fsim_fft2d_batch": (I32, [VP, I32, I32, I32, I32, VP]),
     "fsim_vec_set_elem": (I32, [VP, C.c_size_t, C.c_float, C.c_float]),
     "fsim_vec_get_elem": (I32, [VP, C.c_size_t, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "fsim_set_stream": (I32, [VP]),

@@ -112,6 +112,10 @@ int fsim_vec_sum(const fsim_vec* x, double* re, double* im);            /* sumEl
 int fsim_vec_dot(const fsim_vec* x, const fsim_vec* y, double* re, double* im); /* <conj(x), y> */
 /* nativeFFT (AccelVectorCplx.java:489): 2D C2C in place; inverse scaled 1/(w*h) */
 int fsim_vec_fft2d(fsim_vec* v, int inverse);
+/* The same 2D FFT on `batch` contiguous w x h complex float32 planes in device memory
+ * (row-major, interleaved), on `stream`; inverse scaled 1/(w*h). No reference counterpart
+ * (the reference transforms one vector per JNI call). */
+int fsim_fft2d_batch(void* data, int w, int h, int batch, int inverse, void* stream);
 /* nativeFourierShift (AccelVectorCplx.java:490): v *= exp(i 2pi (kx x + ky y)/N), square N */
 int fsim_vec_fourier_shift(fsim_vec* v, double kx, double ky);
 /* nativePasteFreq (AccelVectorCplx.java:491): zero out, place in's spectrum with offset */
@@ -214,7 +218,7 @@ int fsim_tune_get(int n, int path, int pass, int* variant, int* n_variants);
 /* Per-pass CUDA-event timing of fused batches (no reference counterpart): while enabled,
  * every batch records events between its passes on its stream; fsim_profile_read waits
  * for the last batch and returns the duration of each pass of its last size class
- * (offline: A, B, C; live: LA, LB, LC, LD). */
+ * (offline: A, G+B1, B2, C; live: LA, LB, LC, LD). */
 int fsim_profile_enable(int on);
 int fsim_profile_read(float* ms, int max_passes, int* n_passes);
 /* Host-buffer convenience: H2D copy of raw, reconstruction, D2H copy of out. */

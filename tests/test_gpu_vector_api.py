@@ -236,7 +236,7 @@ def test_accel_natives_set_get_reshape_plan_buffers(fs, V):
     fs.native.check(lib.fsim_fft_plan_2d(32, 64, C.byref(plan)))
     assert (plan.value >> 32, plan.value & 0xffffffff) == (32, 64)
     v.fft2d(False)
-    assert rel_l2(v.vectorData(), np.fft.fft2(z.astype(np.complex128))) < 3e-6
+    assert rel_l2(v.vectorData().reshape(64, 32), np.fft.fft2(z.astype(np.complex128))) < 3e-6
     assert lib.fsim_vec_reshape(v.handle, 33, 64) == fs.native.FSIM_EINVAL
     assert lib.fsim_vec_set_elem(v.handle, 64 * 32, 0.0, 0.0) == fs.native.FSIM_EINVAL
     for host in (0, 1):
@@ -246,3 +246,22 @@ def test_accel_natives_set_get_reshape_plan_buffers(fs, V):
         fs.native.check(lib.fsim_buffer_free(p, host))
     fs.native.check(lib.fsim_profiler(1))
     fs.native.check(lib.fsim_profiler(0))
+
+
+@pytest.mark.parametrize("w,h,batch", [(64, 64, 3), (384, 384, 2), (512, 256, 4)])
+def test_fft2d_batch_on_device_buffers(fs, V, w, h, batch):
+    import ctypes as C
+
+    import torch
+
+    rng = np.random.default_rng(w * h + batch)
+    z = (rng.standard_normal((batch, h, w)) + 1j * rng.standard_normal((batch, h, w))).astype(np.complex64)
+    d = torch.from_numpy(z).cuda()
+    lib = fs.native.lib()
+    fs.native.check(lib.fsim_fft2d_batch(C.c_void_p(d.data_ptr()), w, h, batch, 0, None))
+    torch.cuda.synchronize()
+    assert rel_l2(d.cpu().numpy(), np.fft.fft2(z.astype(np.complex128))) < 3e-6
+    fs.native.check(lib.fsim_fft2d_batch(C.c_void_p(d.data_ptr()), w, h, batch, 1, None))
+    torch.cuda.synchronize()
+    assert rel_l2(d.cpu().numpy(), z) < 3e-6
+    assert lib.fsim_fft2d_batch(C.c_void_p(d.data_ptr()), 100, h, batch, 0, None) == fs.native.FSIM_EINVAL
