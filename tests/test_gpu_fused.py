@@ -3,7 +3,7 @@ the C ABI) against the oracle's restatement of the reference:
   * offline path = SimAlgorithm.runReconstruction with the GUI's input preparation
     (org/fairsim/sim_gui/ImageControl.java:819-836), CLIPSCALE.NONE;
   * live path = ReconstructionThread.run (org/fairsim/livemode/ReconstructionRunner.java:434-542).
-Tolerance: relative L2 <= 1e-4 against the reference's float semantics (spec bound),
+Tolerance: relative L2 <= 1e-4 against the reference's float semantics (the parity bound),
 and the error against the FP64 oracle is checked to stay below 1e-5."""
 import numpy as np
 import pytest
