@@ -64,7 +64,6 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
   __shared__ JobDesc J;
   __shared__ float2 bz[smem_line_elems(N, 1)], bh[smem_line_elems(N, 1)];
   __shared__ float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
-  extern __shared__ float rows[];  // nP raw rows of this image row (background clip, damping)
   const float2* twN = g_stw + stw_offset(N, EN);  // stage table, read through L1
   const float2* twW = g_tw + tw_offset(W);
   load_job(&J, jobs + blockIdx.z, t, T);
@@ -72,27 +71,23 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
   if (a >= J.nA) return;  // uniform per block
   const int nP = J.nP, nC = J.nC, nPair = (nC - 1) / 2, nS = 1 + nPair;  // I slots per angle
   for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
-  const size_t frame = (size_t)N * N, row = (size_t)y * N;
-  for (int p = 0; p < nP; p++) {
-#pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int x = t + i * T;
-      const size_t at = (size_t)(a * nP + p) * frame + row + x;
-      float v = J.input_u16 ? (float)__ldg((const uint16_t*)J.raw + at) : __ldg((const float*)J.raw + at);
-      if (J.bgr != 0.f) {
-        v = v - J.bgr;
-        if (v < 0) v = 0;
-      }
-      if (J.damp) v = v * __ldg(J.damp + row + x);
-      rows[p * N + x] = v;
-    }
-  }
   __syncthreads();
-  auto mix = [&](int cm, int x) {  // band separation in real space
+  const size_t frame = (size_t)N * N, row = (size_t)y * N;
+  auto raw_at = [&](int p, int x) {  // background clip and border damping of one raw pixel
+    const size_t at = (size_t)(a * nP + p) * frame + row + x;
+    float v = J.input_u16 ? (float)__ldg((const uint16_t*)J.raw + at) : __ldg((const float*)J.raw + at);
+    if (J.bgr != 0.f) {
+      v = v - J.bgr;
+      if (v < 0) v = 0;
+    }
+    if (J.damp) v = v * __ldg(J.damp + row + x);
+    return v;
+  };
+  auto mix = [&](int cm, int x) {  // band separation in real space (pairs after the first)
     float2 z = make_float2(0.f, 0.f);
     for (int p = 0; p < nP; p++) {
       const float2 m = coef[cm * nP + p];
-      const float v = rows[p * N + x];
+      const float v = raw_at(p, x);
       z.x += m.x * v;
       z.y += m.y * v;
     }
@@ -100,15 +95,35 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __rest
   };
   // Components: band 0, then per band b the pair neg = 2b-1, pos = 2b. The separation
   // coefficients of a pair are complex conjugates, so z_pos = conj(z_neg): the pos
-  // component's row transform follows from the neg one's (below).
-  for (int b = 0; b < (nC + 1) / 2; b++) {
-    const int cm = b == 0 ? 0 : 2 * b - 1;
+  // component's row transform follows from the neg one's (below). The row is read once
+  // for band 0 (into bh) and the first pair's neg component (into bz, idle during band 0).
 #pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int x = t + i * T;
-      const float2 z = mix(cm, x);
-      bz[sidx(x)] = z;
-      bh[sidx(x)] = z;
+  for (int i = 0; i < EN; i++) {
+    const int x = t + i * T;
+    float2 z0 = make_float2(0.f, 0.f), zn = make_float2(0.f, 0.f);
+    for (int p = 0; p < nP; p++) {
+      const float v = raw_at(p, x);
+      const float2 m0 = coef[p], mn = coef[(nC > 1 ? nP : 0) + p];
+      z0.x += m0.x * v;
+      z0.y += m0.y * v;
+      zn.x += mn.x * v;
+      zn.y += mn.y * v;
+    }
+    bh[sidx(x)] = z0;
+    bz[sidx(x)] = zn;
+  }
+  for (int b = 0; b < (nC + 1) / 2; b++) {
+    if (b == 1) {
+#pragma unroll
+      for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = bz[sidx(t + i * T)];
+    } else if (b > 1) {
+#pragma unroll
+      for (int i = 0; i < EN; i++) {
+        const int x = t + i * T;
+        const float2 z = mix(2 * b - 1, x);
+        bz[sidx(x)] = z;
+        bh[sidx(x)] = z;
+      }
     }
     __syncthreads();
     line_fft_st<N, T, 1, false>(bh, t, twN);  // Z = FFT_N(z)
@@ -387,8 +402,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_p
         const int xm = nWin - 1 - xp;  // window column of -X in the neg window
         const float* mk = J.masks + (size_t)(a * nC + cp) * nWin * nWin + qoff(xp);
         const float2* tv = Tc + qoff(xm);
-        const float2* Qx = J.nyq + (size_t)(ab * 2) * N;
-        const float2* Qy = Qx + N;
+        const float2* Qx = J.nyq + (size_t)ab * (N + W);
+        const float2* QyT = Qx + N;  // exp(-2 pi i Y/W) Qy[Y mod N]
         const float2 dp = J.Dy[(size_t)ab * nWin + xm];
         const float2 cx = cmul(twW[X], __ldg(Qx + (X < N ? X : X - N)));
         const float2* G = J.G + (size_t)ab * nWin;
@@ -397,10 +412,9 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_p
           const int Y = t + i * T;
           const int yl = wrap(Y - Yp);
           if (yl < nWin) {
-            const int m = Y < N ? Y : Y - N;
             const float f = __ldg(mk + (size_t)yl * 4);
             const float2 e = cconjf(tv[(size_t)(nWin - 1 - yl) * 4]);
-            const float2 u = cadd(cadd(e, cmul(twW[Y], cmul(dp, __ldg(Qy + m)))), cmul(cx, G[yl]));
+            const float2 u = cadd(cadd(e, cmul(dp, __ldg(QyT + Y))), cmul(cx, G[yl]));
             acc[i].x += f * u.x;
             acc[i].y += f * u.y;
           }
@@ -467,12 +481,10 @@ static int launch_offline_v(const JobDesc* d_jobs, int njobs, int maxA, int maxP
   if (!attr) {
     FSIM_CUDA(cudaFuncSetAttribute(k_pass_b1<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
     FSIM_CUDA(cudaFuncSetAttribute(k_pass_b2<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
-    FSIM_CUDA(cudaFuncSetAttribute(k_pass_a<N, ENA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)(sizeof(float) * FSIM_MAX_PHASES * N)));
     attr = true;
   }
   if (ev) cudaEventRecord(ev[0], st);
-  k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, sizeof(float) * maxP * N, st>>>(d_jobs);
+  k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, 0, st>>>(d_jobs);
   if (ev) cudaEventRecord(ev[1], st);
   k_pass_g<N, ENA><<<dim3(maxA * (FSIM_MAX_BANDS - 1), njobs), PA::T, 0, st>>>(d_jobs);
   k_pass_b1<N, ENB, CBB><<<dim3(W / PB::CB, 1 + maxA * (FSIM_MAX_BANDS - 1), njobs), PB::CB * PB::T, smem_b, st>>>(
