@@ -317,6 +317,12 @@ def main():
     h2d = B * NA * NP * N * N * 4
     d2h = B * 4 * N * N * 4
     clk = clocks.stop()
+    # the host link alone: one pinned upload of the raw batch and one download of the images
+    with torch.cuda.stream(stream):
+        raw_dev.copy_(raw_host, non_blocking=True)
+        out_host.copy_(out_dev, non_blocking=True)
+    h2d_ms = timed(lambda: raw_dev.copy_(raw_host, non_blocking=True), 2) / 2
+    d2h_ms = timed(lambda: out_host.copy_(out_dev, non_blocking=True), 2) / 2
 
     # ---- per-pass timing (CUDA events between the passes of the direct batch call) ----
     import ctypes as C
@@ -374,7 +380,8 @@ def main():
                        "l2": "inputs larger than L2 (%.0f MiB raw per step)" % (h2d / 2 ** 20),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": "recon/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "call": "fsim_recon_batch_host (pinned host buffers; chunked upload/passes/download overlapped)"},
+                    "call": "fsim_recon_batch_host (pinned host buffers; chunked upload/passes/download overlapped)",
+                    "h2d_GB_per_s_alone": h2d / (h2d_ms / 1000) / 1e9, "d2h_GB_per_s_alone": d2h / (d2h_ms / 1000) / 1e9},
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "algorithmic_bytes_per_launch": algo[dom] * B},
