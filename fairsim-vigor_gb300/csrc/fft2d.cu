@@ -4,6 +4,8 @@
 //   pass 2: columns - C adjacent columns per block interleaved in shared memory so that
 //           every global access moves C*8 contiguous bytes (64 B for C = 8).
 // Each pass reads and writes the array once (16 bytes per complex element per pass).
+// Twiddles come from the per-stage tables (one to three loads per butterfly, the other
+// powers by products), read through L1.
 #include "common.cuh"
 #include "fft_line.cuh"
 #include "runtime.cuh"
@@ -33,7 +35,7 @@ __global__ void __launch_bounds__(256) k_fft_rows(float2* __restrict__ data, int
     for (int i = 0; i < E; i++) s[sidx(t + i * T)] = base[t + i * T];
   }
   __syncthreads();
-  line_fft<L, T, 1, INV>(s, t);
+  line_fft_st<L, T, 1, INV>(s, t, g_stw + stw_offset(L, E));
   if (row < nrows) {
 #pragma unroll
     for (int i = 0; i < E; i++) base[t + i * T] = cscale(s[sidx(t + i * T)], scale);
@@ -54,7 +56,7 @@ __global__ void k_fft_cols(float2* __restrict__ data, int ncols, size_t item_str
     s[sidx(k * C + c)] = (x < ncols) ? base[(size_t)k * ncols + x] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  line_fft<L, T, C, INV>(s, threadIdx.x);
+  line_fft_st<L, T, C, INV>(s, threadIdx.x, g_stw + stw_offset(L, E));
   if (x < ncols) {
 #pragma unroll
     for (int i = 0; i < E; i++) {

@@ -217,11 +217,13 @@ __device__ __forceinline__ void dft(float2* v) {
 __host__ __device__ constexpr int pick_radix(int rem, int E) { return pick_radix_fwd(rem, E); }
 
 // ---- one Stockham stage ---------------------------------------------------------
-template <int L, int T, int C, int R, int NS, bool INV, int TS>
+template <int L, int T, int C, int R, int NS, bool INV, int TS, int M = 1>
 __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2* tw) {
   // TS > 0: plain table exp(-2 pi i m/(L*TS)) read at stride TS; TS == 0: stage table
-  // [r-1][k] of this stage (tw points at the stage's first entry)
-  constexpr int E = L / T, NB = E / R, LR = L / R;
+  // [r-1][k] of this stage (tw points at the stage's first entry).
+  // M > 1: the thread transforms M adjacent lines c*M .. c*M+M-1 of C*M interleaved lines,
+  // with one set of twiddles for all of them.
+  constexpr int E = L / T, NB = E / R, LR = L / R, CL = C * M;
   // The twiddle loads depend only on the thread's index: issue them first, so that their
   // latency overlaps the shared-memory reads and the barrier.
   constexpr int NT = NS > 1 ? (TS > 0 ? R - 1 : (R == 16 ? 3 : (R >= 8 || R == 3 ? 2 : 1))) : 1;
@@ -242,12 +244,14 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2*
       }
     }
   }
-  float2 v[NB][R];
+  float2 v[NB][M][R];
 #pragma unroll
   for (int b = 0; b < NB; b++) {
     const int j = t + b * T;
 #pragma unroll
-    for (int r = 0; r < R; r++) v[b][r] = s[sidx((j + r * LR) * C + c)];
+    for (int l = 0; l < M; l++)
+#pragma unroll
+      for (int r = 0; r < R; r++) v[b][l][r] = s[sidx((j + r * LR) * CL + c * M + l)];
   }
   __syncthreads();
 #pragma unroll
@@ -284,25 +288,29 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2*
       for (int r = 1; r < R; r++) {
         float2 ww = w[r];
         if (INV) ww.y = -ww.y;
-        v[b][r] = cmul(v[b][r], ww);
+#pragma unroll
+        for (int l = 0; l < M; l++) v[b][l][r] = cmul(v[b][l][r], ww);
       }
     }
-    dft<R, INV>(v[b]);
     const int base = (j / NS) * NS * R + k;
 #pragma unroll
-    for (int r = 0; r < R; r++) s[sidx((base + r * NS) * C + c)] = v[b][r];
+    for (int l = 0; l < M; l++) {
+      dft<R, INV>(v[b][l]);
+#pragma unroll
+      for (int r = 0; r < R; r++) s[sidx((base + r * NS) * CL + c * M + l)] = v[b][l][r];
+    }
   }
   __syncthreads();
 }
 
-template <int L, int T, int C, bool INV, int NS, int TS>
+template <int L, int T, int C, bool INV, int NS, int TS, int M = 1>
 __device__ __forceinline__ void fft_stages(float2* s, int c, int t, const float2* tw) {
   if constexpr (NS < L) {
     constexpr int R = pick_radix(L / NS, L / T);
     static_assert((L / NS) % R == 0 && (L / T) % R == 0, "bad radix plan");
-    fft_stage<L, T, C, R, NS, INV, TS>(s, c, t, tw);
+    fft_stage<L, T, C, R, NS, INV, TS, M>(s, c, t, tw);
     // stage tables: the next stage's entries follow this stage's (R-1)*NS entries
-    fft_stages<L, T, C, INV, NS * R, TS>(s, c, t, TS > 0 ? tw : tw + (R - 1) * NS);
+    fft_stages<L, T, C, INV, NS * R, TS, M>(s, c, t, TS > 0 ? tw : tw + (R - 1) * NS);
   }
 }
 
@@ -328,6 +336,18 @@ template <int L, int T, int C, bool INV>
 __device__ __forceinline__ void line_fft_st(float2* s, int lt, const float2* stw_smem) {
   static_assert(supported_len(L) && plan_ok(L, T) && stw_ok(L, L / T), "no stage table for this plan");
   fft_stages<L, T, C, INV, 1, 0>(s, lt % C, lt / C, stw_smem);
+}
+// C*M interleaved lines by C*T threads, M adjacent lines per thread (stage tables).
+template <int L, int T, int C, int M, bool INV>
+__device__ __forceinline__ void line_fft_st_m(float2* s, int lt, const float2* stw) {
+  static_assert(supported_len(L) && plan_ok(L, T) && stw_ok(L, L / T), "no stage table for this plan");
+  fft_stages<L, T, C, INV, 1, 0, M>(s, lt % C, lt / C, stw);
+}
+// One line `c` of CL interleaved lines, by T threads (lane t).
+template <int L, int T, int CL, bool INV>
+__device__ __forceinline__ void line_fft_st_one(float2* s, int c, int t, const float2* stw) {
+  static_assert(supported_len(L) && plan_ok(L, T) && stw_ok(L, L / T), "no stage table for this plan");
+  fft_stages<L, T, CL, INV, 1, 0>(s, c, t, stw);
 }
 template <int L, int E>
 __device__ __forceinline__ void stage_stage_twiddles(float2* dst, int tid, int nthreads) {

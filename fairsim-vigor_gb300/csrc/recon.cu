@@ -161,15 +161,13 @@ int Plan::build(cudaStream_t st) {
       win[2 * (a * nC + cn) + 1] = ((W - win[2 * (a * nC + cp) + 1] - nwin + 1) % W + W) % W;
     }
   // Nyquist response of each pair's pos component along x and along y:
-  // Q[m] = FFT_N((-1)^n ro[n]) with ro[n] = exp(+2 pi i k (2n+1)/W)/W (k = kx, resp. -ky),
-  // i.e. exp(i phi0)/W * sum_n exp(i theta n), theta = 4 pi k/W + pi - 2 pi m/N, in closed
-  // form. Stored per (a, b) as Qx[N] followed by exp(-2 pi i Y/W) Qy[Y mod N] for Y < W.
-  std::vector<float2> nyq((size_t)nA * nPair * (N + W));
+  // FFT_N((-1)^n ro[n]) with ro[n] = exp(+2 pi i k (2n+1)/W)/W (k = kx, resp. -ky), i.e.
+  // exp(i phi0)/W * sum_n exp(i theta n), theta = 4 pi k/W + pi - 2 pi m/N, in closed form
+  std::vector<float2> nyq((size_t)nA * nPair * 2 * N);
   for (int a = 0; a < nA; a++)
     for (int b = 1; b <= nPair; b++) {
       double kx, ky;
       comp_shift(&prm, a, 2 * b, &kx, &ky);
-      float2* out = &nyq[((size_t)a * nPair + (b - 1)) * (N + W)];
       for (int dim = 0; dim < 2; dim++) {
         const double k = dim == 0 ? kx : -ky;
         const double f0 = k / W - std::floor(k / W), f1 = 2 * k / W - std::floor(2 * k / W);
@@ -186,14 +184,7 @@ int Plan::build(cudaStream_t st) {
             S = (1.0 - std::polar(1.0, 2 * M_PI * fn)) / (1.0 - std::polar(1.0, th));
           }
           const std::complex<double> q = e0 * S;
-          if (dim == 0) {
-            out[m] = make_float2((float)q.real(), (float)q.imag());
-          } else {
-            for (int Y = m; Y < W; Y += N) {
-              const std::complex<double> v = std::polar(1.0, -2 * M_PI * (double)Y / W) * q;
-              out[N + Y] = make_float2((float)v.real(), (float)v.imag());
-            }
-          }
+          nyq[(((size_t)a * nPair + (b - 1)) * 2 + dim) * N + m] = make_float2((float)q.real(), (float)q.imag());
         }
       }
     }

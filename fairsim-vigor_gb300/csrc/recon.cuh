@@ -19,9 +19,8 @@ struct JobDesc {
   const int* win;       // [a][c] {Xs, Ys} window origins (offline) / {xInt, yInt} paste offsets (live)
   const float* masks;   // [a][c] OTF masks (offline) / N*N conj-OTF vector (live)
   const float* wa;      // Wiener x apodization, quad layout [X/4][Y][X%4]
-  const float2* nyq;    // offline: [a][b-1][N + W]: Qx[N] = FFT_N((-1)^n ro_pos[n]) of the pos component's
-                        // x odd-sample ramp (the Nyquist response, see pass A), then
-                        // exp(-2 pi i Y/W) Qy[Y mod N] for Y < W (the same along y)
+  const float2* nyq;    // offline: [a][b-1][x, y][N] FFT_N((-1)^n ro_pos[n]) of the pos component's x and y
+                        // odd-sample ramps (the Nyquist response, see pass A)
   float2* I;            // workspace: row-transformed windows [a][band 0, neg of each pair][nWin/4][N][4]
   float2* D;            // workspace: [a][b-1][N] Nyquist term d of every row's neg component (pass A)
   float2* G;            // workspace: [a][b-1][nWin] column transform of D with the pos y shift (pass G)

@@ -56,8 +56,15 @@ __device__ __forceinline__ int paste_src(int X) {
 }
 
 // ---- pass A: rows ----------------------------------------------------------------------------
+// 64-thread blocks at up to 8 elements per thread: ask for 20 resident blocks (51
+// registers) so that registers, not only shared memory, allow 40 warps per SM.
+template <int T, int EN>
+__host__ __device__ constexpr int pass_a_min_blocks() {
+  return (T == 64 && EN <= 8) ? 20 : 1;
+}
 template <int N, int ENV>
-__global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_a(const JobDesc* __restrict__ jobs) {
+__global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>::T, Cfg<N, ENV>::EN>())
+    k_pass_a(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N, ENV>;
   constexpr int W = P::W, T = P::T, EN = P::EN;
   const int y = blockIdx.x, a = blockIdx.y, t = threadIdx.x;
@@ -402,8 +409,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_p
         const int xm = nWin - 1 - xp;  // window column of -X in the neg window
         const float* mk = J.masks + (size_t)(a * nC + cp) * nWin * nWin + qoff(xp);
         const float2* tv = Tc + qoff(xm);
-        const float2* Qx = J.nyq + (size_t)ab * (N + W);
-        const float2* QyT = Qx + N;  // exp(-2 pi i Y/W) Qy[Y mod N]
+        const float2* Qx = J.nyq + (size_t)(ab * 2) * N;
+        const float2* Qy = Qx + N;
         const float2 dp = J.Dy[(size_t)ab * nWin + xm];
         const float2 cx = cmul(twW[X], __ldg(Qx + (X < N ? X : X - N)));
         const float2* G = J.G + (size_t)ab * nWin;
@@ -412,9 +419,10 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_p
           const int Y = t + i * T;
           const int yl = wrap(Y - Yp);
           if (yl < nWin) {
+            const int m = Y < N ? Y : Y - N;
             const float f = __ldg(mk + (size_t)yl * 4);
             const float2 e = cconjf(tv[(size_t)(nWin - 1 - yl) * 4]);
-            const float2 u = cadd(cadd(e, cmul(dp, __ldg(QyT + Y))), cmul(cx, G[yl]));
+            const float2 u = cadd(cadd(e, cmul(twW[Y], cmul(dp, __ldg(Qy + m)))), cmul(cx, G[yl]));
             acc[i].x += f * u.x;
             acc[i].y += f * u.y;
           }
