@@ -109,15 +109,17 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
   for (size_t g = 0; g < groups.size() && rc == FSIM_OK; g++) {
     const int k = groups[g].first, e = groups[g].second;
     const Plan* p0 = static_cast<const Plan*>(jobs[order[k]].plan);
-    int maxA = 0, maxP = 0;
+    int maxA = 0, maxPair = 0, maxWin = 0;
     for (int i = k; i < e; i++) {
-      maxA = std::max(maxA, static_cast<const Plan*>(jobs[order[i]].plan)->prm.nr_dirs);
-      maxP = std::max(maxP, static_cast<const Plan*>(jobs[order[i]].plan)->prm.nr_phases);
+      const Plan* pi = static_cast<const Plan*>(jobs[order[i]].plan);
+      maxA = std::max(maxA, pi->prm.nr_dirs);
+      maxPair = std::max(maxPair, pi->prm.nr_bands - 1);
+      maxWin = std::max(maxWin, pi->nwin);
     }
     // largest classes sort last; the first class stays on st, the rest spread over aux
     cudaStream_t s = (nfork > 0 && g > 0) ? aux[(g - 1) % nfork] : st;
     rc = (p0->path == FSIM_PATH_LIVE) ? launch_live_size(p0->prm.w, d_table + k, e - k, maxA, s)
-                                      : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxP, s);
+                                      : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxPair, maxWin, s);
   }
   if (nfork > 0) {
     // join even after a failed launch, so that a capture in progress can still end

@@ -310,15 +310,15 @@ int offline_tune_get(int n, int pass) {
   return k < 0 ? -1 : (pass == 0 ? g_var_a : g_var_b)[k];
 }
 
-extern template int launch_offline<64>(const JobDesc*, int, int, int, cudaStream_t);
-extern template int launch_offline<128>(const JobDesc*, int, int, int, cudaStream_t);
-extern template int launch_offline<192>(const JobDesc*, int, int, int, cudaStream_t);
-extern template int launch_offline<256>(const JobDesc*, int, int, int, cudaStream_t);
-extern template int launch_offline<384>(const JobDesc*, int, int, int, cudaStream_t);
-extern template int launch_offline<512>(const JobDesc*, int, int, int, cudaStream_t);
-extern template int launch_offline<768>(const JobDesc*, int, int, int, cudaStream_t);
-extern template int launch_offline<1024>(const JobDesc*, int, int, int, cudaStream_t);
-extern template int launch_offline<2048>(const JobDesc*, int, int, int, cudaStream_t);
+extern template int launch_offline<64>(const JobDesc*, int, int, int, int, cudaStream_t);
+extern template int launch_offline<128>(const JobDesc*, int, int, int, int, cudaStream_t);
+extern template int launch_offline<192>(const JobDesc*, int, int, int, int, cudaStream_t);
+extern template int launch_offline<256>(const JobDesc*, int, int, int, int, cudaStream_t);
+extern template int launch_offline<384>(const JobDesc*, int, int, int, int, cudaStream_t);
+extern template int launch_offline<512>(const JobDesc*, int, int, int, int, cudaStream_t);
+extern template int launch_offline<768>(const JobDesc*, int, int, int, int, cudaStream_t);
+extern template int launch_offline<1024>(const JobDesc*, int, int, int, int, cudaStream_t);
+extern template int launch_offline<2048>(const JobDesc*, int, int, int, int, cudaStream_t);
 
 #define FSIM_RECON_SIZES(X) X(64) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(2048)
 
@@ -333,11 +333,11 @@ bool offline_size_supported(int n) {
   }
 }
 
-int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st) {
+int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st) {
   switch (n) {
 #define CASE(v) \
   case v:       \
-    return launch_offline<v>(d_jobs, njobs, maxA, maxP, st);
+    return launch_offline<v>(d_jobs, njobs, maxA, maxPair, maxWin, st);
     FSIM_RECON_SIZES(CASE)
 #undef CASE
   }

@@ -73,7 +73,9 @@ int offline_variants(int pass);
 int offline_tune_set(int n, int pass, int v);
 int offline_tune_get(int n, int pass);
 bool live_size_supported(int n);
-int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st);
+// maxA, maxPair, maxWin: the largest angle count, band-pair count and OTF-support window
+// of the batch's datasets of size n (they bound the grids; extra blocks exit at once)
+int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st);
 int launch_live_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);
 
 // Fill the job table of a batch (sorted by path and size) into host_table, optionally copy it

@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::TC) k_pass_c(const JobDesc
 
 // ---- launch ---------------------------------------------------------------------------------------
 template <int N, int ENA, int ENB, int CBB>
-static int launch_offline_v(const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st) {
+static int launch_offline_v(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st) {
   using PA = Cfg<N, ENA>;
   using PB = Cfg<N, ENB, CBB>;
   using PC = Cfg<N>;
@@ -494,9 +494,9 @@ static int launch_offline_v(const JobDesc* d_jobs, int njobs, int maxA, int maxP
   if (ev) cudaEventRecord(ev[0], st);
   k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, 0, st>>>(d_jobs);
   if (ev) cudaEventRecord(ev[1], st);
-  k_pass_g<N, ENA><<<dim3(maxA * (FSIM_MAX_BANDS - 1), njobs), PA::T, 0, st>>>(d_jobs);
-  k_pass_b1<N, ENB, CBB><<<dim3(W / PB::CB, 1 + maxA * (FSIM_MAX_BANDS - 1), njobs), PB::CB * PB::T, smem_b, st>>>(
-      d_jobs);
+  k_pass_g<N, ENA><<<dim3(maxA * maxPair, njobs), PA::T, 0, st>>>(d_jobs);
+  k_pass_b1<N, ENB, CBB><<<dim3((maxWin + PB::CB - 1) / PB::CB, 1 + maxA * maxPair, njobs), PB::CB * PB::T, smem_b,
+                           st>>>(d_jobs);
   if (ev) cudaEventRecord(ev[2], st);
   k_pass_b2<N, ENB, CBB><<<dim3(W / PB::CB, njobs), PB::CB * PB::T, smem_b, st>>>(d_jobs);
   if (ev) cudaEventRecord(ev[3], st);
@@ -529,12 +529,12 @@ __host__ inline int size_slot(int n) {
 // variant lists: pass A elements/thread {E0, E1}; passes B1/B2 (elements, columns per block)
 // {(E0,4), (E0,2), (E1,4), (E1,2)} with E0 = 8, E1 = 16 (3*2^k sizes: 12, 24)
 template <int N>
-int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxP, cudaStream_t st) {
+int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st) {
   constexpr bool p3 = (N % 3 == 0);
   constexpr int E0 = p3 ? 12 : 8, E1 = p3 ? 24 : 16;
   const int k = size_slot(N);
   const int va = g_var_a[k], vb = g_var_b[k];
-#define L_(EA, EB, CB) return launch_offline_v<N, EA, EB, CB>(d_jobs, njobs, maxA, maxP, st)
+#define L_(EA, EB, CB) return launch_offline_v<N, EA, EB, CB>(d_jobs, njobs, maxA, maxPair, maxWin, st)
   if constexpr (N <= 128 || N >= 2048) {
     L_(E0, E0, (N >= 2048 ? 2 : 4));  // single variant at the extremes
   } else {
