@@ -360,6 +360,7 @@ def main():
         extras["serve_saturated"]["speedup_vs_plain"] = (extras["serve_saturated"]["recon_per_s"]
                                                          / extras["plain_gpu"]["value"])
         extras["mixed_batch"] = mixed_leg(fs, torch, stream, timed)
+        extras["live_batch"] = live_leg(fs, torch, stream, timed)
         extras["large_3x5_2048"] = large_leg(fs, torch, stream, timed)
         extras["estimate_1024"] = estimate_leg(fs, torch)
         extras["fft2d_vs_cufft"] = [fft_leg(fs, torch, stream, timed, n, b) for n, b in ((512, 64), (1024, 16))]
@@ -473,6 +474,35 @@ def mixed_leg(fs, torch, stream, timed, n_datasets=64, steps=5, seed=77):
     for p in plans:
         p.close()
     return res
+
+
+def live_leg(fs, torch, stream, timed, batch=64, steps=10):
+    """The live path's kernels (ReconstructionThread semantics: u16 frames, damping, OTF
+    before the fast shift, apodization bend 1) on a device-resident batch of 512^2 stacks
+    from 3 channels, one CUDA-graph replay per step: the device throughput behind the
+    served form."""
+    N_ = fs.native
+    chans = []
+    for ch, lam in enumerate([488.0, 525.0, 600.0]):
+        raw, truth = fs.synth.make_dataset(n=N, seed=700 + ch, em_wavelength=lam, as_u16=True)
+        plan = fs.plan.ReconPlan(fs.synth.sim_param_for(truth, N), path=N_.PATH_LIVE, input_type=N_.INPUT_U16,
+                                 fade_px=10)
+        chans.append((plan, torch.from_numpy(raw.view(np.int16)).cuda()))
+    plans = [chans[i % 3][0] for i in range(batch)]
+    raws = [chans[i % 3][1].clone() for i in range(batch)]
+    outs = torch.empty((batch, 2 * N, 2 * N), dtype=torch.float32, device="cuda")
+    wfs = torch.empty((batch, N, N), dtype=torch.float32, device="cuda")
+    ws = torch.empty(fs.plan.batch_workspace_bytes(plans), dtype=torch.uint8, device="cuda")
+    jobs = [(p, r.data_ptr(), outs[i].data_ptr(), wfs[i].data_ptr()) for i, (p, r) in enumerate(zip(plans, raws))]
+    g = fs.plan.BatchGraph(jobs, ws.data_ptr(), ws.numel(), stream.cuda_stream)
+    for _ in range(3):
+        g.launch(stream.cuda_stream)
+    ms = timed(lambda: g.launch(stream.cuda_stream), steps)
+    g.close()
+    for p, _ in chans:
+        p.close()
+    return {"recon_per_s": batch * steps / (ms / 1000.0), "ms_per_batch": ms / steps, "batch": batch,
+            "workload": "live path, 512^2 3x3 u16 -> 1024^2 + widefield, 3 channels"}
 
 
 def large_leg(fs, torch, stream, timed, steps=5):

@@ -186,8 +186,9 @@ int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t w
                      void* stream);
 /* Host-buffer batch (replaces the per-op Java-array copies of the accel vectors,
  * AccelVectorReal.java:218-247 / AccelVectorCplx.java:296-331, for whole stacks): uploads,
- * passes and downloads of successive chunks of `chunk` jobs (0 = about 96 MiB of raw frames)
- * overlap on three library-owned streams; returns when every output is in host memory.
+ * passes and downloads of successive chunks of `chunk` jobs
+ * overlap on three library-owned streams (chunk 0 = about 40 MiB of raw frames); returns
+ * when every output is in host memory.
  * Page-locked host buffers are copied by DMA; pageable ones copy synchronously. One call
  * runs at a time per process (others wait). */
 typedef struct fsim_host_job {
