@@ -1,8 +1,8 @@
 """Autotuner for the fused reconstruction's launch shapes.
 
 For every image size it times each variant of the row pass (elements per thread, i.e. the
-radix plan and threads per line) and of the column passes (elements per thread x interleaved
-columns per block) with the library's per-pass CUDA events on a batch of datasets larger
+radix plan and threads per line) and of each of the two column passes (elements per thread x
+interleaved columns per block) with the library's per-pass CUDA events on a batch of datasets larger
 than L2, picks the fastest of each, and writes ``tuning.json`` next to this file.
 ``native.init()`` applies the table (fsim_tune_set). Variants change launch shapes only;
 every variant computes the same reconstruction (covered by tests/test_gpu_fused.py).
@@ -64,26 +64,28 @@ def tune(sizes=(256, 384, 512, 768, 1024), reps=5, target_bytes=1 << 30, verbose
             lib.fsim_profile_enable(0)
             return np.median(np.array(ms), axis=0)
 
-        na, nb = C.c_int(), C.c_int()
         v, cnt = C.c_int(), C.c_int()
-        N_.check(lib.fsim_tune_get(n, N_.PATH_OFFLINE, 0, C.byref(v), C.byref(cnt)))
-        nva = cnt.value
-        N_.check(lib.fsim_tune_get(n, N_.PATH_OFFLINE, 1, C.byref(v), C.byref(cnt)))
-        nvb = cnt.value
-        a_ms, b_ms = [], []
-        N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, 1, 0))
-        for va in range(nva):
-            N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, 0, va))
-            a_ms.append(float(measure()[0]))
-        best_a = int(np.argmin(a_ms))
-        N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, 0, best_a))
-        for vb in range(nvb):
-            N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, 1, vb))
-            m = measure()
-            b_ms.append(float(sum(m[1:-1])))  # the column passes (G+B1, B2)
-        best_b = int(np.argmin(b_ms))
-        N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, 1, best_b))
-        result[str(n)] = {"a": best_a, "b": best_b, "batch": B, "a_ms": a_ms, "b_ms": b_ms,
+        counts = []
+        for p in range(3):
+            N_.check(lib.fsim_tune_get(n, N_.PATH_OFFLINE, p, C.byref(v), C.byref(cnt)))
+            counts.append(cnt.value)
+        for p in range(3):
+            N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, p, 0))
+        # one pass at a time, the others at their best so far; the per-pass CUDA events give
+        # [A, G+B1, B2, C]
+        timed_index = {0: 0, 1: 1, 2: 2}
+        best, times = [], []
+        for p in range(3):
+            ms = []
+            for var in range(counts[p]):
+                N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, p, var))
+                ms.append(float(measure()[timed_index[p]]))
+            b = int(np.argmin(ms))
+            N_.check(lib.fsim_tune_set(n, N_.PATH_OFFLINE, p, b))
+            best.append(b)
+            times.append(ms)
+        result[str(n)] = {"a": best[0], "b": best[1], "b2": best[2], "batch": B, "a_ms": times[0],
+                          "b1_ms": times[1], "b2_ms": times[2],
                           "us_per_dataset": float(sum(measure())) * 1000 / B}
         if verbose:
             print(n, result[str(n)], flush=True)

@@ -366,7 +366,7 @@ int fsim_tune_set(int n, int path, int pass, int variant) {
 
 int fsim_tune_get(int n, int path, int pass, int* variant, int* n_variants) {
   FSIM_REQUIRE(variant && n_variants, FSIM_EINVAL, "tune_get: bad arguments");
-  FSIM_REQUIRE(path == FSIM_PATH_OFFLINE && pass >= 0 && pass <= 1, FSIM_EINVAL, "tune_get: bad path/pass");
+  FSIM_REQUIRE(path == FSIM_PATH_OFFLINE && pass >= 0 && pass <= 2, FSIM_EINVAL, "tune_get: bad path/pass");
   *variant = offline_tune_get(n, pass);
   *n_variants = offline_variants(pass);
   FSIM_REQUIRE(*variant >= 0, FSIM_EINVAL, "tune_get: unsupported size %d", n);

@@ -293,21 +293,21 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws
 }
 
 // ---- autotuned variants ------------------------------------------------------------------------
-int g_var_a[16] = {0}, g_var_b[16] = {0};
-// variant lists: pass A elements/thread {default, alternative}; pass B (elements, columns)
-//   pow2 sizes:  A {16, 8}      B {(16,4), (8,4), (16,2), (8,2)}
-//   3*2^k sizes: A {24, 12}     B {(24,4), (12,4), (24,2), (12,2)}
+int g_var_a[16] = {0}, g_var_b[16] = {0}, g_var_b2[16] = {0};
+// variant lists: pass 0 = A (and G) elements/thread {default, alternative}; passes 1 = B1 and
+// 2 = B2 (elements, columns per block), four each (recon_kernels.cuh, launch_offline)
 int offline_variants(int pass) { return pass == 0 ? 2 : 4; }
+static int* var_table(int pass) { return pass == 0 ? g_var_a : (pass == 1 ? g_var_b : g_var_b2); }
 int offline_tune_set(int n, int pass, int v) {
   int k = size_slot(n);
-  FSIM_REQUIRE(k >= 0 && pass >= 0 && pass <= 1 && v >= 0 && v < offline_variants(pass), FSIM_EINVAL,
+  FSIM_REQUIRE(k >= 0 && pass >= 0 && pass <= 2 && v >= 0 && v < offline_variants(pass), FSIM_EINVAL,
                "tune: bad size/pass/variant %d/%d/%d", n, pass, v);
-  (pass == 0 ? g_var_a : g_var_b)[k] = v;
+  var_table(pass)[k] = v;
   return FSIM_OK;
 }
 int offline_tune_get(int n, int pass) {
   int k = size_slot(n);
-  return k < 0 ? -1 : (pass == 0 ? g_var_a : g_var_b)[k];
+  return (k < 0 || pass < 0 || pass > 2) ? -1 : var_table(pass)[k];
 }
 
 extern template int launch_offline<64>(const JobDesc*, int, int, int, int, cudaStream_t);

@@ -476,41 +476,47 @@ __global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::TC) k_pass_c(const JobDesc
   for (int i = 0; i < EW; i++) out[t + i * T] = s[sidx(t + i * T)].x * scale;
 }
 
-// ---- launch ---------------------------------------------------------------------------------------
-template <int N, int ENA, int ENB, int CBB>
-static int launch_offline_v(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st) {
+// ---- launch ----------------------------------------------------------------------------------------
+// Each pass has its own launch-shape variants (autotuner: tuning.json); a batch launches
+// A, G, B1, B2, C in order on one stream.
+template <int N, int ENA>
+static void launch_a(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, cudaStream_t st) {
   using PA = Cfg<N, ENA>;
+  k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, 0, st>>>(d_jobs);
+}
+template <int N, int ENA>
+static void launch_g(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, cudaStream_t st) {
+  using PA = Cfg<N, ENA>;
+  k_pass_g<N, ENA><<<dim3(maxA * maxPair, njobs), PA::T, 0, st>>>(d_jobs);
+}
+template <int N, int ENB, int CBB>
+static int launch_b1(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st) {
   using PB = Cfg<N, ENB, CBB>;
-  using PC = Cfg<N>;
-  constexpr int W = PC::W;
-  cudaEvent_t* ev = profile_events();
+  const size_t smem = sizeof(float2) * 2 * smem_line_elems(N, PB::CB);
   static bool attr = false;
-  const size_t smem_b = sizeof(float2) * 2 * smem_line_elems(N, PB::CB);
   if (!attr) {
-    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b1<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
-    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b2<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
+    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b1<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  if (ev) cudaEventRecord(ev[0], st);
-  k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, 0, st>>>(d_jobs);
-  if (ev) cudaEventRecord(ev[1], st);
-  k_pass_g<N, ENA><<<dim3(maxA * maxPair, njobs), PA::T, 0, st>>>(d_jobs);
-  k_pass_b1<N, ENB, CBB><<<dim3((maxWin + PB::CB - 1) / PB::CB, 1 + maxA * maxPair, njobs), PB::CB * PB::T, smem_b,
+  k_pass_b1<N, ENB, CBB><<<dim3((maxWin + PB::CB - 1) / PB::CB, 1 + maxA * maxPair, njobs), PB::CB * PB::T, smem,
                            st>>>(d_jobs);
-  if (ev) cudaEventRecord(ev[2], st);
-  k_pass_b2<N, ENB, CBB><<<dim3(W / PB::CB, njobs), PB::CB * PB::T, smem_b, st>>>(d_jobs);
-  if (ev) cudaEventRecord(ev[3], st);
-  k_pass_c<N><<<dim3(W / PC::GC, njobs), PC::GC * PC::TC, 0, st>>>(d_jobs);
-  if (ev) {
-    cudaEventRecord(ev[4], st);
-    profile_mark(4);
+  return FSIM_OK;
+}
+template <int N, int ENB, int CBB>
+static int launch_b2(const JobDesc* d_jobs, int njobs, cudaStream_t st) {
+  using PB = Cfg<N, ENB, CBB>;
+  const size_t smem = sizeof(float2) * 2 * smem_line_elems(N, PB::CB);
+  static bool attr = false;
+  if (!attr) {
+    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b2<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
   }
-  FSIM_CHECK_LAUNCH();
+  k_pass_b2<N, ENB, CBB><<<dim3(PB::W / PB::CB, njobs), PB::CB * PB::T, smem, st>>>(d_jobs);
   return FSIM_OK;
 }
 
 // tuned variants per size: index into the variant lists of launch_offline
-extern int g_var_a[16], g_var_b[16];
+extern int g_var_a[16], g_var_b[16], g_var_b2[16];
 __host__ inline int size_slot(int n) {
   switch (n) {
     case 64: return 0;
@@ -526,31 +532,57 @@ __host__ inline int size_slot(int n) {
   return -1;
 }
 
-// variant lists: pass A elements/thread {E0, E1}; passes B1/B2 (elements, columns per block)
-// {(E0,4), (E0,2), (E1,4), (E1,2)} with E0 = 8, E1 = 16 (3*2^k sizes: 12, 24)
+// variant lists: pass A (and G) elements/thread {E0, E1}; passes B1 and B2, each on its own,
+// (elements, columns per block) {(E0,4), (E0,2), (E1,4), (E1,2)} with E0 = 8, E1 = 16
+// (3*2^k sizes: 12, 24). The extremes (N <= 128, N >= 2048) have one variant.
 template <int N>
 int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st) {
   constexpr bool p3 = (N % 3 == 0);
   constexpr int E0 = p3 ? 12 : 8, E1 = p3 ? 24 : 16;
+  constexpr bool single = (N <= 128 || N >= 2048);
+  constexpr int CBX = N >= 2048 ? 2 : 4;
   const int k = size_slot(N);
-  const int va = g_var_a[k], vb = g_var_b[k];
-#define L_(EA, EB, CB) return launch_offline_v<N, EA, EB, CB>(d_jobs, njobs, maxA, maxPair, maxWin, st)
-  if constexpr (N <= 128 || N >= 2048) {
-    L_(E0, E0, (N >= 2048 ? 2 : 4));  // single variant at the extremes
+  const int va = single ? 0 : g_var_a[k], vb1 = single ? 0 : g_var_b[k], vb2 = single ? 0 : g_var_b2[k];
+  cudaEvent_t* ev = profile_events();
+  if (ev) cudaEventRecord(ev[0], st);
+  if (va == 0) launch_a<N, E0>(d_jobs, njobs, maxA, maxPair, st);
+  else if constexpr (!single) launch_a<N, E1>(d_jobs, njobs, maxA, maxPair, st);
+  if (ev) cudaEventRecord(ev[1], st);
+  if (va == 0) launch_g<N, E0>(d_jobs, njobs, maxA, maxPair, st);
+  else if constexpr (!single) launch_g<N, E1>(d_jobs, njobs, maxA, maxPair, st);
+  int rc = FSIM_OK;
+  if constexpr (single) {
+    rc = launch_b1<N, E0, CBX>(d_jobs, njobs, maxA, maxPair, maxWin, st);
   } else {
-    if (va == 0) {
-      if (vb == 0) L_(E0, E0, 4);
-      if (vb == 1) L_(E0, E0, 2);
-      if (vb == 2) L_(E0, E1, 4);
-      L_(E0, E1, 2);
-    } else {
-      if (vb == 0) L_(E1, E0, 4);
-      if (vb == 1) L_(E1, E0, 2);
-      if (vb == 2) L_(E1, E1, 4);
-      L_(E1, E1, 2);
+    switch (vb1) {
+      case 0: rc = launch_b1<N, E0, 4>(d_jobs, njobs, maxA, maxPair, maxWin, st); break;
+      case 1: rc = launch_b1<N, E0, 2>(d_jobs, njobs, maxA, maxPair, maxWin, st); break;
+      case 2: rc = launch_b1<N, E1, 4>(d_jobs, njobs, maxA, maxPair, maxWin, st); break;
+      default: rc = launch_b1<N, E1, 2>(d_jobs, njobs, maxA, maxPair, maxWin, st); break;
     }
   }
-#undef L_
+  if (rc) return rc;
+  if (ev) cudaEventRecord(ev[2], st);
+  if constexpr (single) {
+    rc = launch_b2<N, E0, CBX>(d_jobs, njobs, st);
+  } else {
+    switch (vb2) {
+      case 0: rc = launch_b2<N, E0, 4>(d_jobs, njobs, st); break;
+      case 1: rc = launch_b2<N, E0, 2>(d_jobs, njobs, st); break;
+      case 2: rc = launch_b2<N, E1, 4>(d_jobs, njobs, st); break;
+      default: rc = launch_b2<N, E1, 2>(d_jobs, njobs, st); break;
+    }
+  }
+  if (rc) return rc;
+  if (ev) cudaEventRecord(ev[3], st);
+  using PC = Cfg<N>;
+  k_pass_c<N><<<dim3(PC::W / PC::GC, njobs), PC::GC * PC::TC, 0, st>>>(d_jobs);
+  if (ev) {
+    cudaEventRecord(ev[4], st);
+    profile_mark(4);
+  }
+  FSIM_CHECK_LAUNCH();
+  return FSIM_OK;
 }
 
 }  // namespace fsim

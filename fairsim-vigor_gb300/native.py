@@ -267,6 +267,7 @@ def apply_tuning(path=None):
     for n, v in t.get("offline", {}).items():
         check(lib().fsim_tune_set(int(n), PATH_OFFLINE, 0, int(v["a"])))
         check(lib().fsim_tune_set(int(n), PATH_OFFLINE, 1, int(v["b"])))
+        check(lib().fsim_tune_set(int(n), PATH_OFFLINE, 2, int(v.get("b2", v["b"]))))
     _tuned = True
     return True
 

@@ -212,7 +212,8 @@ int fsim_batch_graph_info(const fsim_batch_graph* g, int* n_jobs, int* n_kernels
 int fsim_batch_graph_destroy(fsim_batch_graph* g);
 /* Kernel variant per image size (no reference counterpart), chosen by the project's
  * autotuner (fairsim-vigor_gb300/autotune.py, results in tuning.json): pass 0 = row pass
- * (elements per thread), pass 1 = column pass (elements per thread x interleaved columns).
+ * (elements per thread), pass 1 = column transforms, pass 2 = masked column sum and inverse
+ * (elements per thread x interleaved columns).
  * Variants only change launch shapes; results are identical to float rounding. */
 int fsim_tune_set(int n, int path, int pass, int variant);
 int fsim_tune_get(int n, int path, int pass, int* variant, int* n_variants);

@@ -158,18 +158,19 @@ def test_every_tuned_variant_matches_oracle(fs, oracle, n):
     plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
     v, cnt = C.c_int(), C.c_int()
     saved = []
-    for p in (0, 1):
+    for p in (0, 1, 2):
         fs.native.check(lib.fsim_tune_get(n, fs.native.PATH_OFFLINE, p, C.byref(v), C.byref(cnt)))
         saved.append((v.value, cnt.value))
     try:
-        for va in range(saved[0][1]):
-            for vb in range(saved[1][1]):
-                fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 0, va))
-                fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 1, vb))
-                assert rel_l2(plan.reconstruct_host(raw), exp) < 1e-4, (va, vb)
+        # every variant of each pass, the other passes at their tuned choice
+        for p in (0, 1, 2):
+            for var in range(saved[p][1]):
+                fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, p, var))
+                assert rel_l2(plan.reconstruct_host(raw), exp) < 1e-4, (p, var)
+            fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, p, saved[p][0]))
     finally:
-        fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 0, saved[0][0]))
-        fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, 1, saved[1][0]))
+        for p in (0, 1, 2):
+            fs.native.check(lib.fsim_tune_set(n, fs.native.PATH_OFFLINE, p, saved[p][0]))
 
 
 def test_batch_graph_replays_match_batch(fs, torch_cuda):
