@@ -60,7 +60,13 @@ __device__ __forceinline__ int paste_src(int X) {
 // registers) so that registers, not only shared memory, allow 40 warps per SM.
 template <int T, int EN>
 __host__ __device__ constexpr int pass_a_min_blocks() {
-  return (T == 64 && EN <= 8) ? 20 : 1;
+  return (T == 64 && EN <= 8) ? 20 : ((T == 32 && EN == 12) ? 20 : ((T == 64 && EN == 12) ? 10 : 1));
+}
+// The column passes at 12 elements per thread (3*2^k sizes) otherwise hold 120-160
+// registers per thread: ask for a budget of about 80.
+template <int THREADS, int EN>
+__host__ __device__ constexpr int col_min_blocks() {
+  return EN == 12 ? (65536 / (THREADS * 80) > 0 ? 65536 / (THREADS * 80) : 1) : 1;
 }
 template <int N, int ENV>
 __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>::T, Cfg<N, ENV>::EN>())
@@ -255,7 +261,9 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_g(const JobDesc* __rest
 // component gets the full y shift (even/odd split). The results over the component's
 // row window go to Tw in quad layout; for neg columns also d' = -2i conj(Z[N/2]).
 template <int N, int ENV, int CBV>
-__global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_pass_b1(const JobDesc* __restrict__ jobs) {
+__global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
+                                  col_min_blocks<Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T, Cfg<N, ENV, CBV>::EN>())
+    k_pass_b1(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N, ENV, CBV>;
   constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN;
   const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
@@ -346,7 +354,9 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_p
 //                 + exp(-2 pi i X/W) Qx[X mod N] G[Y]
 // (the identity of pass A along y, plus pass G's column for the x term).
 template <int N, int ENV, int CBV>
-__global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T) k_pass_b2(const JobDesc* __restrict__ jobs) {
+__global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
+                                  col_min_blocks<Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T, Cfg<N, ENV, CBV>::EN>())
+    k_pass_b2(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N, ENV, CBV>;
   constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN;
   const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
