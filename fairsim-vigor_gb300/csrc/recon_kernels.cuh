@@ -58,15 +58,19 @@ __device__ __forceinline__ int paste_src(int X) {
 // ---- pass A: rows ----------------------------------------------------------------------------
 // 64-thread blocks at up to 8 elements per thread: ask for 20 resident blocks (51
 // registers) so that registers, not only shared memory, allow 40 warps per SM.
+// Register budgets (the compiler otherwise keeps 90-230 registers per thread in the longer
+// radix plans, which caps occupancy at a few warps per scheduler): 48 per thread for the
+// 64-thread row blocks of 8 elements, 64 for longer rows at 8 elements, 96 at 12 elements.
 template <int T, int EN>
 __host__ __device__ constexpr int pass_a_min_blocks() {
-  return (T == 64 && EN <= 8) ? 20 : ((T == 32 && EN == 12) ? 20 : ((T == 64 && EN == 12) ? 10 : 1));
+  return EN <= 8 ? (T == 64 ? 20 : (65536 / (T * 64) > 0 ? 65536 / (T * 64) : 1))
+                 : (EN == 12 ? (65536 / (T * 96) > 0 ? 65536 / (T * 96) : 1) : 1);
 }
-// The column passes at 12 elements per thread (3*2^k sizes) otherwise hold 120-160
-// registers per thread: ask for a budget of about 80.
+// The column passes: 64 registers per thread at 8 elements, 80 at 12.
 template <int THREADS, int EN>
 __host__ __device__ constexpr int col_min_blocks() {
-  return EN == 12 ? (65536 / (THREADS * 80) > 0 ? 65536 / (THREADS * 80) : 1) : 1;
+  return EN <= 8 ? (65536 / (THREADS * 64) > 0 ? 65536 / (THREADS * 64) : 1)
+                 : (EN == 12 ? (65536 / (THREADS * 80) > 0 ? 65536 / (THREADS * 80) : 1) : 1);
 }
 template <int N, int ENV>
 __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>::T, Cfg<N, ENV>::EN>())
