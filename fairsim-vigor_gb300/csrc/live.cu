@@ -41,6 +41,12 @@ struct LCfg {
   static constexpr int CD = (N >= 2048) ? 2 : (N >= 1024 ? 4 : 8);  // columns per block, pass LD
 };
 
+// Register budget of about 80 per thread for the column and shift passes (they otherwise keep
+// 120-130 and run at 16 warps per SM).
+__host__ __device__ constexpr int live_min_blocks(int threads) {
+  return 65536 / (threads * 80) > 0 ? 65536 / (threads * 80) : 1;
+}
+
 // pasteFreq's source index for output index o (as in vec_ops.cu)
 __device__ __forceinline__ int paste_source(int o, int off, int ni, int no) {
   int p1 = ((o - off) % no + no) % no;
@@ -109,7 +115,8 @@ __global__ void __launch_bounds__(LCfg<N>::GA* LCfg<N>::TN) k_live_a(const JobDe
 
 // ---- LB -----------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(LCfg<N>::CBL* LCfg<N>::TN) k_live_b(const JobDesc* __restrict__ jobs) {
+__global__ void __launch_bounds__(LCfg<N>::CBL* LCfg<N>::TN, live_min_blocks(LCfg<N>::CBL* LCfg<N>::TN))
+    k_live_b(const JobDesc* __restrict__ jobs) {
   using P = LCfg<N>;
   constexpr int T = P::TN, C = P::CBL, E = P::EN;
   const JobDesc& J = jobs[blockIdx.y];
@@ -160,7 +167,7 @@ __global__ void __launch_bounds__(LCfg<N>::CBL* LCfg<N>::TN) k_live_b(const JobD
 
 // ---- LC -----------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(LCfg<N>::TW) k_live_c(const JobDesc* __restrict__ jobs) {
+__global__ void __launch_bounds__(LCfg<N>::TW, live_min_blocks(LCfg<N>::TW)) k_live_c(const JobDesc* __restrict__ jobs) {
   using P = LCfg<N>;
   constexpr int W = P::W, TW = P::TW, EW = P::EW, EN = N / TW;
   const JobDesc& J = jobs[blockIdx.y];
