@@ -216,10 +216,14 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--distinct", type=int, default=16)
     ap.add_argument("--no-extras", action="store_true", help="skip plain-GPU, serve, mixed, large and CPU legs")
+    ap.add_argument("--only", choices=["live", "fft", "estimate", "mixed", "large", "serve"],
+                    help="run one extra leg alone and print its JSON (profiling of its kernels)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        return run_only(args)
 
     import torch
 
@@ -398,6 +402,41 @@ def main():
     graph.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_only(args):
+    """One extra leg on its own (GPU 0), e.g. to capture its kernels with ncu."""
+    import torch
+
+    fs = load_package()
+    fs.native.init(0)
+    stream = torch.cuda.Stream()
+
+    def timed(fn, k):
+        with torch.cuda.stream(stream):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(k):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1)
+
+    if args.only == "live":
+        res = live_leg(fs, torch, stream, timed, batch=args.batch, steps=args.steps)
+    elif args.only == "fft":
+        res = [fft_leg(fs, torch, stream, timed, n, b, steps=args.steps) for n, b in ((512, 64), (1024, 16))]
+    elif args.only == "estimate":
+        res = estimate_leg(fs, torch, reps=max(1, args.steps))
+    elif args.only == "mixed":
+        res = mixed_leg(fs, torch, stream, timed, steps=args.steps)
+    elif args.only == "large":
+        res = large_leg(fs, torch, stream, timed, steps=args.steps)
+    else:
+        res = {"poisson": serve_leg(fs), "saturated": serve_capacity_leg(fs)}
+    print(json.dumps({args.only: res}))
     return 0
 
 
