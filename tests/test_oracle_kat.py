@@ -119,3 +119,17 @@ def test_estimation_recovers_seeded_k0(oracle, fs):
         assert abs(est["pX"][d] - truth["pxpy"][d][0]) < 0.1
         assert abs(est["pY"][d] - truth["pxpy"][d][1]) < 0.1
         assert abs(est["modulations"][d][1] - truth["modulation"]) < 0.15
+
+
+@pytest.mark.parametrize("n,n_phases,n_bands", [(64, 3, 2), (128, 3, 2), (128, 5, 2), (128, 5, 3)])
+def test_float_oracle_against_fp64_oracle(oracle, fs, n, n_phases, n_bands):
+    """The reference's float semantics (float phases, MTool.fsin/fcos, float vectors) stay
+    within the parity tolerance of the same algorithm in double precision; the error is
+    printed (the GPU path is compared against both)."""
+    raw, truth = fs.synth.make_dataset(n=n, seed=50 + n + n_phases, n_phases=n_phases, n_bands=n_bands)
+    sp = fs.synth.sim_param_for(truth, n, n_phases=n_phases, n_bands=n_bands)
+    f32 = oracle.recon_raw(sp, raw, fade=10)
+    f64 = oracle.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+    err = float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64))
+    print("oracle float vs FP64 at %d^2, %d phases, %d bands: rel-L2 %.2e" % (n, n_phases, n_bands, err))
+    assert err < 1e-4
