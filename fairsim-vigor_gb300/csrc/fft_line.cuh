@@ -303,6 +303,97 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2*
   __syncthreads();
 }
 
+// ---- register-chained transform ------------------------------------------------------
+// In this Stockham plan the first stage reads, and the last stage writes, exactly the
+// elements t + i*T of the thread's line (stage input j + r*L/R with j = t + b*T is element
+// t + T*(b + r*E/R); the last stage writes base + r*L/R with base = j). So a line can enter
+// and leave the transform in registers, x[i] = element t + i*T, and chained transforms
+// with pointwise products in between skip the shared-memory round trip at both ends:
+// 2(S-1) shared-memory passes for S stages instead of 2(S+1), and 2(S-1) barriers.
+// The caller must not be using `s` when the transform starts (the first stage writes it);
+// `s` is free again when it returns.
+template <int L, int T, int C, int R, int NS, bool INV, bool FIRST, bool LAST>
+__device__ __forceinline__ void fft_stage_reg(float2 (&x)[L / T], float2* s, int c, int t, const float2* tw) {
+  constexpr int E = L / T, NB = E / R, LR = L / R;
+  constexpr int NT = NS > 1 ? (R == 16 ? 3 : (R >= 8 || R == 3 ? 2 : 1)) : 1;
+  float2 tl[NB][NT];
+  if constexpr (NS > 1) {
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+      const int k = (t + b * T) % NS;
+      tl[b][0] = tw[k];
+      if constexpr (R == 3) tl[b][1] = tw[NS + k];
+      if constexpr (R >= 8) tl[b][1] = tw[3 * NS + k];
+      if constexpr (R == 16) tl[b][2] = tw[7 * NS + k];
+    }
+  }
+  float2 v[NB][R];
+#pragma unroll
+  for (int b = 0; b < NB; b++)
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      if constexpr (FIRST) v[b][r] = x[b + NB * r];
+      else v[b][r] = s[sidx((t + b * T + r * LR) * C + c)];
+    }
+  if constexpr (!FIRST) __syncthreads();
+#pragma unroll
+  for (int b = 0; b < NB; b++) {
+    const int j = t + b * T;
+    const int k = j % NS;
+    if constexpr (NS > 1) {
+      float2 w[R];
+      w[1] = tl[b][0];
+      if constexpr (R == 3) w[2] = tl[b][1];
+      if constexpr (R == 4) {
+        w[2] = cmul(w[1], w[1]);
+        w[3] = cmul(w[2], w[1]);
+      }
+      if constexpr (R >= 8) {
+        w[4] = tl[b][1];
+        w[2] = cmul(w[1], w[1]);
+        w[3] = cmul(w[2], w[1]);
+#pragma unroll
+        for (int r = 5; r < 8; r++) w[r] = cmul(w[4], w[r - 4]);
+      }
+      if constexpr (R == 16) {
+        w[8] = tl[b][2];
+#pragma unroll
+        for (int r = 9; r < 16; r++) w[r] = cmul(w[8], w[r - 8]);
+      }
+#pragma unroll
+      for (int r = 1; r < R; r++) {
+        float2 ww = w[r];
+        if (INV) ww.y = -ww.y;
+        v[b][r] = cmul(v[b][r], ww);
+      }
+    }
+    dft<R, INV>(v[b]);
+    if constexpr (LAST) {
+#pragma unroll
+      for (int r = 0; r < R; r++) x[b + NB * r] = v[b][r];
+    } else {
+      const int base = (j / NS) * NS * R + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) s[sidx((base + r * NS) * C + c)] = v[b][r];
+    }
+  }
+  if constexpr (!LAST) __syncthreads();
+}
+template <int L, int T, int C, bool INV, int NS>
+__device__ __forceinline__ void fft_stages_reg(float2 (&x)[L / T], float2* s, int c, int t, const float2* tw) {
+  constexpr int R = pick_radix(L / NS, L / T);
+  static_assert((L / NS) % R == 0 && (L / T) % R == 0, "bad radix plan");
+  fft_stage_reg<L, T, C, R, NS, INV, NS == 1, NS * R == L>(x, s, c, t, tw);
+  if constexpr (NS * R < L) fft_stages_reg<L, T, C, INV, NS * R>(x, s, c, t, tw + (R - 1) * NS);
+}
+// Transform line c of C interleaved lines held in registers (x[i] = element t + i*T),
+// with `s` (C interleaved lines, shared memory) as scratch; stage tables (g_stw layout).
+template <int L, int T, int C, bool INV>
+__device__ __forceinline__ void line_fft_reg(float2 (&x)[L / T], float2* s, int c, int t, const float2* stw) {
+  static_assert(supported_len(L) && plan_ok(L, T) && stw_ok(L, L / T), "no stage table for this plan");
+  fft_stages_reg<L, T, C, INV, 1>(x, s, c, t, stw);
+}
+
 template <int L, int T, int C, bool INV, int NS, int TS, int M = 1>
 __device__ __forceinline__ void fft_stages(float2* s, int c, int t, const float2* tw) {
   if constexpr (NS < L) {

@@ -63,7 +63,7 @@ __device__ __forceinline__ int paste_src(int X) {
 // 64-thread row blocks of 8 elements, 64 for longer rows at 8 elements, 96 at 12 elements.
 template <int T, int EN>
 __host__ __device__ constexpr int pass_a_min_blocks() {
-  return EN <= 8 ? (T == 64 ? 20 : (65536 / (T * 64) > 0 ? 65536 / (T * 64) : 1))
+  return EN <= 8 ? (T == 64 ? 16 : (65536 / (T * 64) > 0 ? 65536 / (T * 64) : 1))
                  : (EN == 12 ? (65536 / (T * 96) > 0 ? 65536 / (T * 96) : 1) : 1);
 }
 // The column passes: 64 registers per thread at 8 elements, 80 at 12.
@@ -112,84 +112,80 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   };
   // Components: band 0, then per band b the pair neg = 2b-1, pos = 2b. The separation
   // coefficients of a pair are complex conjugates, so z_pos = conj(z_neg): the pos
-  // component's row transform follows from the neg one's (below). The row is read once
-  // for band 0 (into bh) and the first pair's neg component (into bz, idle during band 0).
+  // component's row transform follows from the neg one's (below). A line stays in
+  // registers from one transform to the next (x[i] = element t + i*T), bz and bh serve as
+  // scratch.
+  float2 x[EN], zk[EN];  // zk: the first pair's neg component, kept for the even-sample product
 #pragma unroll
   for (int i = 0; i < EN; i++) {
-    const int x = t + i * T;
+    const int xx = t + i * T;
     float2 z0 = make_float2(0.f, 0.f), zn = make_float2(0.f, 0.f);
     for (int p = 0; p < nP; p++) {
-      const float v = raw_at(p, x);
-      const float2 m0 = coef[p], mn = coef[(nC > 1 ? nP : 0) + p];
+      const float v = raw_at(p, xx);
+      const float2 m0 = coef[p], mn = coef[nP + p];
       z0.x += m0.x * v;
       z0.y += m0.y * v;
       zn.x += mn.x * v;
       zn.y += mn.y * v;
     }
-    bh[sidx(x)] = z0;
-    bz[sidx(x)] = zn;
+    x[i] = z0;
+    zk[i] = zn;
   }
-  for (int b = 0; b < (nC + 1) / 2; b++) {
-    if (b == 1) {
+  // band 0: Z0 = FFT_N(z0), pasteFreq only; keep the OTF-support window in quad layout
+  line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
 #pragma unroll
-      for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = bz[sidx(t + i * T)];
-    } else if (b > 1) {
-#pragma unroll
-      for (int i = 0; i < EN; i++) {
-        const int x = t + i * T;
-        const float2 z = mix(2 * b - 1, x);
-        bz[sidx(x)] = z;
-        bh[sidx(x)] = z;
-      }
+  for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
+  __syncthreads();
+  {
+    const int Xs = J.win[2 * (a * nC)];
+    float2* I = J.I + (size_t)(a * nS) * J.nWin * N;
+    for (int xl = t; xl < J.nWin; xl += T) {
+      int X = Xs + xl;
+      if (X >= W) X -= W;
+      const int m = paste_src<N>(X);
+      I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = m >= 0 ? bh[sidx(m)] : make_float2(0.f, 0.f);
     }
-    __syncthreads();
-    line_fft_st<N, T, 1, false>(bh, t, twN);  // Z = FFT_N(z)
-    if (b == 0) {
-      // band 0: pasteFreq only; keep the OTF-support window in quad layout
-      const int Xs = J.win[2 * (a * nC)];
-      float2* I = J.I + (size_t)(a * nS) * J.nWin * N;
-      for (int xl = t; xl < J.nWin; xl += T) {
-        int X = Xs + xl;
-        if (X >= W) X -= W;
-        const int m = paste_src<N>(X);
-        I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = m >= 0 ? bh[sidx(m)] : make_float2(0.f, 0.f);
-      }
-      __syncthreads();
-      continue;
-    }
-    // pair (neg, pos): only the neg component is transformed and stored. With
-    // z_pos = conj(z_neg) and opposite shifts (ro_pos = conj(ro_neg), re_pos = conj(re_neg)):
-    //   E_pos[m] = conj(E_neg[-m]),
-    //   O_pos[m] = conj(O_neg[-m]) + d * Q[m],  d = -2i conj(Z_neg[N/2]),
-    // where the d term is the pasted Nyquist bin, whose half-sample phase s(N/2) = -i is
-    // not conjugate-symmetric, and Q = FFT_N((-1)^n ro_pos[n]) is a plan table. So the pos
-    // row spectrum is conj(F_neg[-X]) + exp(-2 pi i X/W) Q[X mod N] d: the column pass
-    // forms it from the neg windows (mirror images of the pos windows) and d, kept here.
+  }
+  // pair (neg, pos): only the neg component is transformed and stored. With
+  // z_pos = conj(z_neg) and opposite shifts (ro_pos = conj(ro_neg), re_pos = conj(re_neg)):
+  //   E_pos[m] = conj(E_neg[-m]),
+  //   O_pos[m] = conj(O_neg[-m]) + d * Q[m],  d = -2i conj(Z_neg[N/2]),
+  // where the d term is the pasted Nyquist bin, whose half-sample phase s(N/2) = -i is
+  // not conjugate-symmetric, and Q = FFT_N((-1)^n ro_pos[n]) is a plan table. So the pos
+  // row spectrum is conj(F_neg[-X]) + exp(-2 pi i X/W) Q[X mod N] d: the column pass
+  // forms it from the neg windows (mirror images of the pos windows) and d, kept here.
+  for (int b = 1; b <= nPair; b++) {
     const int cn = 2 * b - 1;
+    if (b > 1) {
+#pragma unroll
+      for (int i = 0; i < EN; i++) zk[i] = mix(cn, t + i * T);
+    }
+#pragma unroll
+    for (int i = 0; i < EN; i++) x[i] = zk[i];
+    __syncthreads();  // the previous window reads of bh and bz are done
+    line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);  // Z = FFT_N(z)
     if (t == (N / 2) % T) {
-      const float2 zn = bh[sidx(N / 2)];
+      const float2 zn = x[(N / 2) / T];
       J.D[(size_t)(a * nPair + (b - 1)) * N + y] = make_float2(-2.f * zn.y, -2.f * zn.x);
     }
-    // odd samples of the upsampled line: iFFT_N(Z * s)
-#pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int m = t + i * T;
-      bh[sidx(m)] = cmul(bh[sidx(m)], half_shift<N>(twW, m));
-    }
-    __syncthreads();
-    line_fft_st<N, T, 1, true>(bh, t, twN);
-    // times the even/odd ramp samples, forward transforms
     const float2* re = J.ramps + (size_t)(a * nC + cn) * 2 * W;
     const float2* ro = re + N;
+    // odd samples of the upsampled line, iFFT_N(Z * s), times the odd-sample ramp, FFT: O
 #pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int m = t + i * T;
-      bz[sidx(m)] = cmul(bz[sidx(m)], __ldg(re + m));
-      bh[sidx(m)] = cmul(bh[sidx(m)], __ldg(ro + m));
-    }
+    for (int i = 0; i < EN; i++) x[i] = cmul(x[i], half_shift<N>(twW, t + i * T));
+    line_fft_reg<N, T, 1, true>(x, bh, 0, t, twN);
+#pragma unroll
+    for (int i = 0; i < EN; i++) x[i] = cmul(x[i], __ldg(ro + t + i * T));
+    line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
+#pragma unroll
+    for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
+    // even samples times the even-sample ramp, FFT: E
+#pragma unroll
+    for (int i = 0; i < EN; i++) zk[i] = cmul(zk[i], __ldg(re + t + i * T));
+    line_fft_reg<N, T, 1, false>(zk, bz, 0, t, twN);
+#pragma unroll
+    for (int i = 0; i < EN; i++) bz[sidx(t + i * T)] = zk[i];
     __syncthreads();
-    line_fft_st<N, T, 1, false>(bz, t, twN);
-    line_fft_st<N, T, 1, false>(bh, t, twN);
     // neg window of the shifted spectrum: E[X mod N] + exp(-2 pi i X/W) O[X mod N]
     const int Xs = J.win[2 * (a * nC + cn)];
     float2* I = J.I + (size_t)(a * nS + b) * J.nWin * N;
@@ -197,10 +193,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
       int X = Xs + xl;
       if (X >= W) X -= W;
       const int m = X < N ? X : X - N;
-      const float2 e = bz[sidx(m)], o = bh[sidx(m)];
-      I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(e, cmul(twW[X], o));
+      I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(bz[sidx(m)], cmul(twW[X], bh[sidx(m)]));
     }
-    __syncthreads();
   }
 }
 
