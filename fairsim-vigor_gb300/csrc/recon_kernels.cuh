@@ -441,23 +441,23 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   // Wiener denominator x apodization, then iFFT_W along y as two N-point inverse FFTs:
   //   out[2n] = iFFT_N(A[k] + A[k+N]),  out[2n+1] = iFFT_N((A[k] - A[k+N]) exp(i pi k/N))
   const float* wa = J.wa + (size_t)(X >> 2) * W * 4 + (X & 3);
+  float2 xe[EN], xo[EN];  // even and odd output rows, in registers through the transforms
 #pragma unroll
   for (int i = 0; i < EN; i++) {
     const int k = t + i * T;
     const float f0 = __ldg(wa + (size_t)k * 4), f1 = __ldg(wa + (size_t)(k + N) * 4);
     const float2 u0 = make_float2(acc[i].x * f0, acc[i].y * f0);
     const float2 u1 = make_float2(acc[i + EN].x * f1, acc[i + EN].y * f1);
-    bz[sidx(k * CB + lane)] = cadd(u0, u1);
-    bh[sidx(k * CB + lane)] = cmul(csub(u0, u1), cconjf(twW[k]));
+    xe[i] = cadd(u0, u1);
+    xo[i] = cmul(csub(u0, u1), cconjf(twW[k]));
   }
-  __syncthreads();
-  line_fft_st<N, T, CB, true>(bz, lt, twN);
-  line_fft_st<N, T, CB, true>(bh, lt, twN);
+  line_fft_reg<N, T, CB, true>(xe, bz, lane, t, twN);
+  line_fft_reg<N, T, CB, true>(xo, bh, lane, t, twN);
 #pragma unroll
   for (int i = 0; i < EN; i++) {
     const int k = t + i * T;
-    J.O[(size_t)(2 * k) * W + X] = bz[sidx(k * CB + lane)];
-    J.O[(size_t)(2 * k + 1) * W + X] = bh[sidx(k * CB + lane)];
+    J.O[(size_t)(2 * k) * W + X] = xe[i];
+    J.O[(size_t)(2 * k + 1) * W + X] = xo[i];
   }
 }
 
@@ -474,14 +474,15 @@ __global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::TC) k_pass_c(const JobDesc
   stage_stage_twiddles<W, EW>(tw, threadIdx.x, G * T);
   float2* s = sm + g * smem_line_elems(W, 1);
   const float2* row = J.O + (size_t)Y * W;
+  float2 x[EW];  // element t + i*T of the row, in registers through the transform
 #pragma unroll
-  for (int i = 0; i < EW; i++) s[sidx(t + i * T)] = row[t + i * T];
-  __syncthreads();
-  line_fft_st<W, T, 1, true>(s, t, tw);
+  for (int i = 0; i < EW; i++) x[i] = row[t + i * T];
+  __syncthreads();  // the twiddle table is staged
+  line_fft_reg<W, T, 1, true>(x, s, 0, t, tw);
   const float scale = 1.f / ((float)W * (float)W);
   float* out = J.out + (size_t)Y * W;
 #pragma unroll
-  for (int i = 0; i < EW; i++) out[t + i * T] = s[sidx(t + i * T)].x * scale;
+  for (int i = 0; i < EW; i++) out[t + i * T] = x[i].x * scale;
 }
 
 // ---- launch ----------------------------------------------------------------------------------------
