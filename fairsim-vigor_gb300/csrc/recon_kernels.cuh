@@ -279,6 +279,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   const int xl = blockIdx.x * CB + lane;  // nWin is a multiple of 4: every lane is inside
   const size_t quad = ((size_t)(xl >> 2) * N) * 4 + (xl & 3);
   float2* out = J.Tw + (size_t)comp * nWin * nWin + ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3);
+  float2 x[EN];  // element t + i*T of this lane's column, in registers through the transforms
   if (comp == 0) {
 #pragma unroll
     for (int i = 0; i < EN; i++) {
@@ -289,10 +290,12 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
         v.x += u.x;
         v.y += u.y;
       }
-      bh[sidx(k * CB + lane)] = v;
+      x[i] = v;
     }
+    line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);
+#pragma unroll
+    for (int i = 0; i < EN; i++) bh[sidx((t + i * T) * CB + lane)] = x[i];
     __syncthreads();
-    line_fft_st<N, T, CB, false>(bh, lt, twN);
     const int Ys = J.win[1];
     for (int yl = t; yl < nWin; yl += T) {
       int Y = Ys + yl;
@@ -305,36 +308,30 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   const int a = (comp - 1) / nPair, b = 1 + (comp - 1) % nPair, cn = 2 * b - 1;
   const float2* I = J.I + (size_t)(a * nS + b) * nWin * N + quad;
 #pragma unroll
-  for (int i = 0; i < EN; i++) {
-    const int k = t + i * T;
-    const float2 v = I[(size_t)k * 4];
-    bz[sidx(k * CB + lane)] = v;
-    bh[sidx(k * CB + lane)] = v;
-  }
-  __syncthreads();
-  line_fft_st<N, T, CB, false>(bh, lt, twN);  // Z along y
+  for (int i = 0; i < EN; i++) x[i] = I[(size_t)(t + i * T) * 4];
+  line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);  // Z along y
   if (t == (N / 2) % T) {
-    const float2 z = bh[sidx((N / 2) * CB + lane)];
+    const float2 z = x[(N / 2) / T];
     J.Dy[(size_t)(comp - 1) * nWin + xl] = make_float2(-2.f * z.y, -2.f * z.x);
   }
-#pragma unroll
-  for (int i = 0; i < EN; i++) {
-    const int m = t + i * T;
-    bh[sidx(m * CB + lane)] = cmul(bh[sidx(m * CB + lane)], half_shift<N>(twW, m));
-  }
-  __syncthreads();
-  line_fft_st<N, T, CB, true>(bh, lt, twN);
   const float2* re = J.ramps + (size_t)(a * nC + cn) * 2 * W + W;  // y ramps
   const float2* ro = re + N;
+  // odd samples, iFFT_N(Z * s), times the odd-sample ramp, FFT: O
 #pragma unroll
-  for (int i = 0; i < EN; i++) {
-    const int m = t + i * T;
-    bz[sidx(m * CB + lane)] = cmul(bz[sidx(m * CB + lane)], __ldg(re + m));
-    bh[sidx(m * CB + lane)] = cmul(bh[sidx(m * CB + lane)], __ldg(ro + m));
-  }
+  for (int i = 0; i < EN; i++) x[i] = cmul(x[i], half_shift<N>(twW, t + i * T));
+  line_fft_reg<N, T, CB, true>(x, bh, lane, t, twN);
+#pragma unroll
+  for (int i = 0; i < EN; i++) x[i] = cmul(x[i], __ldg(ro + t + i * T));
+  line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);
+#pragma unroll
+  for (int i = 0; i < EN; i++) bh[sidx((t + i * T) * CB + lane)] = x[i];
+  // even samples (the column again, from L2) times the even-sample ramp, FFT: E
+#pragma unroll
+  for (int i = 0; i < EN; i++) x[i] = cmul(I[(size_t)(t + i * T) * 4], __ldg(re + t + i * T));
+  line_fft_reg<N, T, CB, false>(x, bz, lane, t, twN);
+#pragma unroll
+  for (int i = 0; i < EN; i++) bz[sidx((t + i * T) * CB + lane)] = x[i];
   __syncthreads();
-  line_fft_st<N, T, CB, false>(bz, lt, twN);
-  line_fft_st<N, T, CB, false>(bh, lt, twN);
   const int Yn = J.win[2 * (a * nC + cn) + 1];
   for (int yl = t; yl < nWin; yl += T) {
     int Y = Yn + yl;
