@@ -5,7 +5,7 @@
 //           every global access moves C*8 contiguous bytes (64 B for C = 8).
 // Each pass reads and writes the array once (16 bytes per complex element per pass).
 // Twiddles come from the per-stage tables (one to three loads per butterfly, the other
-// powers by products), read through L1.
+// powers by products), read through L1; lines enter and leave the transform in registers.
 #include "common.cuh"
 #include "fft_line.cuh"
 #include "runtime.cuh"
@@ -30,15 +30,13 @@ __global__ void __launch_bounds__(256) k_fft_rows(float2* __restrict__ data, int
   const int row = blockIdx.x * G + g;
   float2* s = sm + g * SL;
   float2* base = data + blockIdx.y * item_stride + (size_t)row * L;
+  float2 x[E];  // element t + i*T of the row: in and out of the transform in registers
+#pragma unroll
+  for (int i = 0; i < E; i++) x[i] = row < nrows ? base[t + i * T] : make_float2(0.f, 0.f);
+  line_fft_reg<L, T, 1, INV>(x, s, 0, t, g_stw + stw_offset(L, E));
   if (row < nrows) {
 #pragma unroll
-    for (int i = 0; i < E; i++) s[sidx(t + i * T)] = base[t + i * T];
-  }
-  __syncthreads();
-  line_fft_st<L, T, 1, INV>(s, t, g_stw + stw_offset(L, E));
-  if (row < nrows) {
-#pragma unroll
-    for (int i = 0; i < E; i++) base[t + i * T] = cscale(s[sidx(t + i * T)], scale);
+    for (int i = 0; i < E; i++) base[t + i * T] = cscale(x[i], scale);
   }
 }
 
@@ -50,19 +48,13 @@ __global__ void k_fft_cols(float2* __restrict__ data, int ncols, size_t item_str
   const int c = threadIdx.x % C, t = threadIdx.x / C;
   const int x = blockIdx.x * C + c;
   float2* base = data + blockIdx.y * item_stride;
+  float2 v[E];  // element t + i*T of the column: in and out of the transform in registers
 #pragma unroll
-  for (int i = 0; i < E; i++) {
-    int k = t + i * T;
-    s[sidx(k * C + c)] = (x < ncols) ? base[(size_t)k * ncols + x] : make_float2(0.f, 0.f);
-  }
-  __syncthreads();
-  line_fft_st<L, T, C, INV>(s, threadIdx.x, g_stw + stw_offset(L, E));
+  for (int i = 0; i < E; i++) v[i] = (x < ncols) ? base[(size_t)(t + i * T) * ncols + x] : make_float2(0.f, 0.f);
+  line_fft_reg<L, T, C, INV>(v, s, c, t, g_stw + stw_offset(L, E));
   if (x < ncols) {
 #pragma unroll
-    for (int i = 0; i < E; i++) {
-      int k = t + i * T;
-      base[(size_t)k * ncols + x] = cscale(s[sidx(k * C + c)], scale);
-    }
+    for (int i = 0; i < E; i++) base[(size_t)(t + i * T) * ncols + x] = cscale(v[i], scale);
   }
 }
 

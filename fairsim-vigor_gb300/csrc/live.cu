@@ -89,9 +89,11 @@ __global__ void __launch_bounds__(LCfg<N>::GA* LCfg<N>::TN) k_live_a(const JobDe
       J.widefield[row + x] = __fmul_rn(wf, sc);
     }
   }
+  __syncthreads();  // the twiddle table is staged
   for (int a = 0; a < nA; a++)
     for (int c = 0; c < nC; c++) {
       const float2* coef = J.coef + (a * nC + c) * nP;
+      float2 xv[E];  // element t + i*T of the line, in registers through the transform
 #pragma unroll
       for (int i = 0; i < E; i++) {
         const int x = t + i * T;
@@ -102,14 +104,12 @@ __global__ void __launch_bounds__(LCfg<N>::GA* LCfg<N>::TN) k_live_a(const JobDe
           z.x += m.x * v;
           z.y += m.y * v;
         }
-        s[sidx(x)] = z;
+        xv[i] = z;
       }
-      __syncthreads();
-      line_fft_st<N, T, 1, false>(s, t, tw);
+      line_fft_reg<N, T, 1, false>(xv, s, 0, t, tw);
       float2* X = J.I + (size_t)(a * nC + c) * frame + row;
 #pragma unroll
-      for (int i = 0; i < E; i++) X[t + i * T] = s[sidx(t + i * T)];
-      __syncthreads();
+      for (int i = 0; i < E; i++) X[t + i * T] = xv[i];
     }
 }
 
@@ -126,42 +126,29 @@ __global__ void __launch_bounds__(LCfg<N>::CBL* LCfg<N>::TN, live_min_blocks(LCf
   __shared__ float2 tw[stw_len(N, E)];
   stage_stage_twiddles<N, E>(tw, lt, C * T);
   const size_t frame = (size_t)N * N;
+  __syncthreads();  // the twiddle table is staged
   for (int a = 0; a < J.nA; a++)
     for (int c = 0; c < J.nC; c++) {
       float2* X = J.I + (size_t)(a * J.nC + c) * frame;
+      float2 v[E];  // element t + i*T of this lane's column, in registers through the transforms
 #pragma unroll
-      for (int i = 0; i < E; i++) {
-        const int k = t + i * T;
-        s[sidx(k * C + lane)] = X[(size_t)k * N + x];
-      }
-      __syncthreads();
-      line_fft_st<N, T, C, false>(s, lt, tw);
+      for (int i = 0; i < E; i++) v[i] = X[(size_t)(t + i * T) * N + x];
+      line_fft_reg<N, T, C, false>(v, s, lane, t, tw);
       // times conj(OTF): the OTF vector is real (estimate), conj(OTF)*v = (v.re*o, v.im*o)
 #pragma unroll
       for (int i = 0; i < E; i++) {
-        const int k = t + i * T;
-        const float o = __ldg(&J.masks[(size_t)k * N + x]);
-        float2& v = s[sidx(k * C + lane)];
-        v = make_float2(__fmul_rn(v.x, o), __fmul_rn(v.y, o));
+        const float o = __ldg(&J.masks[(size_t)(t + i * T) * N + x]);
+        v[i] = make_float2(__fmul_rn(v[i].x, o), __fmul_rn(v[i].y, o));
       }
-      __syncthreads();
       if (c > 0) {
-        line_fft_st<N, T, C, true>(s, lt, tw);
+        line_fft_reg<N, T, C, true>(v, s, lane, t, tw);
         const float2* ry = J.ramps + (size_t)(a * J.nC + c) * 2 * N + N;
 #pragma unroll
-        for (int i = 0; i < E; i++) {
-          const int k = t + i * T;
-          s[sidx(k * C + lane)] = cmul(s[sidx(k * C + lane)], __ldg(&ry[k]));
-        }
-        __syncthreads();
-        line_fft_st<N, T, C, false>(s, lt, tw);
+        for (int i = 0; i < E; i++) v[i] = cmul(v[i], __ldg(&ry[t + i * T]));
+        line_fft_reg<N, T, C, false>(v, s, lane, t, tw);
       }
 #pragma unroll
-      for (int i = 0; i < E; i++) {
-        const int k = t + i * T;
-        X[(size_t)k * N + x] = s[sidx(k * C + lane)];
-      }
-      __syncthreads();
+      for (int i = 0; i < E; i++) X[(size_t)(t + i * T) * N + x] = v[i];
     }
 }
 
@@ -186,20 +173,20 @@ __global__ void __launch_bounds__(LCfg<N>::TW, live_min_blocks(LCfg<N>::TW)) k_l
       const int ys = paste_source(Y, yInt, N, W);
       if (ys < 0) continue;  // uniform per block
       const float2* X = J.I + (size_t)(a * J.nC + c) * frame + (size_t)ys * N;
+      float2 v[EN];  // element t + i*TW of the row, in registers through the transforms
 #pragma unroll
-      for (int i = 0; i < EN; i++) s[sidx(t + i * TW)] = X[t + i * TW];
-      __syncthreads();
+      for (int i = 0; i < EN; i++) v[i] = X[t + i * TW];
+      __syncthreads();  // the twiddle tables are staged; the previous paste has read s
       if (c > 0) {
-        line_fft_st<N, TW, 1, true>(s, t, twN);
+        line_fft_reg<N, TW, 1, true>(v, s, 0, t, twN);
         const float2* rx = J.ramps + (size_t)(a * J.nC + c) * 2 * N;
 #pragma unroll
-        for (int i = 0; i < EN; i++) {
-          const int k = t + i * TW;
-          s[sidx(k)] = cmul(s[sidx(k)], __ldg(&rx[k]));
-        }
-        __syncthreads();
-        line_fft_st<N, TW, 1, false>(s, t, twN);
+        for (int i = 0; i < EN; i++) v[i] = cmul(v[i], __ldg(&rx[t + i * TW]));
+        line_fft_reg<N, TW, 1, false>(v, s, 0, t, twN);
       }
+#pragma unroll
+      for (int i = 0; i < EN; i++) s[sidx(t + i * TW)] = v[i];
+      __syncthreads();
       // pasteFreq at (xInt, yInt) and fullResult.add
 #pragma unroll
       for (int i = 0; i < EW; i++) {
@@ -214,18 +201,19 @@ __global__ void __launch_bounds__(LCfg<N>::TW, live_min_blocks(LCfg<N>::TW)) k_l
       __syncthreads();
     }
   const float* wa = J.wa + (size_t)Y * W;
+  float2 u[EW];
 #pragma unroll
   for (int i = 0; i < EW; i++) {
     const int k = t + i * TW;
     const float f = __ldg(&wa[k]);
-    float2& o = acc[sidx(k)];
-    o = make_float2(o.x * f, o.y * f);
+    const float2 o = acc[sidx(k)];
+    u[i] = make_float2(o.x * f, o.y * f);
   }
-  __syncthreads();
-  line_fft_st<W, TW, 1, true>(acc, t, twW);
+  __syncthreads();  // acc is read: it becomes the transform's scratch
+  line_fft_reg<W, TW, 1, true>(u, acc, 0, t, twW);
   float2* O = J.O + (size_t)Y * W;
 #pragma unroll
-  for (int i = 0; i < EW; i++) O[t + i * TW] = acc[sidx(t + i * TW)];
+  for (int i = 0; i < EW; i++) O[t + i * TW] = u[i];
 }
 
 // ---- LD -----------------------------------------------------------------------------------
@@ -239,19 +227,14 @@ __global__ void __launch_bounds__(LCfg<N>::CD* LCfg<N>::TW) k_live_d(const JobDe
   extern __shared__ float2 s[];
   __shared__ float2 tw[stw_len(W, EW)];
   stage_stage_twiddles<W, EW>(tw, lt, C * TW);
+  float2 v[EW];  // element t + i*TW of the column, in registers through the transform
 #pragma unroll
-  for (int i = 0; i < EW; i++) {
-    const int k = t + i * TW;
-    s[sidx(k * C + lane)] = J.O[(size_t)k * W + X];
-  }
-  __syncthreads();
-  line_fft_st<W, TW, C, true>(s, lt, tw);
+  for (int i = 0; i < EW; i++) v[i] = J.O[(size_t)(t + i * TW) * W + X];
+  __syncthreads();  // the twiddle table is staged
+  line_fft_reg<W, TW, C, true>(v, s, lane, t, tw);
   const float scale = 1.f / ((float)W * (float)W);
 #pragma unroll
-  for (int i = 0; i < EW; i++) {
-    const int k = t + i * TW;
-    J.out[(size_t)k * W + X] = s[sidx(k * C + lane)].x * scale;
-  }
+  for (int i = 0; i < EW; i++) J.out[(size_t)(t + i * TW) * W + X] = v[i].x * scale;
 }
 
 // ---- plan tables ----------------------------------------------------------------------------
