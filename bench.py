@@ -216,7 +216,7 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--distinct", type=int, default=16)
     ap.add_argument("--no-extras", action="store_true", help="skip plain-GPU, serve, mixed, large and CPU legs")
-    ap.add_argument("--only", choices=["live", "fft", "estimate", "mixed", "large", "serve"],
+    ap.add_argument("--only", choices=["live", "fft", "estimate", "mixed", "large", "serve", "widefield"],
                     help="run one extra leg alone and print its JSON (profiling of its kernels)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -365,6 +365,7 @@ def main():
                                                          / extras["plain_gpu"]["value"])
         extras["mixed_batch"] = mixed_leg(fs, torch, stream, timed)
         extras["live_batch"] = live_leg(fs, torch, stream, timed)
+        extras["widefield_outputs"] = widefield_leg(fs, torch, stream, timed)
         extras["large_3x5_2048"] = large_leg(fs, torch, stream, timed)
         extras["estimate_1024"] = estimate_leg(fs, torch)
         extras["fft2d_vs_cufft"] = [fft_leg(fs, torch, stream, timed, n, b) for n, b in ((512, 64), (1024, 16))]
@@ -434,6 +435,8 @@ def run_only(args):
         res = mixed_leg(fs, torch, stream, timed, steps=args.steps)
     elif args.only == "large":
         res = large_leg(fs, torch, stream, timed, steps=args.steps)
+    elif args.only == "widefield":
+        res = widefield_leg(fs, torch, stream, timed, batch=args.batch, steps=args.steps)
     else:
         res = {"poisson": serve_leg(fs), "saturated": serve_capacity_leg(fs)}
     print(json.dumps({args.only: res}))
@@ -512,6 +515,38 @@ def mixed_leg(fs, torch, stream, timed, n_datasets=64, steps=5, seed=77):
            "raw_MB_per_batch": sum(r.numel() * 4 for r in raws) / 1e6}
     for p in plans:
         p.close()
+    return res
+
+
+def widefield_leg(fs, torch, stream, timed, batch=64, steps=10, n=512, seed=88):
+    """The offline batch of the headline (64 x 512^2 3x3 stacks) with and without the two
+    widefield side outputs (runReconstruction's "Widefield" and "filtered Widefield",
+    2w x 2w each): the added time per batch, and the widefield passes' algorithmic bytes
+    (raw read + band-0 rows + filter + column outputs + images, per dataset) over that time."""
+    N_ = fs.native
+    raw, truth = fs.synth.make_dataset(n=n, seed=seed)
+    sp = fs.synth.sim_param_for(truth, n)
+    plan = fs.plan.ReconPlan(sp, path=N_.PATH_OFFLINE, input_type=N_.INPUT_F32, fade_px=10)
+    d_raw = [torch.from_numpy(raw).cuda() for _ in range(batch)]
+    img = lambda: torch.empty((2 * n, 2 * n), dtype=torch.float32, device="cuda")  # noqa: E731
+    d_out, d_wf, d_fwf = [img() for _ in range(batch)], [img() for _ in range(batch)], [img() for _ in range(batch)]
+    ws = torch.empty(fs.plan.batch_workspace_bytes([plan] * batch), dtype=torch.uint8, device="cuda")
+    res = {}
+    for key, with_wf in (("without", False), ("with", True)):
+        jobs = [(plan, r.data_ptr(), o.data_ptr()) + ((w.data_ptr(), f.data_ptr()) if with_wf else ())
+                for r, o, w, f in zip(d_raw, d_out, d_wf, d_fwf)]
+        g = fs.plan.BatchGraph(jobs, ws.data_ptr(), ws.numel(), stream.cuda_stream)
+        for _ in range(3):
+            g.launch(stream.cuda_stream)
+        ms = timed(lambda: g.launch(stream.cuda_stream), steps) / steps
+        res[key] = {"ms_per_batch": ms, "recon_per_s": batch / (ms / 1000.0), "kernels": g.info()["kernels"]}
+        g.close()
+    nf = NA * NP
+    wf_bytes = (nf * 4 * n * n + 8 * n * n) + (8 * n * n + 4 * n * n + 2 * 16 * n * n) + 2 * (16 * n * n + 16 * n * n)
+    added = res["with"]["ms_per_batch"] - res["without"]["ms_per_batch"]
+    res.update({"added_ms_per_batch": added, "algorithmic_MB_per_dataset": wf_bytes / 1e6,
+                "widefield_GB_per_s": wf_bytes * batch / (added / 1000.0) / 1e9 if added > 0 else None})
+    plan.close()
     return res
 
 

@@ -25,7 +25,7 @@ namespace fsim {
 namespace {
 
 struct Slot {
-  char* dev = nullptr;  // raw | out | widefield | workspace
+  char* dev = nullptr;  // raw | out | widefields | workspace
   size_t bytes = 0;
   JobDesc* table = nullptr;  // pinned job table of the chunk in this slot
   int table_cap = 0;
@@ -47,15 +47,18 @@ size_t raw_bytes(const Plan* p) {
   return (size_t)p->prm.w * p->prm.w * p->prm.nr_dirs * p->prm.nr_phases * (p->input_type == FSIM_INPUT_U16 ? 2 : 4);
 }
 size_t out_bytes(const Plan* p) { return (size_t)4 * p->prm.w * p->prm.w * sizeof(float); }
-size_t wf_bytes(const Plan* p) { return (size_t)p->prm.w * p->prm.w * sizeof(float); }
+// widefield: w x w on the live path, 2w x 2w (as the output) on the offline path
+size_t wf_bytes(const Plan* p) {
+  return p->path == FSIM_PATH_LIVE ? (size_t)p->prm.w * p->prm.w * sizeof(float) : out_bytes(p);
+}
 
-// device bytes of one chunk: per job raw + out (+ widefield) + workspace, plus the table
+// device bytes of one chunk: per job raw + out (+ widefields) + workspace, plus the table
 size_t chunk_bytes(const fsim_host_job* jobs, int k0, int k1) {
   size_t b = a256(sizeof(JobDesc) * (k1 - k0));
   for (int k = k0; k < k1; k++) {
     const Plan* p = reinterpret_cast<const Plan*>(jobs[k].plan);
     b += a256(raw_bytes(p)) + a256(out_bytes(p)) + (jobs[k].widefield_host ? a256(wf_bytes(p)) : 0) +
-         a256(plan_ws(p));
+         (jobs[k].filtered_widefield_host ? a256(out_bytes(p)) : 0) + a256(plan_ws(p));
   }
   return b;
 }
@@ -84,8 +87,8 @@ extern "C" int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int 
   for (int k = 0; k < n_jobs; k++) {
     const Plan* p = reinterpret_cast<const Plan*>(jobs[k].plan);
     FSIM_REQUIRE(p && jobs[k].raw_host && jobs[k].out_host, FSIM_EINVAL, "host job %d: null plan/raw/out", k);
-    FSIM_REQUIRE(!jobs[k].widefield_host || p->path == FSIM_PATH_LIVE, FSIM_EINVAL,
-                 "host job %d: widefield output needs a live-path plan", k);
+    FSIM_REQUIRE(!jobs[k].filtered_widefield_host || p->path == FSIM_PATH_OFFLINE, FSIM_EINVAL,
+                 "host job %d: the filtered widefield needs an offline-path plan", k);
   }
   int rc = ensure_init();
   if (rc) return rc;
@@ -149,6 +152,11 @@ extern "C" int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int 
         dj[i].widefield = reinterpret_cast<float*>(cur);
         cur += a256(wf_bytes(p));
       }
+      dj[i].filtered_widefield = nullptr;
+      if (h.filtered_widefield_host) {
+        dj[i].filtered_widefield = reinterpret_cast<float*>(cur);
+        cur += a256(out_bytes(p));
+      }
     }
     FSIM_CUDA(cudaEventRecord(S.up, P.s_up));
     FSIM_CUDA(cudaStreamWaitEvent(P.s_comp, S.up, 0));
@@ -167,6 +175,9 @@ extern "C" int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int 
       FSIM_CUDA(cudaMemcpyAsync(h.out_host, dj[i].out, out_bytes(p), cudaMemcpyDeviceToHost, P.s_down));
       if (h.widefield_host)
         FSIM_CUDA(cudaMemcpyAsync(h.widefield_host, dj[i].widefield, wf_bytes(p), cudaMemcpyDeviceToHost, P.s_down));
+      if (h.filtered_widefield_host)
+        FSIM_CUDA(cudaMemcpyAsync(h.filtered_widefield_host, dj[i].filtered_widefield, out_bytes(p),
+                                  cudaMemcpyDeviceToHost, P.s_down));
     }
     FSIM_CUDA(cudaEventRecord(S.down, P.s_down));
     S.used = true;

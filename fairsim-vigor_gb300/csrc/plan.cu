@@ -62,6 +62,10 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
   std::vector<int> order(n);
   for (int i = 0; i < n; i++) {
     FSIM_REQUIRE(jobs[i].plan && jobs[i].raw && jobs[i].out, FSIM_EINVAL, "job %d: null plan/raw/out", i);
+    FSIM_REQUIRE(!jobs[i].filtered_widefield || static_cast<const Plan*>(jobs[i].plan)->path == FSIM_PATH_OFFLINE,
+                 FSIM_EINVAL, "job %d: the filtered widefield needs an offline-path plan", i);
+    FSIM_REQUIRE(((uintptr_t)jobs[i].widefield & 7) == 0 && ((uintptr_t)jobs[i].filtered_widefield & 7) == 0,
+                 FSIM_EINVAL, "job %d: widefield outputs must be 8-byte aligned", i);
     order[i] = i;
   }
   auto key = [&](int i) {
@@ -81,7 +85,7 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
     if (p->path == FSIM_PATH_LIVE)
       p->fill_job_live(host_table[k], jb.raw, jb.out, jb.widefield, cur);
     else
-      p->fill_job(host_table[k], jb.raw, jb.out, jb.widefield, cur);
+      p->fill_job(host_table[k], jb.raw, jb.out, jb.widefield, jb.filtered_widefield, cur);
     cur += align256(plan_ws(p));
   }
   if (upload_table) FSIM_CUDA(cudaMemcpyAsync(d_table, host_table, sizeof(JobDesc) * n, cudaMemcpyHostToDevice, st));
@@ -120,6 +124,11 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
     cudaStream_t s = (nfork > 0 && g > 0) ? aux[(g - 1) % nfork] : st;
     rc = (p0->path == FSIM_PATH_LIVE) ? launch_live_size(p0->prm.w, d_table + k, e - k, maxA, s)
                                       : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxPair, maxWin, s);
+    if (rc == FSIM_OK && p0->path == FSIM_PATH_OFFLINE) {
+      bool wf = false;
+      for (int i = k; i < e; i++) wf = wf || jobs[order[i]].widefield || jobs[order[i]].filtered_widefield;
+      if (wf) rc = launch_widefield_size(p0->prm.w, d_table + k, e - k, s);
+    }
   }
   if (nfork > 0) {
     // join even after a failed launch, so that a capture in progress can still end

@@ -197,7 +197,8 @@ int Plan::build(cudaStream_t st) {
   size_t off_mask = off_damp + al((size_t)N * N * sizeof(float));
   size_t off_wa = off_mask + al((size_t)nA * nC * nwin * nwin * sizeof(float));
   size_t off_nyq = off_wa + al((size_t)W * W * sizeof(float));
-  size_t total = off_nyq + al(nyq.size() * sizeof(float2));
+  size_t off_wff = off_nyq + al(nyq.size() * sizeof(float2));
+  size_t total = off_wff + al((size_t)N * N * sizeof(float));
   if (total > dev_bytes) {
     if (dev) cudaFree(dev);
     dev = nullptr;
@@ -206,6 +207,7 @@ int Plan::build(cudaStream_t st) {
   }
   char* b = (char*)dev;
   d_nyq = (float2*)(b + off_nyq);
+  d_wff = (float*)(b + off_wff);
   d_coef = (float2*)(b + off_coef);
   d_ramps = (float2*)(b + off_ramp);
   d_win = (int*)(b + off_win);
@@ -240,6 +242,10 @@ int Plan::build(cudaStream_t st) {
                                   ht.cutoff * prm.apo_cutoff, prm.apo_bend);
   }
   FSIM_CHECK_LAUNCH();
+  {
+    int rc = build_widefield_filter(d_wff, N, d_otf, (float)(prm.wiener * prm.wiener), st);
+    if (rc) return rc;
+  }
   FSIM_CUDA(cudaStreamSynchronize(st));
   filter_bytes = total;
   return FSIM_OK;
@@ -260,14 +266,17 @@ static void ws_parts(const fsim_sim_param& p, int nwin, size_t part[6]) {
 size_t Plan::workspace_bytes() const {
   size_t part[6];
   ws_parts(prm, nwin, part);
-  return part[0] + part[1] + part[2] + part[3] + part[4] + part[5];
+  return std::max(part[0] + part[1] + part[2] + part[3] + part[4] + part[5], widefield_ws_bytes(prm.w));
 }
 
-void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws) const {
+void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, float* fwf, char* ws) const {
   const int N = prm.w, nC = 2 * prm.nr_bands - 1;
   j.raw = raw;
   j.out = out;
   j.widefield = wf;
+  j.fwf = fwf;
+  j.wff = d_wff;
+  j.Wf = (float2*)ws;
   j.input_u16 = input_type == FSIM_INPUT_U16;
   j.nA = prm.nr_dirs;
   j.nP = prm.nr_phases;

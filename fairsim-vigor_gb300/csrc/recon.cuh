@@ -27,6 +27,10 @@ struct JobDesc {
   float2* Tw;           // workspace: column-transformed windows [band 0, neg of (a, b)][nWin/4][nWin][4] (pass B1)
   float2* Dy;           // workspace: [a][b-1][nWin] Nyquist term d' of every neg window column (pass B1)
   float2* O;            // workspace: W*W after the column pass
+  // widefield side outputs of the offline path (widefield.cu), run after the passes above
+  float* fwf;              // W*W filtered widefield, nullable (widefield: W*W offline, N*N live)
+  const float* wff;        // N*N filter of the filtered widefield (resident, k_build_wff)
+  float2* Wf;              // workspace (reused after pass C): N*N band-0 rows, then 2 x [W][N] columns
 };
 
 struct Plan {
@@ -47,6 +51,7 @@ struct Plan {
   float* d_masks = nullptr;
   float* d_wa = nullptr;
   float2* d_nyq = nullptr;
+  float* d_wff = nullptr;  // filtered-widefield filter, N*N
   // host-call convenience buffers (fsim_recon_host)
   void* h_ws = nullptr;
   size_t h_ws_bytes = 0;
@@ -59,7 +64,7 @@ struct Plan {
   int build_live(cudaStream_t st);  // live tables
   size_t workspace_bytes() const;
   size_t workspace_bytes_live() const;
-  void fill_job(JobDesc& j, const void* raw, float* out, float* wf, char* ws) const;
+  void fill_job(JobDesc& j, const void* raw, float* out, float* wf, float* fwf, char* ws) const;
   void fill_job_live(JobDesc& j, const void* raw, float* out, float* wf, char* ws) const;
 };
 
@@ -77,6 +82,13 @@ bool live_size_supported(int n);
 // of the batch's datasets of size n (they bound the grids; extra blocks exit at once)
 int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st);
 int launch_live_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);
+// widefield and filtered widefield of the offline jobs that ask for them (widefield.cu);
+// launched after launch_offline_size on the same stream (it reuses the job workspaces)
+int launch_widefield_size(int n, const JobDesc* d_jobs, int njobs, cudaStream_t st);
+// workspace bytes the widefield kernels need per job of size n
+size_t widefield_ws_bytes(int n);
+// the plan's filtered-widefield filter (n*n floats), from its device OTF table
+int build_widefield_filter(float* d_wff, int n, const OtfTable* d_otf, float wp, cudaStream_t st);
 
 // Fill the job table of a batch (sorted by path and size) into host_table, optionally copy it
 // to the head of the workspace, and launch every size class's passes. With aux streams, the

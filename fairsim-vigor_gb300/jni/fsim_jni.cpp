@@ -305,6 +305,31 @@ GFN(void, reconstruct)(JNIEnv* env, jclass, jlong plan, jarray raw, jfloatArray 
   if (r) env->ReleasePrimitiveArrayCritical(raw, r, JNI_ABORT);
   throw_status(env, rc);
 }
+// the reconstruction with runReconstruction's "Widefield" and "filtered Widefield" images
+// (SimAlgorithm.java:533-576): offline plans, each output float[] 2w*2w; wf or fwf may be null
+GFN(void, reconstructWidefield)(JNIEnv* env, jclass, jlong plan, jarray raw, jfloatArray out, jfloatArray wf,
+                                jfloatArray fwf) {
+  fsim_host_job j{};
+  j.plan = reinterpret_cast<const fsim_plan*>(plan);
+  j.raw_host = env->GetPrimitiveArrayCritical(raw, nullptr);
+  int rc = j.raw_host ? FSIM_OK : FSIM_EOOM;
+  if (rc == FSIM_OK) j.out_host = static_cast<float*>(env->GetPrimitiveArrayCritical(out, nullptr));
+  if (rc == FSIM_OK && !j.out_host) rc = FSIM_EOOM;
+  if (rc == FSIM_OK && wf) {
+    j.widefield_host = static_cast<float*>(env->GetPrimitiveArrayCritical(wf, nullptr));
+    if (!j.widefield_host) rc = FSIM_EOOM;
+  }
+  if (rc == FSIM_OK && fwf) {
+    j.filtered_widefield_host = static_cast<float*>(env->GetPrimitiveArrayCritical(fwf, nullptr));
+    if (!j.filtered_widefield_host) rc = FSIM_EOOM;
+  }
+  if (rc == FSIM_OK) rc = fsim_recon_batch_host(&j, 1, 1);
+  if (j.filtered_widefield_host) env->ReleasePrimitiveArrayCritical(fwf, j.filtered_widefield_host, 0);
+  if (j.widefield_host) env->ReleasePrimitiveArrayCritical(wf, j.widefield_host, 0);
+  if (j.out_host) env->ReleasePrimitiveArrayCritical(out, j.out_host, 0);
+  if (j.raw_host) env->ReleasePrimitiveArrayCritical(raw, const_cast<void*>(j.raw_host), JNI_ABORT);
+  throw_status(env, rc);
+}
 // many stacks at once: overlapped uploads, passes and downloads (fsim_recon_batch_host)
 GFN(void, reconstructBatch)(JNIEnv* env, jclass, jlongArray plans, jobjectArray raws, jobjectArray outs) {
   const jsize n = env->GetArrayLength(plans);
@@ -323,6 +348,7 @@ GFN(void, reconstructBatch)(JNIEnv* env, jclass, jlongArray plans, jobjectArray 
     jobs[i].raw_host = env->GetPrimitiveArrayCritical(ra[i], nullptr);
     jobs[i].out_host = static_cast<float*>(env->GetPrimitiveArrayCritical(oa[i], nullptr));
     jobs[i].widefield_host = nullptr;
+    jobs[i].filtered_widefield_host = nullptr;
     if (!jobs[i].raw_host || !jobs[i].out_host) rc = FSIM_EOOM;
   }
   if (rc == FSIM_OK) rc = fsim_recon_batch_host(jobs.data(), n, 0);

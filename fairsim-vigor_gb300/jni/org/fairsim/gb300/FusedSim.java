@@ -69,6 +69,12 @@ public final class FusedSim {
 	/** raw: float[] (INPUT_F32) or short[] (INPUT_U16); out: float[4*w*w] */
 	public void reconstruct(Object raw, float [] out) { reconstruct(handle, raw, out); }
 
+	/** The reconstruction plus runReconstruction's "Widefield" and "filtered Widefield"
+	 *  images (SimAlgorithm.java:533-576; offline plans): wf, fwf float[4*w*w], either null */
+	public void reconstruct(Object raw, float [] out, float [] wf, float [] fwf) {
+	    reconstructWidefield(handle, raw, out, wf, fwf);
+	}
+
 	/** New shifts / phases / modulations (same geometry). */
 	public void update(SimParam p, double na, double lambdaNm, double otfA) {
 	    planUpdate(handle, geometry(p, w), optics(p, w, na, lambdaNm, otfA), directions(p));
@@ -113,6 +119,7 @@ public final class FusedSim {
     static native void planUpdate(long plan, int [] geom, double [] optics, double [] dirs);
     static native void planDestroy(long plan);
     static native void reconstruct(long plan, Object raw, float [] out);
+    static native void reconstructWidefield(long plan, Object raw, float [] out, float [] wf, float [] fwf);
     static native void reconstructBatch(long [] plans, Object [] raws, float [][] outs);
     static native void estimate(int [] geom, double [] optics, double [] dirs, float [] raw,
 	int fadePx, int fitBand, double fitExclude);

@@ -77,7 +77,8 @@ class SimParamC(C.Structure):
 
 
 class Job(C.Structure):
-    _fields_ = [("plan", C.c_void_p), ("raw", C.c_void_p), ("out", C.c_void_p), ("widefield", C.c_void_p)]
+    _fields_ = [("plan", C.c_void_p), ("raw", C.c_void_p), ("out", C.c_void_p), ("widefield", C.c_void_p),
+                ("filtered_widefield", C.c_void_p)]
 
 
 HostJob = Job  # fsim_host_job: same four pointer fields, host addresses

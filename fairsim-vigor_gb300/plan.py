@@ -67,6 +67,26 @@ class ReconPlan:
         N.check(N.lib().fsim_recon_host(self._h, raw.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p)))
         return out
 
+    def reconstruct_host_widefield(self, raw):
+        """The reconstruction with its widefield side outputs, host buffers in and out.
+        Offline plans: (image, widefield, filtered widefield), each 2w x 2w, as
+        runReconstruction's "Widefield" and "filtered Widefield" (SimAlgorithm.java:533-576);
+        live plans: (image, w x w widefield)."""
+        raw = np.ascontiguousarray(raw, dtype=self.raw_dtype())
+        n = self.sp.w
+        if raw.size != self.sp.nrDirs * self.sp.nrPhases * n * n:
+            raise ValueError("raw stack size mismatch")
+        out = np.empty((2 * n, 2 * n), dtype=np.float32)
+        ptr = lambda a: a.ctypes.data  # noqa: E731
+        if self.path == N.PATH_LIVE:
+            wf = np.empty((n, n), dtype=np.float32)
+            recon_batch_host([(self, ptr(raw), ptr(out), ptr(wf))])
+            return out, wf
+        wf = np.empty((2 * n, 2 * n), dtype=np.float32)
+        fwf = np.empty((2 * n, 2 * n), dtype=np.float32)
+        recon_batch_host([(self, ptr(raw), ptr(out), ptr(wf), ptr(fwf))])
+        return out, wf, fwf
+
     def close(self):
         if getattr(self, "_h", None):
             N.lib().fsim_plan_destroy(self._h)
@@ -93,11 +113,14 @@ def _job_array(jobs):
         arr[i].raw = j[1]
         arr[i].out = j[2]
         arr[i].widefield = j[3] if len(j) > 3 else None
+        arr[i].filtered_widefield = j[4] if len(j) > 4 else None
     return arr
 
 
 def recon_batch(jobs, workspace_ptr: int, workspace_bytes: int, stream_ptr: int = 0):
-    """jobs: iterable of (plan, raw_device_ptr, out_device_ptr[, widefield_device_ptr])."""
+    """jobs: iterable of (plan, raw_device_ptr, out_device_ptr[, widefield_device_ptr
+    [, filtered_widefield_device_ptr]]). The widefield is w x w on live plans and 2w x 2w on
+    offline plans; the filtered widefield (2w x 2w) exists on offline plans only."""
     arr = _job_array(jobs)
     N.check(N.lib().fsim_recon_batch(arr, len(arr), C.c_void_p(workspace_ptr), C.c_size_t(workspace_bytes),
                                      C.c_void_p(stream_ptr) if stream_ptr else None))
@@ -105,7 +128,8 @@ def recon_batch(jobs, workspace_ptr: int, workspace_bytes: int, stream_ptr: int 
 
 def recon_batch_host(jobs, chunk: int = 0):
     """Host-buffer batch (fsim_recon_batch_host): jobs is an iterable of
-    (plan, raw_host_ptr, out_host_ptr[, widefield_host_ptr]); uploads, passes and downloads
+    (plan, raw_host_ptr, out_host_ptr[, widefield_host_ptr[, filtered_widefield_host_ptr]]),
+    sized as in ``recon_batch``; uploads, passes and downloads
     of successive chunks overlap, and the call returns when every output is on the host."""
     arr = _job_array(jobs)
     N.check(N.lib().fsim_recon_batch_host(arr, len(arr), int(chunk)))

@@ -174,7 +174,13 @@ typedef struct fsim_job {
   const fsim_plan* plan;
   const void* raw;  /* device: nr_dirs*nr_phases frames, w*w each, f32 or u16 (plan input type) */
   float* out;       /* device: 2w x 2w float32 reconstruction (real part, CLIPSCALE.NONE) */
-  float* widefield; /* device, nullable: w x w mean of the damped raw frames (live path) */
+  float* widefield; /* device, nullable. Live plans: w x w mean of the damped raw frames
+                       (ReconstructionRunner.java:449-496). Offline plans: the 2w x 2w
+                       "Widefield" image of runReconstruction (SimAlgorithm.java:533-560) */
+  float* filtered_widefield; /* device, nullable; offline plans only: the 2w x 2w "filtered
+                                Widefield" (OTF band 0, widefield Wiener denominator and OTF
+                                support mask, SimAlgorithm.java:562-576). Both widefield
+                                outputs must be 8-byte aligned. */
 } fsim_job;
 /* Reconstruct n_jobs datasets (mixed sizes and plans allowed) with one set of launches per
  * size class; the size classes run side by side on library-owned streams forked from and
@@ -195,7 +201,8 @@ typedef struct fsim_host_job {
   const fsim_plan* plan;
   const void* raw_host;  /* nr_dirs*nr_phases frames, w*w each, f32 or u16 */
   float* out_host;       /* 2w x 2w float32 */
-  float* widefield_host; /* nullable; live-path plans only: w x w */
+  float* widefield_host; /* nullable; w x w (live plans) or 2w x 2w (offline plans), as fsim_job */
+  float* filtered_widefield_host; /* nullable; offline plans only: 2w x 2w */
 } fsim_host_job;
 int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int chunk);
 /* A fixed batch recorded once as a CUDA graph (no reference counterpart): the job-table

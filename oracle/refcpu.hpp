@@ -953,6 +953,48 @@ inline RVec<T> run_reconstruction(const SimParam<T>& param, const std::vector<st
   return res;
 }
 
+// WienerFilter.getWidefieldDenominator (S/WienerFilter.java:129-139): band 0 of direction 0,
+// no attenuation, on the 2w x 2h grid, then 1/(v + (float)(w^2))
+template <class T>
+inline RVec<T> widefield_denominator(const SimParam<T>& sp, double wParam) {
+  const int w = sp.imgSize;
+  RVec<T> wd(2 * w, 2 * w);
+  add_wiener_denominator(sp, wd, 0, 0, false);
+  T wp = rnd<T>(wParam * wParam);
+  for (auto& v : wd.d) v = T(1) / (v + wp);
+  return wd;
+}
+
+// The two side outputs of runReconstruction's Wiener path (S/SimAlgorithm.java:533-576):
+// "Widefield" = spatial(sum over directions of placeFreq(separated band 0)), and
+// "filtered Widefield" = the same spectrum times conj(OTF band 0) (no attenuation), times the
+// widefield Wiener denominator, masked to the OTF support, then spatial. clipScale as above.
+template <class T>
+inline void widefield_outputs(const SimParam<T>& param, const std::vector<std::vector<CVec<T>>>& inFFT,
+                              int clipScale, RVec<T>& wf, RVec<T>& fwf) {
+  const int w = inFFT[0][0].w, h = inFFT[0][0].h;
+  CVec<T> low(2 * w, 2 * h);
+  for (int a = 0; a < param.nrDirs; a++) {
+    const Dir& par = param.dirs[a];
+    std::vector<CVec<T>> sep(par.nrBands * 2 - 1, CVec<T>(w, h));
+    separate_bands(inFFT[a], sep, par.getPhases(), par.nrBands, par.getModulations());
+    CVec<T> tmp(2 * w, 2 * h);
+    paste_freq(tmp, sep[0], 0, 0);
+    v_add(low, tmp);
+  }
+  auto finish = [&](RVec<T>& r) {
+    if (clipScale == 1) clip_and_scale(r, true, false);
+    if (clipScale == 2) clip_and_scale(r, true, true);
+  };
+  wf = spatial(low);
+  finish(wf);
+  param.otf.otfToVector(low, 0, 0, false, false);
+  v_times_real(low, widefield_denominator(param, param.wiener));
+  param.otf.maskOtf(low, 0, 0);
+  fwf = spatial(low);
+  finish(fwf);
+}
+
 // ---------------------------------------------------------------------------
 // Correlation (S/Correlation.java:43-288)
 // ---------------------------------------------------------------------------

@@ -243,6 +243,17 @@ def recon_raw(p, raw, bgr=0.0, fade=10, clip_scale=0, dtype=np.float32):
     return out
 
 
+def widefield_raw(p, raw, bgr=0.0, fade=10, clip_scale=0, dtype=np.float32):
+    """(widefield, filtered widefield), both 2w x 2w, of runReconstruction's Wiener path."""
+    r = make_param(p)
+    raw = np.ascontiguousarray(raw, dtype=dtype)
+    wf = np.zeros((2 * r.w, 2 * r.w), dtype=dtype)
+    fwf = np.zeros((2 * r.w, 2 * r.w), dtype=dtype)
+    _chk(getattr(lib(), "ref_widefield_raw_" + _suf(dtype))(C.byref(r), _ptr(raw), C.c_double(bgr), fade,
+                                                            clip_scale, _ptr(wf), _ptr(fwf)))
+    return wf, fwf
+
+
 def estimate(p, spectra, fit_band=1, fit_exclude=0.6, dtype=np.float32):
     """Returns (params dict, peaks [nDir,4], coarse [nDir,2])."""
     r = make_param(p)

@@ -268,6 +268,17 @@ int ref_matrix_inverse(const double* in, int n, double* out, int pseudo, int m) 
       std::copy(r.d.begin(), r.d.end(), out);                                                         \
     })                                                                                                \
   }                                                                                                   \
+  int ref_widefield_raw_##SUF(const ref_param* p, const T* raw, double bgr, int fade, int clipScale,   \
+                              T* wf, T* fwf) {                                                        \
+    GUARD({                                                                                           \
+      ref::SimParam<T> sp = make_param<T>(p);                                                         \
+      auto in = prepare_raw<T>(p, raw, bgr, fade);                                                    \
+      ref::RVec<T> a, b;                                                                              \
+      ref::widefield_outputs(sp, in, clipScale, a, b);                                                \
+      std::copy(a.d.begin(), a.d.end(), wf);                                                          \
+      std::copy(b.d.begin(), b.d.end(), fwf);                                                         \
+    })                                                                                                \
+  }                                                                                                   \
   int ref_estimate_##SUF(ref_param* p, const T* inFFT, int fitBand, double fitExclude, double* peaks, \
                          double* coarse) {                                                            \
     GUARD({                                                                                           \

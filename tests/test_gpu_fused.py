@@ -291,3 +291,128 @@ def test_estimate_raw_1024_vs_oracle(fs, oracle, torch_cuda):
         assert abs(got["pX"][d] - est["pX"][d]) < 1e-9 and abs(got["pY"][d] - est["pY"][d]) < 1e-9
         assert abs(got["phaOff"][d] - est["phaOff"][d]) < 1e-4
         assert abs(got["pX"][d] - truth["pxpy"][d][0]) < 0.1 and abs(got["pY"][d] - truth["pxpy"][d][1]) < 0.1
+
+
+@pytest.mark.parametrize("n", [64, 128, 192, 256, 384, 512, 768, 1024])
+def test_offline_widefield_outputs_vs_oracle(fs, oracle, n):
+    """The "Widefield" and "filtered Widefield" side outputs of runReconstruction
+    (S/SimAlgorithm.java:533-576), computed on the device after the passes, against the
+    oracle; the reconstruction itself is unchanged by asking for them."""
+    raw, truth, sp = make(fs, n, seed=60 + n)
+    plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    img, wf, fwf = plan.reconstruct_host_widefield(raw)
+    assert np.array_equal(img, plan.reconstruct_host(raw))
+    e_wf, e_fwf = oracle.widefield_raw(sp, raw, fade=10)
+    assert rel_l2(wf, e_wf) < 1e-4
+    assert rel_l2(fwf, e_fwf) < 1e-4
+    if n <= 512:
+        d_wf, d_fwf = oracle.widefield_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+        assert rel_l2(wf, d_wf) < 1e-5
+        assert rel_l2(fwf, d_fwf) < 1e-5
+
+
+@pytest.mark.parametrize("variant", ["u16_bgr_att", "five_phases", "three_bands", "2048"])
+def test_offline_widefield_variants(fs, oracle, variant):
+    """u16 input with background and an attenuated OTF (the widefield filter is never
+    attenuated), 5 phases (pseudo-inverse separation), 3 bands, and the largest size."""
+    n, kw, bgr = 256, {}, 0.0
+    if variant == "u16_bgr_att":
+        kw = dict(as_u16=True)
+    if variant == "five_phases":
+        kw = dict(n_phases=5)
+    if variant == "three_bands":
+        kw = dict(n_phases=5, n_bands=3)
+    if variant == "2048":
+        n = 2048
+    raw, truth, sp = make(fs, n, seed=71, **kw)
+    u16 = raw.dtype == np.uint16
+    if u16:
+        sp.otf().setAttenuation(0.98, 1.3)
+        sp.otf().switchAttenuation(True)
+        bgr = 3.0
+    plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE,
+                             input_type=fs.native.INPUT_U16 if u16 else fs.native.INPUT_F32, fade_px=10, bgr=bgr)
+    img, wf, fwf = plan.reconstruct_host_widefield(raw)
+    e_wf, e_fwf = oracle.widefield_raw(sp, raw.astype(np.float32), bgr=bgr, fade=10)
+    assert rel_l2(wf, e_wf) < 1e-4
+    assert rel_l2(fwf, e_fwf) < 1e-4
+    assert rel_l2(img, oracle.recon_raw(sp, raw.astype(np.float32), bgr=bgr, fade=10)) < 1e-4
+
+
+def test_widefield_in_batches_and_graphs(fs, torch_cuda):
+    """Widefield outputs for some jobs of a mixed batch: the same bits as each job alone, no
+    change to the jobs that do not ask, the same bits again from a CUDA-graph replay (three
+    more launches per size class that asks), and EINVAL for a filtered widefield on a live plan."""
+    torch = torch_cuda
+    specs = [(256, 130, 2), (512, 131, 0), (384, 132, 1), (256, 133, 0)]  # 2: both, 1: widefield only
+    plans, raws = [], []
+    for n, seed, _ in specs:
+        raw, truth, sp = make(fs, n, seed)
+        plans.append(fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10))
+        raws.append(raw)
+    dev = lambda shape: torch.zeros(shape, dtype=torch.float32, device="cuda")  # noqa: E731
+    d_raw = [torch.from_numpy(r).cuda() for r in raws]
+    d_out = [dev((2 * p.w, 2 * p.w)) for p in plans]
+    d_wf = [dev((2 * p.w, 2 * p.w)) if s[2] >= 1 else None for p, s in zip(plans, specs)]
+    d_fwf = [dev((2 * p.w, 2 * p.w)) if s[2] == 2 else None for p, s in zip(plans, specs)]
+    ws = torch.empty(fs.plan.batch_workspace_bytes(plans), dtype=torch.uint8, device="cuda")
+    ptr = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+    jobs = [(p, ptr(r), ptr(o), ptr(w), ptr(f)) for p, r, o, w, f in zip(plans, d_raw, d_out, d_wf, d_fwf)]
+    fs.plan.recon_batch(jobs, ws.data_ptr(), ws.numel())
+    torch.cuda.synchronize()
+    for i, (p, r) in enumerate(zip(plans, raws)):
+        img, wf, fwf = p.reconstruct_host_widefield(r)
+        assert np.array_equal(d_out[i].cpu().numpy(), img)
+        if d_wf[i] is not None:
+            assert np.array_equal(d_wf[i].cpu().numpy(), wf)
+        if d_fwf[i] is not None:
+            assert np.array_equal(d_fwf[i].cpu().numpy(), fwf)
+    first = [[t.cpu().numpy().copy() if t is not None else None for t in ts] for ts in (d_out, d_wf, d_fwf)]
+    g = fs.plan.BatchGraph(jobs, ws.data_ptr(), ws.numel())
+    assert g.info() == {"jobs": 4, "kernels": 15 + 3 * 2}  # the 256 and 384 classes ask
+    for ts in (d_out, d_wf, d_fwf):
+        for t in ts:
+            if t is not None:
+                t.zero_()
+    g.launch()
+    torch.cuda.synchronize()
+    for ts, fs_ in zip((d_out, d_wf, d_fwf), first):
+        for t, e in zip(ts, fs_):
+            if t is not None:
+                assert np.array_equal(t.cpu().numpy(), e)
+    g.close()
+    live_raw, _, live_sp = make(fs, 256, 134, as_u16=True)
+    live = fs.plan.ReconPlan(live_sp, path=fs.native.PATH_LIVE, input_type=fs.native.INPUT_U16, fade_px=10)
+    lr = torch.from_numpy(live_raw.view(np.int16)).cuda()
+    lo, lw, lf = dev((512, 512)), dev((256, 256)), dev((512, 512))
+    ws2 = torch.empty(fs.plan.batch_workspace_bytes([live]), dtype=torch.uint8, device="cuda")
+    with pytest.raises(ValueError):
+        fs.plan.recon_batch([(live, lr.data_ptr(), lo.data_ptr(), lw.data_ptr(), lf.data_ptr())],
+                            ws2.data_ptr(), ws2.numel())
+
+
+def test_recon_batch_host_widefield(fs, torch_cuda):
+    """Host-buffer batches carry the offline widefield outputs (2w x 2w) and the live one (w x w)."""
+    torch = torch_cuda
+    specs = [(256, 140, "off"), (512, 141, "live"), (384, 142, "off")]
+    plans, raws = [], []
+    for n, seed, kind in specs:
+        live = kind == "live"
+        raw, truth, sp = make(fs, n, seed, as_u16=live)
+        plans.append(fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE if live else fs.native.PATH_OFFLINE,
+                                       input_type=fs.native.INPUT_U16 if live else fs.native.INPUT_F32, fade_px=10))
+        raws.append(raw)
+    pin = lambda shape: torch.empty(shape, dtype=torch.float32).pin_memory()  # noqa: E731
+    h_raw = [torch.from_numpy(r.view(np.int16) if r.dtype == np.uint16 else r).pin_memory() for r in raws]
+    h_out = [pin((2 * p.w, 2 * p.w)) for p in plans]
+    h_wf = [pin((p.w, p.w)) if p.path == fs.native.PATH_LIVE else pin((2 * p.w, 2 * p.w)) for p in plans]
+    h_fwf = [pin((2 * p.w, 2 * p.w)) if p.path == fs.native.PATH_OFFLINE else None for p in plans]
+    jobs = [(p, r.data_ptr(), o.data_ptr(), w.data_ptr(), f.data_ptr() if f is not None else None)
+            for p, r, o, w, f in zip(plans, h_raw, h_out, h_wf, h_fwf)]
+    fs.plan.recon_batch_host(jobs, chunk=2)
+    for p, r, o, w, f in zip(plans, raws, h_out, h_wf, h_fwf):
+        single = p.reconstruct_host_widefield(r)
+        assert np.array_equal(o.numpy(), single[0])
+        assert np.array_equal(w.numpy(), single[1])
+        if f is not None:
+            assert np.array_equal(f.numpy(), single[2])

@@ -133,3 +133,41 @@ def test_float_oracle_against_fp64_oracle(oracle, fs, n, n_phases, n_bands):
     err = float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64))
     print("oracle float vs FP64 at %d^2, %d phases, %d bands: rel-L2 %.2e" % (n, n_phases, n_bands, err))
     assert err < 1e-4
+
+
+def test_widefield_outputs_match_numpy(oracle, fs):
+    """runReconstruction's widefield side outputs (S/SimAlgorithm.java:533-576) against the
+    same steps in numpy: the band-0 spectra of every direction pasted at 2w and summed, then
+    (filtered) times OTF_0 / (2 OTF_0^2 + w^2) inside the OTF support."""
+    n = 64
+    raw, truth = fs.synth.make_dataset(n=n, seed=21)
+    sp = fs.synth.sim_param_for(truth, n)
+    wf, fwf = oracle.widefield_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+    spec = oracle.prepare_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+    n_dirs, n_pha = sp.nrDirs, sp.nrPhases
+    placed = np.zeros((2 * n, 2 * n), complex)
+    lo = np.r_[0:n // 2]
+    hi = np.r_[n // 2:n]
+    for a in range(n_dirs):
+        b0 = oracle.separate_bands(sp, a, spec[a * n_pha:(a + 1) * n_pha], dtype=np.float64)[0]
+        for ys, yd in ((lo, lo), (hi, hi + n)):
+            for xs, xd in ((lo, lo), (hi, hi + n)):
+                placed[np.ix_(yd, xd)] += b0[np.ix_(ys, xs)]
+    assert rel_l2(wf, np.fft.ifft2(placed).real) < 1e-12
+    W = 2 * n
+    xh = np.where(np.arange(W) < n, np.arange(W), np.arange(W) - W)
+    yh = np.where(np.arange(W) < n, -np.arange(W), W - np.arange(W))
+    cpm = 1 / (n * sp.micronsPerPixel)
+    cycl = np.hypot(xh[None, :], yh[:, None]) * cpm
+    otfp = sp.otf()
+    cut = otfp.getCutoff()
+    pos = cycl / (cut / 512)
+    dd = np.clip(np.floor(pos) / 512, 0, 1)
+    otf = (2 / np.pi) * (np.arccos(dd) - dd * np.sqrt(1 - dd * dd)) * otfp.a ** dd
+    otf = np.where((cycl < cut) & (np.ceil(pos) < 512), otf, 0.0)  # getOtfVal's two zero tests
+    filt = otf / (2 * otf * otf + sp.wienerFilterParameter ** 2)
+    filt[cycl > cut] = 0
+    assert rel_l2(fwf, np.fft.ifft2(placed * filt).real) < 1e-12
+    f32 = oracle.widefield_raw(sp, raw, fade=10)
+    for a64, a32 in zip((wf, fwf), f32):
+        assert rel_l2(a32, a64) < 1e-5
