@@ -216,7 +216,7 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--distinct", type=int, default=16)
     ap.add_argument("--no-extras", action="store_true", help="skip plain-GPU, serve, mixed, large and CPU legs")
-    ap.add_argument("--only", choices=["live", "fft", "estimate", "mixed", "large", "serve", "widefield"],
+    ap.add_argument("--only", choices=["live", "fft", "estimate", "mixed", "large", "serve", "widefield", "ingest"],
                     help="run one extra leg alone and print its JSON (profiling of its kernels)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -366,6 +366,7 @@ def main():
         extras["mixed_batch"] = mixed_leg(fs, torch, stream, timed)
         extras["live_batch"] = live_leg(fs, torch, stream, timed)
         extras["widefield_outputs"] = widefield_leg(fs, torch, stream, timed)
+        extras["livesim_ingest"] = ingest_leg(fs)
         extras["large_3x5_2048"] = large_leg(fs, torch, stream, timed)
         extras["estimate_1024"] = estimate_leg(fs, torch)
         extras["fft2d_vs_cufft"] = [fft_leg(fs, torch, stream, timed, n, b) for n, b in ((512, 64), (1024, 16))]
@@ -435,6 +436,8 @@ def run_only(args):
         res = mixed_leg(fs, torch, stream, timed, steps=args.steps)
     elif args.only == "large":
         res = large_leg(fs, torch, stream, timed, steps=args.steps)
+    elif args.only == "ingest":
+        res = ingest_leg(fs)
     elif args.only == "widefield":
         res = widefield_leg(fs, torch, stream, timed, batch=args.batch, steps=args.steps)
     else:
@@ -547,6 +550,61 @@ def widefield_leg(fs, torch, stream, timed, batch=64, steps=10, n=512, seed=88):
     res.update({"added_ms_per_batch": added, "algorithmic_MB_per_dataset": wf_bytes / 1e6,
                 "widefield_GB_per_s": wf_bytes * batch / (added / 1000.0) / 1e9 if added > 0 else None})
     plan.close()
+    return res
+
+
+def ingest_leg(fs, n=512, n_seq=20, chunk=1 << 20, seed=91):
+    """Live stream ingest (host): a two-channel LIVESIM byte stream of 512^2 u16 frames
+    (3x3 per sequence, a sync gap before each) cut into 1 MiB pieces, through the sequence
+    extractor alone (frames/s, GB/s of stream), then into the server as well (stacks/s
+    reconstructed end to end, p50/p99 from submission to result)."""
+    ig = fs.ingest
+    nraw = NA * NP
+    chans = []
+    for k, lam in enumerate((488.0, 568.0)):
+        raw, truth = fs.synth.make_dataset(n=n, seed=seed + k, em_wavelength=lam, as_u16=True)
+        chans.append((int(lam), raw, fs.synth.sim_param_for(truth, n)))
+    per = []
+    for num, raw, _ in chans:
+        frames, seq, t = [], 0, 10 ** 6
+        for _ in range(n_seq):
+            t += 8000
+            for i in range(nraw):
+                frames.append(ig.make_frame(raw[i], seq_nr=seq, pos1=num, time_camera=t))
+                seq += 1
+                t += 1000
+        per.append(frames)
+    blob = b"".join(f for pair in zip(*per) for f in pair)
+    pieces = [blob[at:at + chunk] for at in range(0, len(blob), chunk)]
+
+    def extractor():
+        return ig.SequenceExtractor([c[0] for c in chans], nraw, n, n, sync_mode=0, sync_frame_delay=5000)
+
+    x = extractor()
+    t0 = time.perf_counter()
+    for piece in pieces:
+        x.feed(piece)
+    popped = 0
+    while x.pop() is not None:
+        popped += 1
+    dt = time.perf_counter() - t0
+    frames = 2 * n_seq * nraw
+    res = {"frames_per_s": frames / dt, "stream_GB_per_s": len(blob) / dt / 1e9, "stacks": popped,
+           "note": "host only: header parse, sort, sync search, sequence copy"}
+    x.close()
+    srv = fs.plan.Server([c[2] for c in chans], max_batch=8, max_inflight=64, streams=3, refit_every=0)
+    live = ig.LiveIngest(extractor(), srv)
+    out = np.empty((2 * n, 2 * n), np.float32)
+    t0 = time.perf_counter()
+    tickets = []
+    for piece in pieces:
+        tickets += live.feed(piece)
+    lat = [srv.wait(tk, out) for _, tk in tickets]
+    dt = time.perf_counter() - t0
+    res.update({"e2e_stacks_per_s": len(tickets) / dt, "e2e_p50_ms": float(np.percentile(lat, 50)),
+                "e2e_p99_ms": float(np.percentile(lat, 99)), "e2e_stacks": len(tickets), "dropped": live.dropped})
+    srv.close()
+    live.x.close()
     return res
 
 

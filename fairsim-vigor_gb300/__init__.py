@@ -8,6 +8,7 @@ Layout:
   plan.py        fused batched reconstruction plans, CUDA-graph batches, host-buffer batches
                  and the served (live) form
   replicas.py    multi-GPU form: disjoint dataset shares per rank, max-over-ranks timing
+  ingest.py      live stream ingest: LIVESIM frame headers, SIM sequence detection
   sim_param.py   SimParam / SimParam.Dir / OtfProvider records
   synth.py       seeded synthetic SIM datasets
 """
@@ -20,7 +21,7 @@ def __getattr__(name):
     # vector/algorithm modules load the native library lazily
     import importlib
 
-    if name in ("vectors", "algorithm", "plan", "replicas", "autotune"):
+    if name in ("vectors", "algorithm", "plan", "replicas", "autotune", "ingest"):
         return importlib.import_module("." + name, __name__)
     if name in ("AccelVectorFactory", "Vec2dReal", "Vec2dCplx"):
         return getattr(importlib.import_module(".vectors", __name__), name)

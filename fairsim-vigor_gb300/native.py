@@ -112,6 +112,32 @@ class ServeStats(C.Structure):
     ]
 
 
+MAX_CHANNELS = 8
+LIVESIM_HEADER_BYTES = 128
+
+
+class LiveSimHeader(C.Structure):
+    _fields_ = [("seq_nr", C.c_int64), ("payload_offset", C.c_int32), ("payload_len", C.c_int32),
+                ("version", C.c_int32), ("bytes_per_pixel", C.c_int32), ("width", C.c_int32),
+                ("height", C.c_int32), ("pos_a", C.c_int32), ("pos_b", C.c_int32), ("pos0", C.c_int32),
+                ("pos1", C.c_int32), ("pos2", C.c_int32), ("time_camera", C.c_int64),
+                ("time_capture", C.c_int64), ("time_record", C.c_int64)]
+
+
+class SeqxConfig(C.Structure):
+    _fields_ = [("n_channels", C.c_int32), ("channel_numbers", C.c_int32 * MAX_CHANNELS),
+                ("raws_per_recon", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+                ("sync_mode", C.c_int32), ("sync_frame_freq", C.c_int32), ("sync_frame_avr", C.c_int32),
+                ("sync_frame_delay", C.c_int64), ("raw_queue", C.c_int32), ("sim_queue", C.c_int32)]
+
+
+class SeqxStats(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("bytes", C.c_uint64), ("unknown_channel", C.c_uint64),
+                ("missed_raw", C.c_uint64 * MAX_CHANNELS), ("missed_sim", C.c_uint64 * MAX_CHANNELS),
+                ("sync_frames", C.c_uint64 * MAX_CHANNELS), ("resyncs", C.c_uint64 * MAX_CHANNELS),
+                ("duplicates", C.c_uint64 * MAX_CHANNELS), ("sequences", C.c_uint64)]
+
+
 def to_c_param(p) -> SimParamC:
     """SimParam mirror (or dict) -> the C record."""
     g = (lambda k: p[k]) if isinstance(p, dict) else (lambda k: getattr(p, k))
@@ -219,6 +245,15 @@ _SIGS = {
     "fsim_serve_stats_get": (I32, [VP, VP]),
     "fsim_serve_params": (I32, [VP, I32, VP]),
     "fsim_serve_close": (I32, [VP]),
+    "fsim_livesim_parse": (I32, [VP, I32, I32, VP]),
+    "fsim_livesim_write": (I32, [VP, VP]),
+    "fsim_seqx_create": (I32, [C.POINTER(VP), VP]),
+    "fsim_seqx_push": (I32, [VP, VP, C.c_size_t]),
+    "fsim_seqx_feed": (I32, [VP, VP, C.c_size_t]),
+    "fsim_seqx_pop": (I32, [VP, VP, VP]),
+    "fsim_seqx_stats_get": (I32, [VP, VP]),
+    "fsim_seqx_reset": (I32, [VP]),
+    "fsim_seqx_destroy": (I32, [VP]),
 }
 
 

@@ -291,6 +291,75 @@ int fsim_serve_stats_get(fsim_server* s, fsim_serve_stats* out);
 int fsim_serve_params(fsim_server* s, int channel, fsim_sim_param* out);
 int fsim_serve_close(fsim_server* s);
 
+/* ---- live stream ingest (host only, no device work) -------------------------------------
+ * The camera-stream side of the live path: the 128-byte LIVESIM frame header
+ * (transport/header-definition.md, as transport/ImageWrapper.java:418-478 writes and
+ * checks it), the TCP byte stream split into frames (transport/ImageReceiver.java:122-164)
+ * and the per-channel SIM sequence detection (livemode/SimSequenceExtractor.java:152-518)
+ * that hands complete stacks to the reconstruction. */
+#define FSIM_LIVESIM_HEADER_BYTES 128
+typedef struct fsim_livesim_header {
+  int64_t seq_nr;          /* byte 0 */
+  int32_t payload_offset;  /* byte 8 (0) */
+  int32_t payload_len;     /* byte 12: width*height (pixels, as ImageWrapper writes it) */
+  int32_t version;         /* byte 16 (1) */
+  int32_t bytes_per_pixel; /* byte 17: 1 or 2 */
+  int32_t width, height;   /* bytes 32, 34 */
+  int32_t pos_a, pos_b;    /* bytes 36, 38: angle, phase */
+  int32_t pos0, pos1;      /* bytes 40, 42: z plane, channel (excitation wavelength) */
+  int32_t pos2;            /* byte 44: time point */
+  int64_t time_camera, time_capture, time_record; /* bytes 48, 56, 64: microseconds */
+} fsim_livesim_header;
+/* ImageWrapper.parseHeader: FSIM_EINVAL for a frame larger than max_width x max_height,
+ * payload_len != width*height, bytes per pixel not 1 or 2, or version != 1. */
+int fsim_livesim_parse(const void* header_bytes, int max_width, int max_height, fsim_livesim_header* out);
+/* ImageWrapper.writeHeader: zero-filled 128 bytes, version 1, payload_len = width*height. */
+int fsim_livesim_write(const fsim_livesim_header* h, void* header_bytes);
+
+#define FSIM_MAX_CHANNELS 8
+typedef struct fsim_seqx fsim_seqx;
+typedef struct fsim_seqx_config {
+  int32_t n_channels;
+  int32_t channel_numbers[FSIM_MAX_CHANNELS]; /* header pos1 of each channel ("ChannelNumber") */
+  int32_t raws_per_recon;   /* nr_dirs * nr_phases (at most 20, the sort buffer's size) */
+  int32_t width, height;    /* frame size (larger frames are broken headers) */
+  int32_t sync_mode;        /* "SyncMode" 0: time gap > delay; 1: gap = delay +- 50 or bright frame */
+  int32_t sync_frame_freq;  /* "SyncFrameFreq": SIM sequences per sync frame */
+  int32_t sync_frame_avr;   /* "SyncFrameAvr": mean pixel value of a bright sync frame */
+  int64_t sync_frame_delay; /* "SyncFrameDelay": microseconds */
+  int32_t raw_queue;        /* raw frames buffered per channel (0: raws_per_recon^2 * 10) */
+  int32_t sim_queue;        /* finished sequences buffered per channel (0: the same) */
+} fsim_seqx_config;
+typedef struct fsim_seqx_stats {
+  uint64_t frames, bytes;          /* accepted frames and stream bytes */
+  uint64_t unknown_channel;        /* frames whose pos1 is no configured channel (dropped) */
+  uint64_t missed_raw[FSIM_MAX_CHANNELS];  /* raw queue full (PerChannelBuffer.pushImg) */
+  uint64_t missed_sim[FSIM_MAX_CHANNELS];  /* sequence queue full */
+  uint64_t sync_frames[FSIM_MAX_CHANNELS];
+  uint64_t resyncs[FSIM_MAX_CHANNELS];     /* sort-buffer overflows (a frame lost, re-sorted) */
+  uint64_t duplicates[FSIM_MAX_CHANNELS];  /* frames with a sequence number already buffered */
+  uint64_t sequences;              /* joined multi-channel stacks handed out */
+} fsim_seqx_stats;
+int fsim_seqx_create(fsim_seqx** out, const fsim_seqx_config* cfg);
+/* One frame: 128-byte header followed by its payload (u8 or u16 little endian). Pixels of
+ * 8-bit frames are widened as the reference's getPixels does (Java's signed byte, so values
+ * >= 128 become 0xFF80..0xFFFF). FSIM_EINVAL for a broken header or a short frame,
+ * FSIM_ENOTFOUND for an unknown channel (counted, dropped). */
+int fsim_seqx_push(fsim_seqx* s, const void* frame, size_t bytes);
+/* Raw TCP bytes in arbitrary pieces: split into frames and pushed. A broken header closes
+ * the stream (FSIM_EINVAL now and for every later call until fsim_seqx_reset), as the
+ * reference's receiving thread ends on one. */
+int fsim_seqx_feed(fsim_seqx* s, const void* bytes, size_t n);
+/* The next stack with one SIM sequence of every channel (JoinedChannelBuffer): out is
+ * n_channels x raws_per_recon x height x width u16; first_seq (nullable, n_channels) gets
+ * the sequence number of each channel's first frame. FSIM_ENOTFOUND when none is ready. */
+int fsim_seqx_pop(fsim_seqx* s, uint16_t* out, int64_t* first_seq);
+int fsim_seqx_stats_get(const fsim_seqx* s, fsim_seqx_stats* out);
+/* Clears every buffer and restarts the sequence search (resetChannelBufferThreads and
+ * clearBuffers); reopens a stream closed by a broken header. */
+int fsim_seqx_reset(fsim_seqx* s);
+int fsim_seqx_destroy(fsim_seqx* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,3 +72,49 @@ def test_refit_on_device_matches_oracle(fs, oracle):
     for d in range(3):
         assert abs(got["pX"][d] - exp["pX"][d]) < 1e-9 and abs(got["pY"][d] - exp["pY"][d]) < 1e-9
     srv.close()
+
+
+def test_livesim_stream_to_served_reconstructions(fs):
+    """A two-channel LIVESIM camera stream (128-byte headers, u16 frames, a sync gap before
+    every sequence, neighbouring frames swapped) cut into TCP-sized pieces, through the
+    sequence extractor into the server: every stack reconstructs to the bits of that
+    channel's stack reconstructed alone."""
+    ig = fs.ingest
+    specs = [(488, 256, 21, 488.0), (568, 256, 22, 600.0)]
+    chans = [channel(fs, n, s, lam) for _, n, s, lam in specs]
+    alone = []
+    for raw, sp in chans:
+        plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE, input_type=fs.native.INPUT_U16, fade_px=10)
+        alone.append(plan.reconstruct_host(raw))
+    rng = np.random.default_rng(5)
+    n_seq, nraw = 6, 9
+    per = []
+    for (num, n, _, _), (raw, sp) in zip(specs, chans):
+        frames, seq, t = [], 0, 10 ** 6
+        for _ in range(n_seq):
+            t += 8000  # sync gap (SyncFrameDelay 5000 us)
+            for i in range(nraw):
+                frames.append(ig.make_frame(raw[i], seq_nr=seq, pos1=num, time_camera=t))
+                seq += 1
+                t += 1000
+        for i in range(1, len(frames) - 1, 7):  # out-of-order arrivals
+            frames[i], frames[i + 1] = frames[i + 1], frames[i]
+        per.append(frames)
+    blob = b"".join(f for pair in zip(*per) for f in pair)
+    x = ig.SequenceExtractor([s[0] for s in specs], nraw, 256, 256, sync_mode=0, sync_frame_delay=5000)
+    srv = fs.plan.Server([sp for _, sp in chans], max_batch=8, max_inflight=32, streams=2, refit_every=0)
+    live = ig.LiveIngest(x, srv)
+    tickets = []
+    at = 0
+    while at < len(blob):
+        k = int(rng.integers(1000, 300000))
+        tickets += live.feed(blob[at:at + k])
+        at += k
+    assert len(tickets) == 2 * n_seq and live.dropped == 0
+    out = np.empty((512, 512), np.float32)
+    for c, tk in tickets:
+        srv.wait(tk, out)
+        assert np.array_equal(out, alone[c])
+    assert x.stats()["sync_frames"] == [n_seq, n_seq]
+    srv.close()
+    x.close()
