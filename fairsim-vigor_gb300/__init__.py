@@ -10,10 +10,12 @@ Layout:
   replicas.py    multi-GPU form: disjoint dataset shares per rank, max-over-ranks timing
   ingest.py      live stream ingest: LIVESIM frame headers, SIM sequence detection
   sim_param.py   SimParam / SimParam.Dir / OtfProvider records
+  conf.py        fairSIM / VIGOR XML configuration files (utils/Conf), live channel settings
   synth.py       seeded synthetic SIM datasets
 """
 from .sim_param import Dir, OtfProvider, SimParam  # noqa: F401
 from . import synth  # noqa: F401
+from . import conf  # noqa: F401
 from . import native  # noqa: F401
 
 

@@ -141,6 +141,10 @@ class SeqxStats(C.Structure):
 def to_c_param(p) -> SimParamC:
     """SimParam mirror (or dict) -> the C record."""
     g = (lambda k: p[k]) if isinstance(p, dict) else (lambda k: getattr(p, k))
+    otf = None if isinstance(p, dict) else p.otf()
+    if otf is not None and not getattr(otf, "isEstimate", True):
+        raise NotImplementedError("measured (data) OTFs are not supported by the device path; "
+                                  "only OtfProvider.fromEstimate OTFs are")
     c = SimParamC()
     c.w = g("w")
     c.nr_dirs, c.nr_bands, c.nr_phases = g("nrDirs"), g("nrBands"), g("nrPhases")

@@ -1,4 +1,4 @@
-"""Host-side mirror of fairSIM's ``SimParam`` / ``SimParam.Dir`` / ``OtfProvider`` (estimate).
+"""Host-side mirror of fairSIM's ``SimParam`` / ``SimParam.Dir`` / ``OtfProvider``.
 
 Field meanings follow the reference:
   * ``SimParam.create(bands, dirs, phases, size, micronsPerPxl, otf)``
@@ -8,7 +8,9 @@ Field meanings follow the reference:
   * phases ``2*pi*i/nPhases + phaOff`` (SimParam.java:463-477);
   * modulations clamped to [0.3, 1.1] by ``getModulations`` (SimParam.java:598-607);
   * ``OtfProvider.fromEstimate(na, lambda, a)`` with cutoff ``1000/(lambda/na/2)`` cycles/micron
-    (OtfProvider.java:96-127), attenuation defaults 0.99 / 1.2 (OtfProvider.java:64).
+    (OtfProvider.java:96-127), attenuation defaults 0.99 / 1.2 (OtfProvider.java:64);
+  * ``loadConfig`` / ``saveConfig`` / ``loadFromConfig`` read and write the reference's
+    configuration folders (conf.py; SimParam.java:645-726, OtfProvider.java:575-676).
 
 These are plain parameter records: every computation on them runs in the native library.
 """
@@ -52,6 +54,66 @@ class OtfProvider:
 
     def duplicate(self) -> "OtfProvider":
         return copy.deepcopy(self)
+
+    # measured OTFs (OtfProvider.loadFromConfig with a "data" folder) keep their samples
+    # here: per band, complex values at cyclesPerMicron spacing
+    isEstimate = True
+    measured = None  # dict(bands=[[complex, ...], ...], cycles=float) or None
+
+    @staticmethod
+    def loadFromConfig(cfg) -> "OtfProvider":
+        """OtfProvider.loadFromConfig (S/OtfProvider.java:575-633): the "otf2d" folder;
+        an estimate (NA, emission, a-estimate) or measured band data, then attenuation."""
+        from .conf import from_bytes
+
+        fld = cfg.cd("otf2d")
+        if not fld.contains("data"):
+            ret = OtfProvider.fromEstimate(fld.getDbl("NA").val(), fld.getInt("emission").val(),
+                                           fld.getDbl("a-estimate").val())
+        else:
+            ret = OtfProvider.__new__(OtfProvider)
+            ret.na = fld.getDbl("NA").val()
+            ret.emWavelength = float(fld.getInt("emission").val())
+            ret.a = 1.0
+            ret.attStrength, ret.attFWHM, ret.useAttenuation = 0.99, 1.2, False
+            data = fld.cd("data")
+            nb, ns = data.getInt("bands").val(), data.getInt("samples").val()
+            bands = []
+            for b in range(nb):
+                v = from_bytes(data.getData("band-%d" % b).val())
+                bands.append([complex(v[2 * i], v[2 * i + 1]) for i in range(ns)])
+            ret.isEstimate = False
+            ret.measured = dict(bands=bands, cycles=data.getDbl("cycles").val())
+        if fld.contains("attenuation"):
+            att = fld.cd("attenuation")
+            ret.setAttenuation(att.getDbl("strength").val(), att.getDbl("FWHM").val())
+            ret.switchAttenuation(True)
+        return ret
+
+    def saveConfig(self, cfg) -> None:
+        """OtfProvider.saveConfig (S/OtfProvider.java:636-676) into folder ``cfg``."""
+        from .conf import to_bytes
+
+        fld = cfg.mk("otf2d")
+        fld.newDbl("NA").setVal(self.na)
+        fld.newInt("emission").setVal(int(self.emWavelength))
+        if self.isEstimate:
+            fld.newDbl("a-estimate").setVal(self.a)
+        else:
+            data = fld.mk("data")
+            bands = self.measured["bands"]
+            data.newInt("bands").setVal(len(bands))
+            data.newInt("samples").setVal(len(bands[0]))
+            data.newDbl("cycles").setVal(self.measured["cycles"])
+            for b, vals in enumerate(bands):
+                flat = []
+                for z in vals:
+                    flat += [z.real, z.imag]
+                data.newData("band-%d" % b).setVal(to_bytes(flat))
+        if self.useAttenuation:
+            att = fld.mk("attenuation")
+            att.newDbl("strength").setVal(self.attStrength)
+            att.newDbl("FWHM").setVal(self.attFWHM)
 
 
 @dataclass
@@ -113,7 +175,8 @@ class Dir:
 class SimParam:
     """2D subset of ``SimParam`` (S/SimParam.java:31-615)."""
 
-    def __init__(self, bands: int, dirs: int, phases: int, size: int, microns_per_pxl: float, otf: OtfProvider):
+    def __init__(self, bands: int, dirs: int, phases: int, size: int, microns_per_pxl: float,
+                 otf: Optional[OtfProvider]):
         if dirs < 1:
             raise ValueError("dirs < 1, not useful")
         self.nrDirs = int(dirs)
@@ -126,6 +189,8 @@ class SimParam:
         self.wienerFilterParameter = 0.05
         self.apoCutOff = 2.0
         self.apoBend = 0.9  # runReconstruction's fixed bend (SimAlgorithm.java:277)
+        self.imgSeq = "PAZ"  # IMGSEQ name (input order of the raw frames, stored only)
+        self.paramDate = 0   # "timestamp" of the parameter set, ms since 1970
 
     @staticmethod
     def create(bands, dirs, phases, size, microns_per_pxl, otf) -> "SimParam":
@@ -142,6 +207,57 @@ class SimParam:
 
     def otf(self) -> OtfProvider:
         return self._otf
+
+    def setOtf(self, otf: OtfProvider) -> "SimParam":
+        """SimParam.otf(OtfProvider): attach the OTF."""
+        self._otf = otf
+        return self
+
+    def saveConfig(self, cfg) -> None:
+        """SimParam.saveConfig (S/SimParam.java:645-672): a "sim-param" folder in ``cfg``."""
+        fd = cfg.mk("sim-param")
+        fd.newInt("nr-angles").setVal(self.nrDirs)
+        fd.newInt("nr-bands").setVal(self.nrBands)
+        fd.newInt("nr-phases").setVal(self.nrPhases)
+        fd.newStr("img-seq").setVal(self.imgSeq)
+        fd.newInt("img-size-pxl").setVal(self.imgSize)
+        fd.newDbl("microns-per-pxl").setVal(self.micronsPerPixel)
+        fd.newDbl("wiener-parameter").setVal(self.wienerFilterParameter)
+        fd.newDbl("apodization-cutoff").setVal(self.apoCutOff)
+        fd.newTDE("timestamp").set(self.paramDate)
+        for d, dr in enumerate(self.directions):
+            df = fd.mk("dir-%d" % d)
+            df.newDbl("shift").setVal(dr.pX * (dr.nrBands - 1), dr.pY * (dr.nrBands - 1))
+            df.newDbl("phase-offset").setVal(dr.phaOff)
+            df.newDbl("modulations").setVal(*dr.modul)
+            if dr.phases is not None:
+                df.newDbl("phases").setVal(*dr.phases)
+
+    @staticmethod
+    def loadConfig(cfg, otf: Optional[OtfProvider] = None) -> "SimParam":
+        """SimParam.loadConfig (S/SimParam.java:675-726) from the "sim-param" folder of
+        ``cfg``; the OTF is attached separately (``setOtf`` / OtfProvider.loadFromConfig)."""
+        fd = cfg.cd("sim-param")
+        ret = SimParam(fd.getInt("nr-bands").val(), fd.getInt("nr-angles").val(), fd.getInt("nr-phases").val(),
+                       fd.getInt("img-size-pxl").val(), fd.getDbl("microns-per-pxl").val(), otf)
+        if fd.contains("timestamp"):
+            ret.paramDate = fd.getTDE("timestamp").val()
+        ret.imgSeq = fd.getStr("img-seq").val().strip()
+        ret.setWienerFilter(fd.getDbl("wiener-parameter").val())
+        ret.setApoCutoff(fd.getDbl("apodization-cutoff").val())
+        for d in range(ret.nrDirs):
+            df = fd.cd("dir-%d" % d)
+            dr = ret.dir(d)
+            sh = df.getDbl("shift").vals()
+            if len(sh) < 2:
+                raise ValueError("Array too short")
+            dr.setPxPy(sh[0], sh[1])
+            dr.setPhaOff(df.getDbl("phase-offset").val())
+            for i, m in enumerate(df.getDbl("modulations").vals()):
+                dr.setModulation(i, m)
+            if df.contains("phases"):
+                dr.setPhases(df.getDbl("phases").vals(), False)
+        return ret
 
     def pxlSizeCyclesMicron(self) -> float:
         return 1.0 / (self.imgSize * self.micronsPerPixel)

@@ -416,3 +416,21 @@ def test_recon_batch_host_widefield(fs, torch_cuda):
         assert np.array_equal(w.numpy(), single[1])
         if f is not None:
             assert np.array_equal(f.numpy(), single[2])
+
+
+def test_plan_from_saved_config(fs, oracle, tmp_path):
+    """A parameter set written as the reference's XML (SimParam.saveConfig,
+    OtfProvider.saveConfig), read back and used for a plan: the reconstruction matches the
+    oracle on the loaded parameters."""
+    raw, truth, sp = make(fs, 256, seed=80)
+    sp.otf().setAttenuation(0.98, 1.3)
+    sp.otf().switchAttenuation(True)
+    cfg = fs.conf.Conf("fairsim")
+    sp.saveConfig(cfg.r())
+    sp.otf().saveConfig(cfg.r())
+    cfg.saveFile(tmp_path / "param.xml")
+    root = fs.conf.Conf.loadFile(tmp_path / "param.xml").r()
+    lp = fs.SimParam.loadConfig(root)
+    lp.setOtf(fs.OtfProvider.loadFromConfig(root))
+    plan = fs.plan.ReconPlan(lp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    assert rel_l2(plan.reconstruct_host(raw), oracle.recon_raw(lp, raw, fade=10)) < 1e-4

@@ -118,3 +118,56 @@ def test_livesim_stream_to_served_reconstructions(fs):
     assert x.stats()["sync_frames"] == [n_seq, n_seq]
     srv.close()
     x.close()
+
+
+def test_vigor_config_drives_ingest_and_server(fs, tmp_path):
+    """A VIGOR configuration (vigor-settings: raw size, angles, phases, sync settings, one
+    folder per channel with its sim-param and otf2d, as the reference's vigor-*.xml files
+    hold them) written, read back and used to set up the sequence extractor and the server;
+    a camera stream then reconstructs to the bits of plans built from the loaded channels."""
+    cfg = fs.conf.Conf("fairsim")
+    vs = cfg.r().mk("vigor-settings")
+    vs.newInt("RawPxlCount").setVal(256)
+    vs.newDbl("RawPxlSize").setVal(0.08)
+    vs.newInt("NrPhases").setVal(3)
+    vs.newInt("NrAngles").setVal(3)
+    vs.newInt("NrBands").setVal(2)
+    for k, v in (("SyncMode", 0), ("SyncFrameFreq", 1), ("SyncFrameAvr", 7000), ("SyncFrameDelay", 5000)):
+        vs.newInt(k).setVal(v)
+    raws = {}
+    for num, seed, lam in ((488, 31, 488.0), (568, 32, 600.0)):
+        raw, sp = channel(fs, 256, seed, lam)
+        raws[num] = raw
+        ch = vs.mk("channel-%d" % num)
+        ch.newDbl("offset").setVal(140.0)
+        ch.newInt("ChannelNumber").setVal(num)
+        sp.saveConfig(ch)
+        sp.otf().saveConfig(ch)
+    cfg.saveFile(tmp_path / "vigor.xml")
+    chans, stream = fs.conf.load_vigor_channels(fs.conf.Conf.loadFile(tmp_path / "vigor.xml").r().cd("vigor-settings"))
+    assert [c.number for c in chans] == [488, 568] and stream["raws_per_recon"] == 9
+    ig = fs.ingest
+    x = ig.SequenceExtractor(**stream)
+    srv = fs.plan.Server([c.param for c in chans], max_batch=4, max_inflight=16, streams=2, refit_every=0)
+    live = ig.LiveIngest(x, srv)
+    frames = []
+    for c in chans:
+        t, seq = 10 ** 6, 0
+        for _ in range(2):
+            t += 9000
+            for i in range(9):
+                frames.append(ig.make_frame(raws[c.number][i], seq_nr=seq, pos1=c.number, time_camera=t))
+                seq += 1
+                t += 1000
+    tickets = []
+    for f in frames:
+        tickets += live.push(f)
+    assert len(tickets) == 4
+    out = np.empty((512, 512), np.float32)
+    for ci, tk in tickets:
+        c = chans[ci]
+        srv.wait(tk, out)
+        plan = fs.plan.ReconPlan(c.param, path=fs.native.PATH_LIVE, input_type=fs.native.INPUT_U16, fade_px=10)
+        assert np.array_equal(out, plan.reconstruct_host(raws[c.number]))
+    srv.close()
+    x.close()
