@@ -357,6 +357,7 @@ def main():
     extras = {}
     if rank == 0 and not args.no_extras:
         extras["plain_gpu"] = plain_gpu_leg(fs, datasets[0])
+        extras["plain_gpu_rl_both"] = plain_gpu_leg(fs, datasets[0], k=3, style=3)
         extras["speedup_batched_vs_plain"] = value / extras["plain_gpu"]["value"]
         extras["speedup_e2e_vs_plain"] = e2e_value / extras["plain_gpu"]["value"]
         extras["serve"] = serve_leg(fs, seconds=3.0)
@@ -446,11 +447,16 @@ def run_only(args):
     return 0
 
 
-def plain_gpu_leg(fs, dataset, k=5):
+def plain_gpu_leg(fs, dataset, k=5, style=0):
     """The plain GPU form: one dataset at a time through the op-by-op device vector path
-    (the reference's accel-backed Java pipeline, one library call per vector op)."""
+    (the reference's accel-backed Java pipeline, one library call per vector op); style:
+    SimParam.FilterStyle (0 Wiener; 3 RL on the input and the output, 5 iterations each)."""
     V = fs.vectors
     raw, sp = dataset
+    if style:
+        sp = sp.duplicate()
+        sp.setFilterStyle(style)
+        sp.setRLiterations(5)
     spec_vecs = [[V.Vec2dCplx(N, N) for _ in range(NP)] for _ in range(NA)]
     fade = V.Vec2dReal(N, N)
     fade.setData(np.ones((N, N), np.float32))
@@ -470,7 +476,7 @@ def plain_gpu_leg(fs, dataset, k=5):
     t0 = time.perf_counter()
     for _ in range(k):
         plain()
-    return {"value": k / (time.perf_counter() - t0), "unit": "recon/s",
+    return {"value": k / (time.perf_counter() - t0), "unit": "recon/s", "filter_style": style,
             "note": "op-by-op device vector path (fsim_vec_* + fsim_run_reconstruction), one dataset at a time, "
                     "host buffers"}
 

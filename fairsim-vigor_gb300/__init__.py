@@ -27,6 +27,7 @@ def __getattr__(name):
         return importlib.import_module("." + name, __name__)
     if name in ("AccelVectorFactory", "Vec2dReal", "Vec2dCplx"):
         return getattr(importlib.import_module(".vectors", __name__), name)
-    if name in ("SimAlgorithm", "BandSeparation", "SimUtils", "Correlation", "WienerFilter", "OtfVectors"):
+    if name in ("SimAlgorithm", "BandSeparation", "SimUtils", "Correlation", "WienerFilter", "OtfVectors",
+                "RLDeconvolution"):
         return getattr(importlib.import_module(".algorithm", __name__), name)
     raise AttributeError(name)

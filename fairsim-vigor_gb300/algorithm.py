@@ -139,11 +139,25 @@ class Correlation:
         return list(out)
 
     @staticmethod
+    def autoCorrelation(inV, kx, ky):
+        """Correlation.autoCorrelation (S/Correlation.java:294-325): Wicker's phase estimate."""
+        re, im = C.c_double(), C.c_double()
+        N.check(N.lib().fsim_auto_correlation(inV.handle, float(kx), float(ky), C.byref(re), C.byref(im)))
+        return complex(re.value, im.value)
+
+    @staticmethod
     def getPeak(band0, band1, bn0, bn1, otf_param, kx, ky, weightLimit):
         out = (C.c_double * 2)()
         N.check(N.lib().fsim_get_peak(band0.handle, band1.handle, C.byref(_cp(otf_param)), float(kx), float(ky),
                                       float(weightLimit), out))
         return complex(out[0], out[1])
+
+
+class RLDeconvolution:
+    @staticmethod
+    def deconvolve(img, otf, steps, inputIsInFreqSpace=False):
+        """RLDeconvolution.deconvolve (S/RLDeconvolution.java:45-103) on device vectors."""
+        N.check(N.lib().fsim_rl_deconvolve(img.handle, otf.handle, int(steps), int(bool(inputIsInFreqSpace))))
 
 
 class SimAlgorithm:

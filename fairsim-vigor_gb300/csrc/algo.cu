@@ -263,6 +263,92 @@ __global__ void k_accum(float2* __restrict__ y, const float2* __restrict__ x, si
 
 static int grid1(size_t n) { return (int)std::min<size_t>((n + 255) / 256, (size_t)ctx().num_sms * 8); }
 
+// Vec.scal(float): v *= a (real factor)
+__global__ void k_scal_band0(float2* __restrict__ v, size_t n, float a) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float2 x = v[i];
+    v[i] = make_float2(__fmul_rn(x.x, a), __fmul_rn(x.y, a));
+  }
+}
+
+// ---- Richardson-Lucy (RLDeconvolution.deconvolve, S/RLDeconvolution.java:45-103) -------------
+// next = d .* reciproc(next): AbstractVectorCplx.reciproc (s = re^2 + im^2; re/s, -im/s,
+// L/AbstractVectorCplx.java:208-216), then times(d) (y = x .* y with x = d)
+__global__ void k_rl_div(float2* __restrict__ next, const float2* __restrict__ d, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float2 v = next[i], x = d[i];
+    const float s = __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y));
+    const float rr = __fdiv_rn(v.x, s), ri = __fdiv_rn(-v.y, s);
+    next[i] = make_float2(__fsub_rn(__fmul_rn(x.x, rr), __fmul_rn(x.y, ri)),
+                          __fadd_rn(__fmul_rn(x.y, rr), __fmul_rn(x.x, ri)));
+  }
+}
+// next = deconv .* next (times(deconvImg)), then deconvImg.copy(nextImg): both hold u_{j+1}
+__global__ void k_rl_update(float2* __restrict__ next, float2* __restrict__ deconv, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float2 v = next[i], x = deconv[i];
+    const float2 r = make_float2(__fsub_rn(__fmul_rn(x.x, v.x), __fmul_rn(x.y, v.y)),
+                                 __fadd_rn(__fmul_rn(x.y, v.x), __fmul_rn(x.x, v.y)));
+    next[i] = r;
+    deconv[i] = r;
+  }
+}
+
+// u_{j+1} = u_j x [(d / (u_j * psf)) * psf], the convolutions as products with `otf` in
+// frequency space, u_0 = d (the observed image); in_freq: img holds a spectrum
+int rl_deconvolve_device(float2* img, const float2* otf, int w, int h, int steps, bool in_freq, cudaStream_t st) {
+  FSIM_REQUIRE(fft2d_supported(w, h), FSIM_EINVAL, "RL deconvolution: unsupported size %d x %d", w, h);
+  FSIM_REQUIRE(steps >= 0, FSIM_EINVAL, "RL deconvolution: negative step count %d", steps);
+  const size_t n = (size_t)w * h;
+  DevBufs bufs(st);
+  float2 *deconv, *next;
+  TRY(bufs.get(&deconv, sizeof(float2) * n));
+  TRY(bufs.get(&next, sizeof(float2) * n));
+  if (in_freq) TRY(fft2d_device(img, w, h, true, st));
+  FSIM_CUDA(cudaMemcpyAsync(deconv, img, sizeof(float2) * n, cudaMemcpyDeviceToDevice, st));
+  FSIM_CUDA(cudaMemcpyAsync(next, img, sizeof(float2) * n, cudaMemcpyDeviceToDevice, st));
+  for (int i = 0; i < steps; i++) {
+    TRY(fft2d_device(next, w, h, false, st));  // u_j * psf
+    TRY(times_cplx_device(next, otf, n, false, st));
+    TRY(fft2d_device(next, w, h, true, st));
+    k_rl_div<<<grid1(n), 256, 0, st>>>(next, img, n);  // d / (u_j * psf)
+    FSIM_CHECK_LAUNCH();
+    TRY(fft2d_device(next, w, h, false, st));  // ... * psf
+    TRY(times_cplx_device(next, otf, n, false, st));
+    TRY(fft2d_device(next, w, h, true, st));
+    k_rl_update<<<grid1(n), 256, 0, st>>>(next, deconv, n);  // u_j x [...]
+    FSIM_CHECK_LAUNCH();
+  }
+  FSIM_CUDA(cudaMemcpyAsync(img, deconv, sizeof(float2) * n, cudaMemcpyDeviceToDevice, st));
+  if (in_freq) TRY(fft2d_device(img, w, h, false, st));
+  return FSIM_OK;
+}
+
+// Correlation.autoCorrelation (S/Correlation.java:294-325)
+int auto_correlation_device(const float2* band, int n, double kx, double ky, double* re, double* im, cudaStream_t st) {
+  const int N = 2 * n;
+  FSIM_REQUIRE(fft2d_supported(N, N), FSIM_EINVAL, "autoCorrelation: unsupported size %d", n);
+  const size_t n2 = (size_t)N * N;
+  DevBufs bufs(st);
+  float2 *a, *b;
+  TRY(bufs.get(&a, sizeof(float2) * n2));
+  TRY(bufs.get(&b, sizeof(float2) * n2));
+  const dim3 pg(div_up(N, 256), N), sg(div_up(N, 32), div_up(N, 8));
+  k_paste<<<pg, 256, 0, st>>>(a, N, band, n);
+  k_paste<<<pg, 256, 0, st>>>(b, N, band, n);
+  FSIM_CHECK_LAUNCH();
+  TRY(fft2d_device(b, N, N, true, st));  // timesShiftVector(kx, -ky) between the transforms
+  k_shift_ramp<<<sg, dim3(32, 8), 0, st>>>(b, N, kx, -ky);
+  FSIM_CHECK_LAUNCH();
+  TRY(fft2d_device(b, N, N, false, st));
+  double sr = 0, si = 0, n2a = 0;
+  TRY(reduce_device(3, reinterpret_cast<const float*>(a), reinterpret_cast<const float*>(b), 2 * n2, 1, st, &sr, &si));
+  TRY(norm2_device(a, n2, &n2a, st));
+  *re = sr / n2a;
+  *im = si / n2a;
+  return FSIM_OK;
+}
+
 int run_reconstruction_device(const fsim_sim_param* p, const float2* const* spec, float* out, bool otf_before_shift,
                               int clip_scale, cudaStream_t st) {
   TRY(validate_param(p));
@@ -281,6 +367,20 @@ int run_reconstruction_device(const fsim_sim_param* p, const float2* const* spec
   TRY(otf.set(p, st));
   OtfTable ht;
   build_otf_table(p, &ht);
+  // SimParam.useWienerFilter / useRLonInput / useRLonOutput (S/SimParam.java:287-304)
+  const int fs = p->filter_style;
+  const bool use_wiener = fs == FSIM_FILTER_WIENER || fs == FSIM_FILTER_RL_IN;
+  const bool rl_in = fs == FSIM_FILTER_RL_IN || fs == FSIM_FILTER_RL_BOTH;
+  const bool rl_out = fs == FSIM_FILTER_RL_OUT || fs == FSIM_FILTER_RL_BOTH;
+  // RL on the input deconvolves the first nrBand*2-1 input images and separates those
+  // (S/SimAlgorithm.java:331-354): with more phases than components the reference throws
+  FSIM_REQUIRE(!rl_in || nP == nC, FSIM_EINVAL, "#input images != phases per band");
+  float2 *in_otf = nullptr, *rl_tmp = nullptr;
+  if (rl_in) {
+    TRY(bufs.get(&in_otf, sizeof(float2) * n));
+    TRY(bufs.get(&rl_tmp, sizeof(float2) * n * nC));
+    TRY(otf_vector_device(in_otf, N, N, otf.d, 0, 0, false, true, st));  // writeOtfVector(band 0)
+  }
   // WienerFilter(param) + getDenominator(wiener) (SimAlgorithm.java:298, 509)
   TRY(wiener_denominator_device(denom, p, p->wiener, otf.d, true, st));
   FSIM_CUDA(cudaMemsetAsync(full, 0, sizeof(float2) * n2, st));
@@ -291,11 +391,19 @@ int run_reconstruction_device(const fsim_sim_param* p, const float2* const* spec
     sa.n_in = nP;
     sa.n_out = nC;
     for (int i = 0; i < nP; i++) sa.in[i] = spec[a * nP + i];
+    if (rl_in) {
+      for (int i = 0; i < nC; i++) {
+        float2* t = rl_tmp + (size_t)i * n;
+        FSIM_CUDA(cudaMemcpyAsync(t, spec[a * nP + i], sizeof(float2) * n, cudaMemcpyDeviceToDevice, st));
+        TRY(rl_deconvolve_device(t, in_otf, N, N, p->rl_iterations, true, st));
+        sa.in[i] = t;
+      }
+    }
     for (int b = 0; b < nC; b++) sa.out[b] = sep + b * n;
     for (int b = 0; b < nC; b++)
       for (int q = 0; q < nP; q++) sa.coef[b * nP + q] = make_float2(coef[b * nP + q].real(), coef[b * nP + q].imag());
     TRY(separate_device(sa, n, st));
-    if (otf_before_shift)
+    if (otf_before_shift && use_wiener)
       for (int i = 0; i < nC; i++) TRY(otf_vector_device(sep + i * n, N, N, otf.d, 0, 0, p->use_attenuation, false, st));
     for (int i = 0; i < nC; i++) k_paste<<<pg, 256, 0, st>>>(shifted + i * n2, W, sep + i * n, N);
     FSIM_CHECK_LAUNCH();
@@ -311,7 +419,13 @@ int run_reconstruction_device(const fsim_sim_param* p, const float2* const* spec
         TRY(fft2d_device(v, W, W, false, st));
       }
     }
-    if (!otf_before_shift) {
+    if (!use_wiener) {
+      // RL styles: no OTF on the shifted bands; band 0 scaled by 1.f/nrDir for RL on the output
+      if (rl_out) {
+        k_scal_band0<<<grid1(n2), 256, 0, st>>>(shifted, n2, 1.f / (float)p->nr_dirs);
+        FSIM_CHECK_LAUNCH();
+      }
+    } else if (!otf_before_shift) {
       TRY(otf_vector_device(shifted, W, W, otf.d, 0, 0, p->use_attenuation, false, st));
       for (int b = 1; b < nB; b++) {
         TRY(otf_vector_device(shifted + 2 * b * n2, W, W, otf.d, band_px(p, a, b), band_py(p, a, b), p->use_attenuation,
@@ -328,10 +442,33 @@ int run_reconstruction_device(const fsim_sim_param* p, const float2* const* spec
     for (int i = 0; i < nC; i++) k_accum<<<grid1(n2), 256, 0, st>>>(full, shifted + i * n2, n2);
     FSIM_CHECK_LAUNCH();
   }
-  // Wiener denominator, then apodization (bend apo_bend, cutoff apo_cutoff) as a complex vector
-  TRY(times_real_device(full, denom, n2, st));
-  TRY(apo_device(reinterpret_cast<float*>(apo), 1, W, W, ht.vec_cpm, ht.cutoff * p->apo_cutoff, p->apo_bend, st));
-  TRY(times_cplx_device(full, apo, n2, false, st));
+  if (use_wiener) {
+    // Wiener denominator, then apodization (bend apo_bend, cutoff apo_cutoff) as a complex vector
+    TRY(times_real_device(full, denom, n2, st));
+    TRY(apo_device(reinterpret_cast<float*>(apo), 1, W, W, ht.vec_cpm, ht.cutoff * p->apo_cutoff, p->apo_bend, st));
+    TRY(times_cplx_device(full, apo, n2, false, st));
+  } else {
+    // RL on the output with the effective SIM OTF: band 0 (1/nrDir per direction) and every
+    // other band at +-k of every direction (S/SimAlgorithm.java:591-611, 630-631); `apo`
+    // holds the sum, shifted[0] / shifted[1] the OTF vectors
+    float2 *osim = apo, *opos = shifted, *oneg = shifted + n2;
+    FSIM_CUDA(cudaMemsetAsync(osim, 0, sizeof(float2) * n2, st));
+    for (int a = 0; a < p->nr_dirs; a++)
+      for (int b = 0; b < nB; b++) {
+        const double kx = band_px(p, a, b), ky = band_py(p, a, b);
+        TRY(otf_vector_device(opos, W, W, otf.d, kx, ky, false, true, st));
+        if (b == 0) {
+          k_scal_band0<<<grid1(n2), 256, 0, st>>>(opos, n2, 1.f / (float)p->nr_dirs);
+          k_accum<<<grid1(n2), 256, 0, st>>>(osim, opos, n2);
+        } else {
+          TRY(otf_vector_device(oneg, W, W, otf.d, -kx, -ky, false, true, st));
+          k_accum<<<grid1(n2), 256, 0, st>>>(osim, opos, n2);
+          k_accum<<<grid1(n2), 256, 0, st>>>(osim, oneg, n2);
+        }
+        FSIM_CHECK_LAUNCH();
+      }
+    TRY(rl_deconvolve_device(full, osim, W, W, p->rl_iterations, true, st));
+  }
   // SimUtils.spatial: inverse FFT, real part, clipAndScale
   TRY(fft2d_device(full, W, W, true, st));
   k_real_part<<<grid1(n2), 256, 0, st>>>(out, full, n2);
@@ -472,6 +609,23 @@ int fsim_live_refit(fsim_sim_param* p, const uint16_t* raw_device, double* peaks
   std::vector<const float2*> ptrs(frames);
   for (int i = 0; i < frames; i++) ptrs[i] = spec + i * n;
   return estimate_core(p, ptrs.data(), 1, .8, true, peaks_out, st);
+}
+
+int fsim_rl_deconvolve(fsim_vec* img, const fsim_vec* otf, int steps, int input_in_freq_space) {
+  NEED_INIT();
+  FSIM_REQUIRE(img && otf && img->d && otf->d && img->cplx && otf->cplx, FSIM_EINVAL,
+               "RL deconvolution: complex image and OTF vectors required");
+  FSIM_REQUIRE(img->w == otf->w && img->h == otf->h, FSIM_EINVAL, "RL deconvolution: size mismatch %dx%d / %dx%d",
+               img->w, img->h, otf->w, otf->h);
+  return rl_deconvolve_device(reinterpret_cast<float2*>(img->d), reinterpret_cast<const float2*>(otf->d), img->w,
+                              img->h, steps, input_in_freq_space != 0, ctx().stream);
+}
+
+int fsim_auto_correlation(const fsim_vec* band, double kx, double ky, double* re, double* im) {
+  NEED_INIT();
+  FSIM_REQUIRE(band && band->d && band->cplx && re && im, FSIM_EINVAL, "autoCorrelation: null argument");
+  FSIM_REQUIRE(band->w == band->h, FSIM_EINVAL, "Vector len mismatch %d %d", band->w, band->h);  // checkSquare
+  return auto_correlation_device(reinterpret_cast<const float2*>(band->d), band->w, kx, ky, re, im, ctx().stream);
 }
 
 int fsim_run_reconstruction(const fsim_sim_param* p, fsim_vec* const* in_fft, fsim_vec* out_real, int otf_before_shift,

@@ -164,6 +164,11 @@ int validate_param(const fsim_sim_param* p) {
     set_error("SimParam: bad image size %d / pixel size %g", p->w, p->microns_per_pixel);
     return FSIM_EINVAL;
   }
+  if (p->filter_style < FSIM_FILTER_WIENER || p->filter_style > FSIM_FILTER_RL_BOTH ||
+      (p->filter_style != FSIM_FILTER_WIENER && p->rl_iterations < 0)) {
+    set_error("SimParam: bad filter style %d / RL iterations %d", p->filter_style, p->rl_iterations);
+    return FSIM_EINVAL;
+  }
   return FSIM_OK;
 }
 

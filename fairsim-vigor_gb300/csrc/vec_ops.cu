@@ -138,7 +138,7 @@ __global__ void k_reduce_partial(const float* __restrict__ x, const float* __res
     } else {
       for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nf; i += stride) a += x[i];
     }
-  } else {
+  } else if (MODE == 2) {
     // dot: sum conj(x)*y (L/AbstractVectorCplx.java:258-270)
     const float2* x2 = reinterpret_cast<const float2*>(x);
     const float2* y2 = reinterpret_cast<const float2*>(y);
@@ -146,6 +146,17 @@ __global__ void k_reduce_partial(const float* __restrict__ x, const float* __res
       float2 u = x2[i], v = y2[i];
       a += (double)(u.x * v.x - (-u.y) * v.y);
       b += (double)((-u.y) * v.x + u.x * v.y);
+    }
+  } else {
+    // sum x*conj(y) with the products in double (Correlation.autoCorrelation: Cplx.Double
+    // mult of the float values, S/Correlation.java:313-318)
+    const float2* x2 = reinterpret_cast<const float2*>(x);
+    const float2* y2 = reinterpret_cast<const float2*>(y);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nf / 2; i += stride) {
+      const float2 u = x2[i], v = y2[i];
+      const double ur = u.x, ui = u.y, vr = v.x, vi = -(double)v.y;
+      a += __dsub_rn(__dmul_rn(ur, vr), __dmul_rn(ui, vi));
+      b += __dadd_rn(__dmul_rn(ur, vi), __dmul_rn(ui, vr));
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -207,8 +218,10 @@ int reduce_device(int mode, const float* x, const float* y, size_t nf, int cplx,
     k_reduce_partial<0><<<blocks, threads, 0, st>>>(x, nullptr, nf, cplx, part);
   else if (mode == 1)
     k_reduce_partial<1><<<blocks, threads, 0, st>>>(x, nullptr, nf, cplx, part);
-  else
+  else if (mode == 2)
     k_reduce_partial<2><<<blocks, threads, 0, st>>>(x, y, nf, 1, part);
+  else
+    k_reduce_partial<3><<<blocks, threads, 0, st>>>(x, y, nf, 1, part);
   k_reduce_final<<<1, 256, 0, st>>>(part, blocks, out);
   FSIM_CHECK_LAUNCH();
   FSIM_CUDA(cudaMemcpyAsync(c.red_host, out, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -73,6 +73,8 @@ class SimParamC(C.Structure):
         ("modulation", (C.c_double * MAXB) * MAXD),
         ("has_phases", C.c_int32),
         ("phases", (C.c_double * MAXP) * MAXD),
+        ("filter_style", C.c_int32),
+        ("rl_iterations", C.c_int32),
     ]
 
 
@@ -153,6 +155,10 @@ def to_c_param(p) -> SimParamC:
     c.use_attenuation = int(g("useAttenuation"))
     c.att_strength, c.att_fwhm = g("attStrength"), g("attFWHM")
     c.wiener, c.apo_cutoff, c.apo_bend = g("wiener"), g("apoCutoff"), g("apoBend")
+    if isinstance(p, dict):
+        c.filter_style, c.rl_iterations = int(p.get("filterStyle", 0)), int(p.get("rlIterations", 5))
+    else:
+        c.filter_style, c.rl_iterations = int(getattr(p, "filterStyle", 0)), int(getattr(p, "rlIterations", 5))
     for d in range(c.nr_dirs):
         c.px[d], c.py[d], c.pha_off[d] = g("pX")[d], g("pY")[d], g("phaOff")[d]
         for b in range(c.nr_bands):
@@ -249,6 +255,8 @@ _SIGS = {
     "fsim_serve_stats_get": (I32, [VP, VP]),
     "fsim_serve_params": (I32, [VP, I32, VP]),
     "fsim_serve_close": (I32, [VP]),
+    "fsim_rl_deconvolve": (I32, [VP, VP, I32, I32]),
+    "fsim_auto_correlation": (I32, [VP, F64, F64, C.POINTER(F64), C.POINTER(F64)]),
     "fsim_livesim_parse": (I32, [VP, I32, I32, VP]),
     "fsim_livesim_write": (I32, [VP, VP]),
     "fsim_seqx_create": (I32, [C.POINTER(VP), VP]),

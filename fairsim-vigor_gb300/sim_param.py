@@ -22,6 +22,11 @@ from dataclasses import dataclass, field
 from typing import List, Optional
 
 
+# SimParam.FilterStyle (S/SimParam.java:33-43), by ordinal
+FILTER_WIENER, FILTER_RL_IN, FILTER_RL_OUT, FILTER_RL_BOTH = 0, 1, 2, 3
+FILTER_STYLES = ["Wiener", "RLin", "RLout", "RLboth"]
+
+
 class OtfProvider:
     """``OtfProvider.fromEstimate`` parameters (S/OtfProvider.java:96-127)."""
 
@@ -189,6 +194,8 @@ class SimParam:
         self.wienerFilterParameter = 0.05
         self.apoCutOff = 2.0
         self.apoBend = 0.9  # runReconstruction's fixed bend (SimAlgorithm.java:277)
+        self.filterStyle = FILTER_WIENER  # SimParam.FilterStyle ordinal
+        self.rlIterations = 5
         self.imgSeq = "PAZ"  # IMGSEQ name (input order of the raw frames, stored only)
         self.paramDate = 0   # "timestamp" of the parameter set, ms since 1970
 
@@ -207,6 +214,33 @@ class SimParam:
 
     def otf(self) -> OtfProvider:
         return self._otf
+
+    def setFilterStyle(self, style) -> None:
+        """SimParam.setFilterStyle: FILTER_WIENER, FILTER_RL_IN, FILTER_RL_OUT, FILTER_RL_BOTH
+        (or their names "Wiener", "RLin", "RLout", "RLboth")."""
+        if isinstance(style, str):
+            style = FILTER_STYLES.index(style)
+        if style not in range(4):
+            raise ValueError("unknown filter style %r" % (style,))
+        self.filterStyle = int(style)
+
+    def getFilterStyle(self) -> int:
+        return self.filterStyle
+
+    def useWienerFilter(self) -> bool:
+        return self.filterStyle in (FILTER_WIENER, FILTER_RL_IN)
+
+    def useRLonInput(self) -> bool:
+        return self.filterStyle in (FILTER_RL_BOTH, FILTER_RL_IN)
+
+    def useRLonOutput(self) -> bool:
+        return self.filterStyle in (FILTER_RL_BOTH, FILTER_RL_OUT)
+
+    def setRLiterations(self, n: int) -> None:
+        self.rlIterations = int(n)
+
+    def getRLiterations(self) -> int:
+        return self.rlIterations
 
     def setOtf(self, otf: OtfProvider) -> "SimParam":
         """SimParam.otf(OtfProvider): attach the OTF."""

@@ -77,7 +77,16 @@ typedef struct fsim_sim_param {
   double modulation[FSIM_MAX_DIRS][FSIM_MAX_BANDS];
   int32_t has_phases;
   double phases[FSIM_MAX_DIRS][FSIM_MAX_PHASES];
+  /* SimParam.FilterStyle ordinal (SimParam.java:33-43): FSIM_FILTER_WIENER (the fused plans
+   * and the live path), or an RL style (fsim_run_reconstruction); rl_iterations as
+   * SimParam.getRLiterations (the reference's default is 5) */
+  int32_t filter_style;
+  int32_t rl_iterations;
 } fsim_sim_param;
+#define FSIM_FILTER_WIENER 0
+#define FSIM_FILTER_RL_IN 1
+#define FSIM_FILTER_RL_OUT 2
+#define FSIM_FILTER_RL_BOTH 3
 
 /* ---- Vector API: device vectors (AccelVectorReal/Cplx[2d]) ---------------------------- */
 typedef struct fsim_vec fsim_vec;
@@ -142,11 +151,20 @@ int fsim_fit_peak(const fsim_vec* band0, const fsim_vec* band1, const fsim_sim_p
                   double ky, double weight_limit, double search, double out4[4], double* grid_out);
 int fsim_get_peak(const fsim_vec* band0, const fsim_vec* band1, const fsim_sim_param* p, double kx,
                   double ky, double weight_limit, double out2[2]);
+/* Correlation.autoCorrelation (Correlation.java:294-325): Wicker's non-iterative phase
+ * estimate; band (complex, square) pasted to 2w, one copy shifted by (kx, ky), sum of
+ * a*conj(b) in double over norm2(a). */
+int fsim_auto_correlation(const fsim_vec* band, double kx, double ky, double* re, double* im);
+/* RLDeconvolution.deconvolve (RLDeconvolution.java:45-103): `steps` Richardson-Lucy
+ * iterations on img with the complex OTF vector otf (same shape); input_in_freq_space:
+ * img holds a spectrum (transformed to real space and back). */
+int fsim_rl_deconvolve(fsim_vec* img, const fsim_vec* otf, int steps, int input_in_freq_space);
 
 /* ---- SimAlgorithm-compatible entries (SimAlgorithm.java:37, :268) -------------------
  * in_fft: nr_dirs*nr_phases complex w x w spectra (angle-major). The op-by-op variant
  * chains the vector kernels exactly like the reference's Java on an accel factory
- * (the "plain GPU form"). */
+ * (the "plain GPU form"); it runs every filter style (p->filter_style: Wiener, RL on the
+ * input, the output, or both, SimAlgorithm.java:318-361,587-641). */
 int fsim_run_reconstruction(const fsim_sim_param* p, fsim_vec* const* in_fft, fsim_vec* out_real,
                             int otf_before_shift, int clip_scale);
 int fsim_estimate_parameters(fsim_sim_param* p, fsim_vec* const* in_fft, int fit_band,

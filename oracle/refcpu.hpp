@@ -285,6 +285,17 @@ inline C<double> v_sum(const CVec<T>& y) {
   return {re, im};
 }
 
+// reciproc: conj(z)/|z|^2 in float (L/AbstractVectorCplx.java:208-216)
+template <class T>
+inline void v_reciproc(CVec<T>& y) {
+  size_t n = y.n();
+  for (size_t i = 0; i < n; i++) {
+    T s = y.d[2 * i] * y.d[2 * i] + y.d[2 * i + 1] * y.d[2 * i + 1];
+    y.d[2 * i] = y.d[2 * i] / s;
+    y.d[2 * i + 1] = -y.d[2 * i + 1] / s;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // FFT: mixed-radix (2,3,4,5) Stockham, the stand-in for JTransforms 3.1
 // (L/JTransformsConnector.java:76-92): FloatFFT_2D(rows=h, cols=w), in place on
@@ -783,6 +794,11 @@ struct SimParam {
   int imgSize = 0;
   double micronsPerPixel = 0, cyclesPerMicron = 0;
   double wiener = 0.05, apoCutOff = 2;
+  int filterStyle = 0;  // SimParam.FilterStyle: 0 Wiener, 1 RLin, 2 RLout, 3 RLboth (S/SimParam.java:33-43)
+  int rlIterations = 5;
+  bool useWienerFilter() const { return filterStyle == 0 || filterStyle == 1; }  // S/SimParam.java:287-290
+  bool useRLonInput() const { return filterStyle == 3 || filterStyle == 1; }     // :295-298
+  bool useRLonOutput() const { return filterStyle == 3 || filterStyle == 2; }    // :301-304
   std::vector<Dir> dirs;
   Otf<T> otf;
   int vectorWidth() const { return imgSize; }
@@ -896,7 +912,32 @@ inline void clip_and_scale(RVec<T>& v, bool clip, bool scale) {
 }
 
 // ---------------------------------------------------------------------------
-// SimAlgorithm.runReconstruction, Wiener path (S/SimAlgorithm.java:268-582)
+// RLDeconvolution.deconvolve (S/RLDeconvolution.java:45-103): u_{j+1} = u_j x [(d / (u_j * psf)) * psf]
+// with the convolutions as products with `otf` in frequency space; starting guess u_0 = d.
+// ---------------------------------------------------------------------------
+template <class T>
+inline void rl_deconvolve(CVec<T>& img, const CVec<T>& otf, int steps, bool inputIsInFreqSpace) {
+  if (inputIsInFreqSpace) fft2d(img, true);
+  CVec<T> deconv = img, next = img;
+  for (int i = 0; i < steps; i++) {
+    fft2d(next, false);
+    v_times(next, otf, false);
+    fft2d(next, true);
+    v_reciproc(next);
+    v_times(next, img, false);
+    fft2d(next, false);
+    v_times(next, otf, false);
+    fft2d(next, true);
+    v_times(next, deconv, false);
+    deconv = next;
+  }
+  img = deconv;
+  if (inputIsInFreqSpace) fft2d(img, false);
+}
+
+// ---------------------------------------------------------------------------
+// SimAlgorithm.runReconstruction (S/SimAlgorithm.java:268-686): Wiener path, RL on the input
+// (RLin / RLboth, :318-361), RL on the output with the effective SIM OTF (RLout / RLboth, :587-641)
 // clipScale: 0 NONE, 1 CLIP, 2 BOTH
 // ---------------------------------------------------------------------------
 template <class T>
@@ -907,12 +948,27 @@ inline RVec<T> run_reconstruction(const SimParam<T>& param, const std::vector<st
   const Otf<T>& otf = param.otf;
   RVec<T> denom = wiener_denominator(param, param.wiener);
   CVec<T> fullResult(2 * w, 2 * h);
+  const bool useWiener = param.useWienerFilter();
+  CVec<T> inputOtf;  // zero-band OTF for RL on the input (:313-321)
+  if (param.useRLonInput()) {
+    inputOtf = CVec<T>(w, h);
+    otf.writeOtfVector(inputOtf, 0, 0);
+  }
   for (int a = 0; a < param.nrDirs; a++) {
     const Dir& par = param.dirs[a];
     int nc = par.nrBands * 2 - 1;
     std::vector<CVec<T>> sep(nc, CVec<T>(w, h));
-    separate_bands(inFFT[a], sep, par.getPhases(), par.nrBands, par.getModulations());
-    if (otfBeforeShift)
+    if (param.useRLonInput()) {
+      // the reference deconvolves the first nrBand*2-1 input images only and separates those
+      // (:331-354): with more phases than components, separateBands throws
+      if ((int)inFFT[a].size() != nc) throw std::runtime_error("#input images != phases per band");
+      std::vector<CVec<T>> tmp(inFFT[a].begin(), inFFT[a].begin() + nc);
+      for (int i = 0; i < nc; i++) rl_deconvolve(tmp[i], inputOtf, param.rlIterations, true);
+      separate_bands(tmp, sep, par.getPhases(), par.nrBands, par.getModulations());
+    } else {
+      separate_bands(inFFT[a], sep, par.getPhases(), par.nrBands, par.getModulations());
+    }
+    if (otfBeforeShift && useWiener)
       for (int i = 0; i < nc; i++) otf.applyOtf(sep[i], 0, 0);
     std::vector<CVec<T>> shifted(std::max(5, nc), CVec<T>(2 * w, 2 * h));
     paste_freq(shifted[0], sep[0], 0, 0);
@@ -923,18 +979,43 @@ inline RVec<T> run_reconstruction(const SimParam<T>& param, const std::vector<st
       sim_fourier_shift(shifted[pos], par.px(b), par.py(b));
       sim_fourier_shift(shifted[neg], -par.px(b), -par.py(b));
     }
-    if (!otfBeforeShift) {
+    if (useWiener && !otfBeforeShift) {
       otf.applyOtf(shifted[0], 0, 0);
       for (int b = 1; b < par.nrBands; b++) {
         int pos = b * 2, neg = b * 2 - 1;
         otf.applyOtf(shifted[pos], par.px(b), par.py(b));
         otf.applyOtf(shifted[neg], -par.px(b), -par.py(b));
       }
-    } else {
+    } else if (useWiener) {
       // the reference passes (angIdx, component) as the mask centre (S/SimAlgorithm.java:407-409)
       for (int i = 0; i < nc; i++) otf.maskOtf(shifted[i], a, i);
     }
+    if (param.useRLonOutput()) v_scal(shifted[0], rnd<T>(1.0 / param.nrDirs));  // scal(1.f / nrDir())
     for (int i = 0; i < nc; i++) v_add(fullResult, shifted[i]);
+  }
+  if (!useWiener) {
+    // RL on the output with the effective SIM OTF: band 0 once (1/nrDir per direction), the
+    // other bands at +-k of every direction (S/SimAlgorithm.java:591-611, 630-631)
+    CVec<T> otfSim(2 * w, 2 * h), pos(2 * w, 2 * h), neg(2 * w, 2 * h);
+    for (int a = 0; a < param.nrDirs; a++) {
+      const Dir& par = param.dirs[a];
+      for (int b = 0; b < par.nrBands; b++) {
+        otf.writeOtfVector(pos, par.px(b), par.py(b));
+        otf.writeOtfVector(neg, -par.px(b), -par.py(b));
+        if (b == 0) {
+          v_scal(pos, rnd<T>(1.0 / param.nrDirs));
+          v_add(otfSim, pos);
+        } else {
+          v_add(otfSim, pos);
+          v_add(otfSim, neg);
+        }
+      }
+    }
+    rl_deconvolve(fullResult, otfSim, param.rlIterations, true);
+    RVec<T> res = spatial(fullResult);
+    if (clipScale == 1) clip_and_scale(res, true, false);
+    if (clipScale == 2) clip_and_scale(res, true, true);
+    return res;
   }
   CVec<T> apo(2 * w, 2 * h);
   {
@@ -988,11 +1069,38 @@ inline void widefield_outputs(const SimParam<T>& param, const std::vector<std::v
   };
   wf = spatial(low);
   finish(wf);
-  param.otf.otfToVector(low, 0, 0, false, false);
-  v_times_real(low, widefield_denominator(param, param.wiener));
-  param.otf.maskOtf(low, 0, 0);
+  if (param.useRLonOutput()) {
+    // RL styles: the widefield deconvolved with the zero-order OTF (S/SimAlgorithm.java:669-672)
+    CVec<T> zeroOrderOtf(2 * w, 2 * h);
+    param.otf.writeOtfVector(zeroOrderOtf, 0, 0);
+    rl_deconvolve(low, zeroOrderOtf, param.rlIterations, true);
+  } else {
+    param.otf.otfToVector(low, 0, 0, false, false);
+    v_times_real(low, widefield_denominator(param, param.wiener));
+    param.otf.maskOtf(low, 0, 0);
+  }
   fwf = spatial(low);
   finish(fwf);
+}
+
+// Correlation.autoCorrelation (S/Correlation.java:294-325): Wicker's non-iterative phase
+// estimate. The band pasted to 2w, one copy shifted by (kx, ky), sum of a * conj(b) in double,
+// divided by norm2 of the unshifted copy.
+template <class T>
+inline C<double> auto_correlation(const CVec<T>& inV, double kx, double ky) {
+  const int N = inV.w * 2;
+  CVec<T> aV(N, N), bV(N, N);
+  paste_freq(aV, inV, 0, 0);
+  paste_freq(bV, inV, 0, 0);
+  sim_fourier_shift(bV, kx, ky);
+  double re = 0, im = 0;
+  for (size_t i = 0; i < aV.n(); i++) {
+    const double ar = aV.d[2 * i], ai = aV.d[2 * i + 1], br = bV.d[2 * i], bi = -(double)bV.d[2 * i + 1];
+    re += ar * br - ai * bi;
+    im += ar * bi + ai * br;
+  }
+  const double n2 = v_norm2(aV);
+  return {re / n2, im / n2};
 }
 
 // ---------------------------------------------------------------------------

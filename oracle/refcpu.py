@@ -43,6 +43,8 @@ class RefParam(C.Structure):
         ("modul", (C.c_double * MAXB) * MAXD),
         ("hasPhases", C.c_int),
         ("phases", (C.c_double * MAXP) * MAXD),
+        ("filterStyle", C.c_int),
+        ("rlIterations", C.c_int),
     ]
 
 
@@ -111,6 +113,10 @@ def make_param(p) -> RefParam:
         for d in range(r.nrDirs):
             for i in range(r.nrPhases):
                 r.phases[d][i] = ph[d][i]
+    if isinstance(p, dict):
+        r.filterStyle, r.rlIterations = int(p.get("filterStyle", 0)), int(p.get("rlIterations", 5))
+    else:
+        r.filterStyle, r.rlIterations = int(getattr(p, "filterStyle", 0)), int(getattr(p, "rlIterations", 5))
     return r
 
 
@@ -241,6 +247,24 @@ def recon_raw(p, raw, bgr=0.0, fade=10, clip_scale=0, dtype=np.float32):
     out = np.zeros((2 * r.w, 2 * r.w), dtype=dtype)
     _chk(getattr(lib(), "ref_recon_raw_" + _suf(dtype))(C.byref(r), _ptr(raw), C.c_double(bgr), fade, clip_scale, _ptr(out)))
     return out
+
+
+def rl_deconvolve(img, otf, steps, in_freq=True, dtype=np.float32):
+    """RLDeconvolution.deconvolve on a copy of img (complex, h x w) with the complex otf."""
+    d = as_cplx_planes(img, dtype)
+    o = as_cplx_planes(otf, dtype)
+    h, w = d.shape[0], d.shape[1]
+    _chk(getattr(lib(), "ref_rl_deconvolve_" + _suf(dtype))(_ptr(d), _ptr(o), w, h, int(steps), int(in_freq)))
+    return from_interleaved(d)
+
+
+def auto_correlation(band, kx, ky, dtype=np.float32):
+    """Correlation.autoCorrelation: complex (double) for a square band spectrum."""
+    d = as_cplx_planes(band, dtype)
+    out = np.zeros(2)
+    _chk(getattr(lib(), "ref_auto_correlation_" + _suf(dtype))(_ptr(d), d.shape[0], C.c_double(kx), C.c_double(ky),
+                                                               _ptr(out)))
+    return complex(out[0], out[1])
 
 
 def widefield_raw(p, raw, bgr=0.0, fade=10, clip_scale=0, dtype=np.float32):

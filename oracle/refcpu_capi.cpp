@@ -25,6 +25,8 @@ typedef struct {
   double modul[REF_MAXD][REF_MAXB];
   int hasPhases;
   double phases[REF_MAXD][REF_MAXP];
+  int filterStyle;   // SimParam.FilterStyle ordinal
+  int rlIterations;
 } ref_param;
 }
 
@@ -38,6 +40,8 @@ static ref::SimParam<T> make_param(const ref_param* p) {
   sp.nrPhases = p->nrPhases;
   sp.wiener = p->wiener;
   sp.apoCutOff = p->apoCutoff;
+  sp.filterStyle = p->filterStyle;
+  sp.rlIterations = p->rlIterations;
   sp.otf = ref::Otf<T>::fromEstimate(p->na, p->lambda, p->otfA);
   sp.otf.setAttenuation(p->attStr, p->attFWHM);
   sp.otf.useAtt = p->useAtt != 0;
@@ -266,6 +270,24 @@ int ref_matrix_inverse(const double* in, int n, double* out, int pseudo, int m) 
       auto in = prepare_raw<T>(p, raw, bgr, fade);                                                    \
       ref::RVec<T> r = ref::run_reconstruction(sp, in, false, clipScale, p->apoBend);                 \
       std::copy(r.d.begin(), r.d.end(), out);                                                         \
+    })                                                                                                \
+  }                                                                                                   \
+  int ref_rl_deconvolve_##SUF(T* img, const T* otf, int w, int h, int steps, int inFreq) {                \
+    GUARD({                                                                                           \
+      ref::CVec<T> v(w, h), o(w, h);                                                                  \
+      std::copy(img, img + (size_t)2 * w * h, v.d.begin());                                           \
+      std::copy(otf, otf + (size_t)2 * w * h, o.d.begin());                                           \
+      ref::rl_deconvolve(v, o, steps, inFreq != 0);                                                   \
+      std::copy(v.d.begin(), v.d.end(), img);                                                         \
+    })                                                                                                \
+  }                                                                                                   \
+  int ref_auto_correlation_##SUF(const T* band, int w, double kx, double ky, double* out2) {         \
+    GUARD({                                                                                           \
+      ref::CVec<T> v(w, w);                                                                           \
+      std::copy(band, band + (size_t)2 * w * w, v.d.begin());                                         \
+      ref::C<double> r = ref::auto_correlation(v, kx, ky);                                            \
+      out2[0] = r.re;                                                                                 \
+      out2[1] = r.im;                                                                                 \
     })                                                                                                \
   }                                                                                                   \
   int ref_widefield_raw_##SUF(const ref_param* p, const T* raw, double bgr, int fade, int clipScale,   \

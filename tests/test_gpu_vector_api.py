@@ -265,3 +265,47 @@ def test_fft2d_batch_on_device_buffers(fs, V, w, h, batch):
     torch.cuda.synchronize()
     assert rel_l2(d.cpu().numpy(), z) < 3e-6
     assert lib.fsim_fft2d_batch(C.c_void_p(d.data_ptr()), 100, h, batch, 0, None) == fs.native.FSIM_EINVAL
+
+
+def test_rl_deconvolution_and_auto_correlation(fs, oracle, V):
+    """RLDeconvolution.deconvolve and Correlation.autoCorrelation (Wicker) on device vectors
+    against the oracle's float restatement (S/RLDeconvolution.java:45-103,
+    S/Correlation.java:294-325)."""
+    n = 128
+    rng = np.random.default_rng(12)
+    img = rng.uniform(50, 150, (n, n))
+    k = np.fft.fftfreq(n)
+    otf = (np.exp(-(k[None, :] ** 2 + k[:, None] ** 2) * 40) + 0j).astype(np.complex64)
+    spec = np.fft.fft2(img).astype(np.complex64)
+    v, o = cvec(V, spec), cvec(V, otf)
+    fs.algorithm.RLDeconvolution.deconvolve(v, o, 5, True)
+    exp = oracle.rl_deconvolve(spec, otf, 5, True)
+    assert rel_l2(v.vectorData(), exp) < 1e-5
+    band = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    got = fs.algorithm.Correlation.autoCorrelation(cvec(V, band), 7.3, -11.6)
+    ref = oracle.auto_correlation(band, 7.3, -11.6)
+    ref64 = oracle.auto_correlation(band, 7.3, -11.6, dtype=np.float64)
+    assert abs(got - ref) < 1e-5 * abs(ref)
+    assert abs(got - ref64) < 1e-5 * abs(ref64)
+
+
+@pytest.mark.parametrize("style", [1, 2, 3])
+def test_run_reconstruction_rl_styles_vs_oracle(fs, oracle, V, style):
+    """runReconstruction with RL on the input, the output, or both (the op-by-op device path)
+    against the oracle in float and FP64; raw frames carry a camera offset (RL divides by the
+    blurred estimate and needs positive data to be well conditioned)."""
+    n = 128
+    raw, truth = fs.synth.make_dataset(n=n, seed=91)
+    raw = raw + 200.0
+    sp = fs.synth.sim_param_for(truth, n)
+    sp.setFilterStyle(style)
+    sp.setRLiterations(3)
+    spec = oracle.prepare_raw(sp, raw)
+    exp32 = oracle.recon(sp, spec)
+    exp64 = oracle.recon(sp, spec.astype(np.complex128), dtype=np.float64)
+    inFFT = [[cvec(V, spec[a * 3 + p]) for p in range(3)] for a in range(3)]
+    out = fs.algorithm.SimAlgorithm.runReconstruction(sp, inFFT, False, 0).vectorData()
+    assert rel_l2(out, exp32) < 1e-4
+    assert rel_l2(out, exp64) < 1e-4
+    with pytest.raises(ValueError):  # the fused plans apply the Wiener filter only
+        fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)

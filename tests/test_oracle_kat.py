@@ -171,3 +171,63 @@ def test_widefield_outputs_match_numpy(oracle, fs):
     f32 = oracle.widefield_raw(sp, raw, fade=10)
     for a64, a32 in zip((wf, fwf), f32):
         assert rel_l2(a32, a64) < 1e-5
+
+
+def test_rl_deconvolution_matches_numpy(oracle):
+    """RLDeconvolution.deconvolve (S/RLDeconvolution.java:45-103) against the same iteration
+    in numpy (FP64), and the float oracle against FP64."""
+    n = 64
+    rng = np.random.default_rng(5)
+    img = rng.uniform(1, 2, (n, n)) + 0j
+    k = np.fft.fftfreq(n)
+    otf = np.exp(-(k[None, :] ** 2 + k[:, None] ** 2) * 30) + 0j
+    spec = np.fft.fft2(img)
+    got = oracle.rl_deconvolve(spec, otf, 4, True, dtype=np.float64)
+    d = np.fft.ifft2(spec)
+    u = d.copy()
+    for _ in range(4):
+        nx = np.fft.ifft2(np.fft.fft2(u) * otf)
+        nx = d / nx
+        nx = np.fft.ifft2(np.fft.fft2(nx) * otf)
+        u = nx * u
+    assert rel_l2(got, np.fft.fft2(u)) < 1e-12
+    assert rel_l2(oracle.rl_deconvolve(spec, otf, 4, True), got) < 1e-5
+
+
+def test_auto_correlation_matches_numpy(oracle):
+    """Correlation.autoCorrelation (S/Correlation.java:294-325) in FP64 against numpy."""
+    n = 32
+    rng = np.random.default_rng(9)
+    band = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    kx, ky = 3.3, -5.7
+    got = oracle.auto_correlation(band, kx, ky, dtype=np.float64)
+    N = 2 * n
+    a = oracle.paste_freq(band, N, N, dtype=np.float64)
+    X, Y = np.meshgrid(np.arange(N), np.arange(N))
+    b = np.fft.fft2(np.fft.ifft2(a) * np.exp(2j * np.pi * (kx * X - ky * Y) / N))
+    exp = np.sum(a * np.conj(b)) / np.sum(np.abs(a) ** 2)
+    assert abs(got - exp) < 1e-10 * abs(exp)
+    assert abs(oracle.auto_correlation(band, kx, ky) - got) < 1e-5 * abs(got)
+
+
+@pytest.mark.parametrize("style", [1, 2, 3])
+def test_rl_filter_styles_float_vs_fp64(oracle, fs, style):
+    """runReconstruction with RL on the input, the output, or both (S/SimAlgorithm.java:318-361,
+    587-641): the float oracle within the parity bound of FP64; the result differs from the
+    Wiener result (it is a different filter)."""
+    n = 64
+    raw, truth = fs.synth.make_dataset(n=n, seed=77)
+    # a camera offset keeps the raw frames positive: RL divides by the blurred estimate, and
+    # with the generator's zero-mean read noise in dark pixels that division is ill-conditioned
+    # (float and double then part ways in the reference's algorithm itself)
+    raw = raw + 200.0
+    sp = fs.synth.sim_param_for(truth, n)
+    sp.setFilterStyle(style)
+    sp.setRLiterations(3)
+    f32 = oracle.recon_raw(sp, raw, fade=10)
+    f64 = oracle.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+    err = rel_l2(f32, f64)
+    print("RL style %d: float vs FP64 rel-L2 %.2e" % (style, err))
+    assert err < 1e-4
+    sp.setFilterStyle(0)
+    assert rel_l2(f64, oracle.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)) > 1e-2
