@@ -131,7 +131,8 @@ int estimate_core(fsim_sim_param* p, const float2* const* spec, int fit_band, do
     TRY(locate_peak_device(c1, N, N, minDist, s, st, peak));
     double fit[4];
     const int fb = live ? hb : ((fit_band == 1) ? lb : hb);
-    TRY(fit_peak_device(sep, sep + fb * n, N, otf.d, -peak[0], -peak[1], 0.05, 2.5, s, st, fit, nullptr));
+    TRY(fit_peak_device(sep, sep + fb * n, N, otf.d, -peak[0], -peak[1], 0.05, 2.5, s, st, fit, nullptr, 0,
+                        live ? 1 : fit_band));
     std::complex<double> p1, p2;
     if (live) {
       const int nBand = nB - 1;
@@ -146,7 +147,7 @@ int estimate_core(fsim_sim_param* p, const float2* const* spec, int fit_band, do
         fit[1] *= 2;
       }
       TRY(get_peak_device(sep, sep + lb * n, N, otf.d, fit[0] / 2, fit[1] / 2, 0.05, s, st, &p1));
-      TRY(get_peak_device(sep, sep + hb * n, N, otf.d, fit[0], fit[1], 0.05, s, st, &p2));
+      TRY(get_peak_device(sep, sep + hb * n, N, otf.d, fit[0], fit[1], 0.05, s, st, &p2, 0, 2));
       p->px[a] = -fit[0] / (nB - 1);
       p->py[a] = -fit[1] / (nB - 1);
       p->pha_off[a] = std::atan2(p1.imag(), p1.real());
@@ -379,7 +380,7 @@ int run_reconstruction_device(const fsim_sim_param* p, const float2* const* spec
   if (rl_in) {
     TRY(bufs.get(&in_otf, sizeof(float2) * n));
     TRY(bufs.get(&rl_tmp, sizeof(float2) * n * nC));
-    TRY(otf_vector_device(in_otf, N, N, otf.d, 0, 0, false, true, st));  // writeOtfVector(band 0)
+    TRY(otf_vector_device(in_otf, N, N, otf.d, 0, 0, 0, false, true, st));  // writeOtfVector(band 0)
   }
   // WienerFilter(param) + getDenominator(wiener) (SimAlgorithm.java:298, 509)
   TRY(wiener_denominator_device(denom, p, p->wiener, otf.d, true, st));
@@ -404,7 +405,7 @@ int run_reconstruction_device(const fsim_sim_param* p, const float2* const* spec
       for (int q = 0; q < nP; q++) sa.coef[b * nP + q] = make_float2(coef[b * nP + q].real(), coef[b * nP + q].imag());
     TRY(separate_device(sa, n, st));
     if (otf_before_shift && use_wiener)
-      for (int i = 0; i < nC; i++) TRY(otf_vector_device(sep + i * n, N, N, otf.d, 0, 0, p->use_attenuation, false, st));
+      for (int i = 0; i < nC; i++) TRY(otf_vector_device(sep + i * n, N, N, otf.d, (i + 1) / 2, 0, 0, p->use_attenuation, false, st));
     for (int i = 0; i < nC; i++) k_paste<<<pg, 256, 0, st>>>(shifted + i * n2, W, sep + i * n, N);
     FSIM_CHECK_LAUNCH();
     for (int b = 1; b < nB; b++) {
@@ -426,11 +427,11 @@ int run_reconstruction_device(const fsim_sim_param* p, const float2* const* spec
         FSIM_CHECK_LAUNCH();
       }
     } else if (!otf_before_shift) {
-      TRY(otf_vector_device(shifted, W, W, otf.d, 0, 0, p->use_attenuation, false, st));
+      TRY(otf_vector_device(shifted, W, W, otf.d, 0, 0, 0, p->use_attenuation, false, st));
       for (int b = 1; b < nB; b++) {
-        TRY(otf_vector_device(shifted + 2 * b * n2, W, W, otf.d, band_px(p, a, b), band_py(p, a, b), p->use_attenuation,
+        TRY(otf_vector_device(shifted + 2 * b * n2, W, W, otf.d, b, band_px(p, a, b), band_py(p, a, b), p->use_attenuation,
                               false, st));
-        TRY(otf_vector_device(shifted + (2 * b - 1) * n2, W, W, otf.d, -band_px(p, a, b), -band_py(p, a, b),
+        TRY(otf_vector_device(shifted + (2 * b - 1) * n2, W, W, otf.d, b, -band_px(p, a, b), -band_py(p, a, b),
                               p->use_attenuation, false, st));
       }
     } else {
@@ -456,12 +457,12 @@ int run_reconstruction_device(const fsim_sim_param* p, const float2* const* spec
     for (int a = 0; a < p->nr_dirs; a++)
       for (int b = 0; b < nB; b++) {
         const double kx = band_px(p, a, b), ky = band_py(p, a, b);
-        TRY(otf_vector_device(opos, W, W, otf.d, kx, ky, false, true, st));
+        TRY(otf_vector_device(opos, W, W, otf.d, b, kx, ky, false, true, st));
         if (b == 0) {
           k_scal_band0<<<grid1(n2), 256, 0, st>>>(opos, n2, 1.f / (float)p->nr_dirs);
           k_accum<<<grid1(n2), 256, 0, st>>>(osim, opos, n2);
         } else {
-          TRY(otf_vector_device(oneg, W, W, otf.d, -kx, -ky, false, true, st));
+          TRY(otf_vector_device(oneg, W, W, otf.d, b, -kx, -ky, false, true, st));
           k_accum<<<grid1(n2), 256, 0, st>>>(osim, opos, n2);
           k_accum<<<grid1(n2), 256, 0, st>>>(osim, oneg, n2);
         }

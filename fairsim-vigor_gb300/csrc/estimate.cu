@@ -21,30 +21,60 @@
 namespace fsim {
 
 // ---- commonRegion as a gather (Correlation.java:227-288) --------------------------------
+// Cplx.Float.abs: (float)sqrt((double)re*re + (double)im*im)
+__device__ __forceinline__ float cabs_java(float2 v) {
+  return (float)__dsqrt_rn(__dadd_rn(__dmul_rn((double)v.x, (double)v.x), __dmul_rn((double)v.y, (double)v.y)));
+}
+// Cplx.Float.div(a, b) = mult(a, reciproc(b)), reciproc = (re/s, -im/s), s = re^2 + im^2
+__device__ __forceinline__ float2 cdiv_java(float2 a, float2 b) {
+  const float s = __fadd_rn(__fmul_rn(b.x, b.x), __fmul_rn(b.y, b.y));
+  const float rr = __fdiv_rn(b.x, s), ri = __fdiv_rn(-b.y, s);
+  return make_float2(__fsub_rn(__fmul_rn(a.x, rr), __fmul_rn(a.y, ri)), __fadd_rn(__fmul_rn(a.x, ri), __fmul_rn(a.y, rr)));
+}
+
 __global__ void k_common_region(float2* __restrict__ b0, float2* __restrict__ b1, int w, int h,
-                                const OtfTable* __restrict__ t, double kx, double ky, double dist, double wl, int divide) {
+                                const OtfTable* __restrict__ t, double kx, double ky, double dist, double wl, int divide,
+                                int bn0, int bn1) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   if (x >= w) return;
   const double xh = freq_x(x, w), yh = freq_y(y, h);
-  float w0 = 0.f, w1 = 0.f, t0 = 0.f, t1 = 0.f;
-  if (!otf_at(*t, xh, yh, 0, 0, false, &w0)) w0 = 0.f;
-  w1 = w0;  // single-band OTF: weight1 == weight0
-  if (!otf_at(*t, xh, yh, kx, ky, false, &t0)) t0 = 0.f;
-  if (!otf_at(*t, xh, yh, -kx, -ky, false, &t1)) t1 = 0.f;
   const size_t i = (size_t)y * w + x;
   float2 v0 = b0[i], v1 = b1[i];
-  // |OTF| of (val, 0) computed as (float)sqrt((double)val*val) == |val|
-  if (fabsf(w0) < wl || fabsf(t0) < wl) {
-    v0 = make_float2(0.f, 0.f);
-  } else if (divide) {
-    float r = __fdiv_rn(w0, __fmul_rn(w0, w0));  // Cplx.Float.reciproc, real part
-    v0 = make_float2(__fmul_rn(v0.x, r), __fmul_rn(v0.y, r));
-  }
-  if (fabsf(w1) < wl || fabsf(t1) < wl) {
-    v1 = make_float2(0.f, 0.f);
-  } else if (divide) {
-    float r = __fdiv_rn(w1, __fmul_rn(w1, w1));
-    v1 = make_float2(__fmul_rn(v1.x, r), __fmul_rn(v1.y, r));
+  if (t->measured) {
+    // weights of bands bn0 / bn1 at 0 and at +-k (writeOtfVector), complex
+    const float2 z = make_float2(0.f, 0.f);
+    float2 w0, w1, t0, t1;
+    if (!otf_at_c(*t, bn0, xh, yh, 0, 0, false, &w0)) w0 = z;
+    if (!otf_at_c(*t, bn1, xh, yh, 0, 0, false, &w1)) w1 = z;
+    if (!otf_at_c(*t, bn0, xh, yh, kx, ky, false, &t0)) t0 = z;
+    if (!otf_at_c(*t, bn1, xh, yh, -kx, -ky, false, &t1)) t1 = z;
+    if (cabs_java(w0) < wl || cabs_java(t0) < wl)
+      v0 = z;
+    else if (divide)
+      v0 = cdiv_java(v0, w0);
+    if (cabs_java(w1) < wl || cabs_java(t1) < wl)
+      v1 = z;
+    else if (divide)
+      v1 = cdiv_java(v1, w1);
+  } else {
+    float w0 = 0.f, w1 = 0.f, t0 = 0.f, t1 = 0.f;
+    if (!otf_at(*t, xh, yh, 0, 0, false, &w0)) w0 = 0.f;
+    w1 = w0;  // single-band OTF: weight1 == weight0
+    if (!otf_at(*t, xh, yh, kx, ky, false, &t0)) t0 = 0.f;
+    if (!otf_at(*t, xh, yh, -kx, -ky, false, &t1)) t1 = 0.f;
+    // |OTF| of (val, 0) computed as (float)sqrt((double)val*val) == |val|
+    if (fabsf(w0) < wl || fabsf(t0) < wl) {
+      v0 = make_float2(0.f, 0.f);
+    } else if (divide) {
+      float r = __fdiv_rn(w0, __fmul_rn(w0, w0));  // Cplx.Float.reciproc, real part
+      v0 = make_float2(__fmul_rn(v0.x, r), __fmul_rn(v0.y, r));
+    }
+    if (fabsf(w1) < wl || fabsf(t1) < wl) {
+      v1 = make_float2(0.f, 0.f);
+    } else if (divide) {
+      float r = __fdiv_rn(w1, __fmul_rn(w1, w1));
+      v1 = make_float2(__fmul_rn(v1.x, r), __fmul_rn(v1.y, r));
+    }
   }
   const double mx = sqrt(kx * kx + ky * ky);
   auto cut = [&](int xx, int yy) {
@@ -181,9 +211,9 @@ __global__ void k_corr_cols(const double2* __restrict__ Q, const float2* __restr
 
 // ---- host side ------------------------------------------------------------------------------
 int common_region_device(float2* b0, float2* b1, int w, int h, const OtfTable* t, double kx, double ky, double dist,
-                         double wl, bool divide, cudaStream_t st) {
+                         double wl, bool divide, cudaStream_t st, int bn0, int bn1) {
   dim3 g(div_up(w, 128), h);
-  k_common_region<<<g, 128, 0, st>>>(b0, b1, w, h, t, kx, ky, dist, wl, divide ? 1 : 0);
+  k_common_region<<<g, 128, 0, st>>>(b0, b1, w, h, t, kx, ky, dist, wl, divide ? 1 : 0, bn0, bn1);
   FSIM_CHECK_LAUNCH();
   return FSIM_OK;
 }
@@ -292,13 +322,13 @@ int norm2_device(const float2* v, size_t n, double* out, cudaStream_t st);
 
 // Correlation.fitPeak (Correlation.java:43-136) on device spectra band0/band1 (w x w).
 int fit_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
-                    double search, EstScratch& s, cudaStream_t st, double out4[4], double* grid_out) {
+                    double search, EstScratch& s, cudaStream_t st, double out4[4], double* grid_out, int bn0, int bn1) {
   double resPhase = 0, resMag = 0;
   const size_t img = (size_t)N * N * sizeof(float2);
   for (int iter = 0; iter < 3; iter++) {
     FSIM_CUDA(cudaMemcpyAsync(s.b0, band0, img, cudaMemcpyDeviceToDevice, st));
     FSIM_CUDA(cudaMemcpyAsync(s.b1, band1, img, cudaMemcpyDeviceToDevice, st));
-    int rc = common_region_device(s.b0, s.b1, N, N, t, kx, ky, 0.15, wl, true, st);
+    int rc = common_region_device(s.b0, s.b1, N, N, t, kx, ky, 0.15, wl, true, st, bn0, bn1);
     if (rc) return rc;
     rc = fft2d_device(s.b0, N, N, true, st);
     if (rc) return rc;
@@ -346,11 +376,11 @@ int fit_peak_device(const float2* band0, const float2* band1, int N, const OtfTa
 
 // Correlation.getPeak (Correlation.java:183-209)
 int get_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
-                    EstScratch& s, cudaStream_t st, std::complex<double>* out) {
+                    EstScratch& s, cudaStream_t st, std::complex<double>* out, int bn0, int bn1) {
   const size_t img = (size_t)N * N * sizeof(float2);
   FSIM_CUDA(cudaMemcpyAsync(s.b0, band0, img, cudaMemcpyDeviceToDevice, st));
   FSIM_CUDA(cudaMemcpyAsync(s.b1, band1, img, cudaMemcpyDeviceToDevice, st));
-  int rc = common_region_device(s.b0, s.b1, N, N, t, kx, ky, 0.15, wl, true, st);
+  int rc = common_region_device(s.b0, s.b1, N, N, t, kx, ky, 0.15, wl, true, st, bn0, bn1);
   if (rc) return rc;
   if ((rc = fft2d_device(s.b0, N, N, true, st))) return rc;
   if ((rc = fft2d_device(s.b1, N, N, true, st))) return rc;

@@ -21,15 +21,17 @@ struct EstScratch {
   void free(cudaStream_t st);
 };
 
+// bn0 / bn1: the OTF bands of the two spectra (measured multi-band OTFs)
 int common_region_device(float2* b0, float2* b1, int w, int h, const OtfTable* t, double kx, double ky, double dist,
-                         double wl, bool divide, cudaStream_t st);
+                         double wl, bool divide, cudaStream_t st, int bn0 = 0, int bn1 = 1);
 int locate_peak_device(const float2* v, int w, int h, double kmin, EstScratch& s, cudaStream_t st, double out4[4]);
 int corr_grid_device(const float2* b0, const float2* b1, int N, const double* kxs, int nx, const double* kys, int ny,
                      double scal, EstScratch& s, cudaStream_t st, std::vector<std::complex<double>>& out);
 int fit_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
-                    double search, EstScratch& s, cudaStream_t st, double out4[4], double* grid_out);
+                    double search, EstScratch& s, cudaStream_t st, double out4[4], double* grid_out, int bn0 = 0,
+                    int bn1 = 1);
 int get_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
-                    EstScratch& s, cudaStream_t st, std::complex<double>* out);
+                    EstScratch& s, cudaStream_t st, std::complex<double>* out, int bn0 = 0, int bn1 = 1);
 
 // SimAlgorithm.estimateParameters (live=false) or ParameterRefitThread.doRefit (live=true)
 // on device spectra spec[a*nP + p] (N x N complex); updates p's shifts/phases/modulations.

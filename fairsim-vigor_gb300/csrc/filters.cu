@@ -20,10 +20,34 @@ double ideal_otf_host(double d) {
   return (2 / M_PI) * (std::acos(d) - d * std::sqrt(1 - d * d));
 }
 
+// OtfProvider.valAttenuation (java:234-236)
+static float val_attenuation(double dist, double str, double fwhm) {
+  return (float)(1 - str * std::exp(-(std::pow(dist, 2)) / (2 * std::pow(fwhm / 2.355, 2))));
+}
+
 void build_otf_table(const fsim_sim_param* p, OtfTable* t) {
   t->cutoff = 1000 / (p->em_wavelength / p->na / 2);
   t->cycles_per_sample = t->cutoff / OTF_SAMPLES;
   t->vec_cpm = 1 / (p->w * p->microns_per_pixel);
+  t->measured = otf_measured(p) ? 1 : 0;
+  t->multi_band = 0;
+  t->n_bands = t->n_samples = 0;
+  if (t->measured) {
+    // loadFromConfig with band data, then setAttenuation per band (java:588-621, 276-287)
+    t->cycles_per_sample = p->otf_cycles;
+    t->n_bands = p->otf_bands;
+    t->n_samples = p->otf_samples;
+    t->multi_band = p->otf_bands > 1;
+    for (int b = 0; b < t->n_bands; b++)
+      for (int v = 0; v < t->n_samples; v++) {
+        const float re = p->otf_data[2 * ((size_t)b * t->n_samples + v)];
+        const float im = p->otf_data[2 * ((size_t)b * t->n_samples + v) + 1];
+        const float a = val_attenuation(v * t->cycles_per_sample, p->att_strength, p->att_fwhm);
+        t->mvals[b][v] = make_float2(re, im);
+        t->monly_att[b][v] = a;
+        t->mvals_att[b][v] = make_float2(re * a, im * a);
+      }
+  }
   for (int i = 0; i < OTF_SAMPLES; i++) {
     double v = i / (double)OTF_SAMPLES;
     t->vals[i] = (float)(ideal_otf_host(v) * std::pow(p->otf_a, v));
@@ -36,12 +60,26 @@ void build_otf_table(const fsim_sim_param* p, OtfTable* t) {
 }
 
 // ---- kernels ------------------------------------------------------------------------
-__global__ void k_otf_to_vector(float2* __restrict__ v, int w, int h, const OtfTable* __restrict__ t, double kx,
-                                double ky, int att, int write) {
+__global__ void k_otf_to_vector(float2* __restrict__ v, int w, int h, const OtfTable* __restrict__ t, int band,
+                                double kx, double ky, int att, int write) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   if (x >= w) return;
-  float val;
   size_t i = (size_t)y * w + x;
+  if (t->measured) {
+    float2 c;
+    if (!otf_at_c(*t, band, (double)freq_x(x, w), (double)freq_y(y, h), kx, ky, att != 0, &c)) {
+      v[i] = make_float2(0.f, 0.f);
+    } else if (write) {
+      v[i] = c;
+    } else {  // Cplx.Float.mult(a, c.conj())
+      const float2 a = v[i];
+      const float cr = c.x, ci = -c.y;
+      v[i] = make_float2(__fsub_rn(__fmul_rn(a.x, cr), __fmul_rn(a.y, ci)),
+                         __fadd_rn(__fmul_rn(a.x, ci), __fmul_rn(a.y, cr)));
+    }
+    return;
+  }
+  float val;
   if (!otf_at(*t, (double)freq_x(x, w), (double)freq_y(y, h), kx, ky, att != 0, &val)) {
     v[i] = make_float2(0.f, 0.f);
   } else if (write) {
@@ -98,11 +136,22 @@ __global__ void k_wiener_denominator(float* __restrict__ out, int W, int H, cons
       const double kx = shifts.px[d] * b, ky = shifts.py[d] * b;
       double r1 = __dmul_rn(d_hypot_java(__dsub_rn(xh, kx), __dsub_rn(yh, ky)), cpm);
       double r2 = __dmul_rn(d_hypot_java(__dadd_rn(xh, kx), __dadd_rn(yh, ky)), cpm);
-      float o1 = otf_val(*t, r1, false), o2 = otf_val(*t, r2, false);
-      float v1 = __fmul_rn(o1, o1), v2 = __fmul_rn(o2, o2);
-      if (use_att) {
-        v1 = __fmul_rn(v1, att_val(*t, r1));
-        v2 = __fmul_rn(v2, att_val(*t, r2));
+      float v1, v2;
+      if (t->measured) {  // Cplx.Float.absSq of the band's value
+        v1 = abs_sq(otf_val_c(*t, b, r1, false));
+        v2 = abs_sq(otf_val_c(*t, b, r2, false));
+        if (use_att) {
+          v1 = __fmul_rn(v1, att_val_b(*t, b, r1));
+          v2 = __fmul_rn(v2, att_val_b(*t, b, r2));
+        }
+      } else {
+        float o1 = otf_val(*t, r1, false), o2 = otf_val(*t, r2, false);
+        v1 = __fmul_rn(o1, o1);
+        v2 = __fmul_rn(o2, o2);
+        if (use_att) {
+          v1 = __fmul_rn(v1, att_val(*t, r1));
+          v2 = __fmul_rn(v2, att_val(*t, r2));
+        }
       }
       acc = __fadd_rn(__fadd_rn(acc, v1), v2);
     }
@@ -140,7 +189,10 @@ int upload_otf_table(const fsim_sim_param* p, OtfTable** dev, cudaStream_t st) {
   if (!host) FSIM_CUDA(cudaMallocHost(&host, sizeof(OtfTable)));
   const double k[7] = {p->na, p->em_wavelength, p->otf_a, p->att_strength, p->att_fwhm, (double)p->w,
                        p->microns_per_pixel};
-  bool same = true;
+  // estimates are cached by their parameters; measured tables (whose samples the key does
+  // not cover) are rebuilt on every call and leave the cache invalid
+  const bool measured = otf_measured(p);
+  bool same = !measured;
   for (int i = 0; i < 7; i++) same = same && (k[i] == key[i]);
   if (!same) {
     // wait for the previous user of the staging copy before overwriting it
@@ -148,7 +200,7 @@ int upload_otf_table(const fsim_sim_param* p, OtfTable** dev, cudaStream_t st) {
     build_otf_table(p, host);
     FSIM_CUDA(cudaMemcpyAsync(buf, host, sizeof(OtfTable), cudaMemcpyHostToDevice, st ? st : c.stream));
     FSIM_CUDA(cudaStreamSynchronize(st ? st : c.stream));
-    for (int i = 0; i < 7; i++) key[i] = k[i];
+    for (int i = 0; i < 7; i++) key[i] = measured ? std::nan("") : k[i];
   }
   *dev = buf;
   return FSIM_OK;
@@ -189,10 +241,10 @@ int att_device(float* out, int w, int h, double vec_cpm, double str, double fwhm
   return FSIM_OK;
 }
 
-int otf_vector_device(float2* v, int w, int h, const OtfTable* t, double kx, double ky, bool att, bool write,
+int otf_vector_device(float2* v, int w, int h, const OtfTable* t, int band, double kx, double ky, bool att, bool write,
                       cudaStream_t st) {
   dim3 g(div_up(w, 128), h);
-  k_otf_to_vector<<<g, 128, 0, st>>>(v, w, h, t, kx, ky, att ? 1 : 0, write ? 1 : 0);
+  k_otf_to_vector<<<g, 128, 0, st>>>(v, w, h, t, band, kx, ky, att ? 1 : 0, write ? 1 : 0);
   FSIM_CHECK_LAUNCH();
   return FSIM_OK;
 }
@@ -225,7 +277,8 @@ int fsim_otf_to_vector(fsim_vec* v, const fsim_sim_param* p, int band, double kx
   OtfTable* t;
   rc = upload_otf_table(p, &t, ctx().stream);
   if (rc) return rc;
-  return otf_vector_device(reinterpret_cast<float2*>(v->d), v->w, v->h, t, kx, ky, use_att != 0, write != 0, ctx().stream);
+  return otf_vector_device(reinterpret_cast<float2*>(v->d), v->w, v->h, t, band, kx, ky, use_att != 0, write != 0,
+                           ctx().stream);
 }
 
 int fsim_apo_vector(fsim_vec* v, const fsim_sim_param* p, double bend, double cutoff) {

@@ -26,7 +26,8 @@ int wiener_denominator_device(float* out, const fsim_sim_param* p, double wiener
                               cudaStream_t st);
 int apo_device(float* out, int cplx, int W, int H, double vec_cpm, double cutoff_abs, double bend, cudaStream_t st);
 int att_device(float* out, int w, int h, double vec_cpm, double str, double fwhm, double kx, double ky, cudaStream_t st);
-int otf_vector_device(float2* v, int w, int h, const OtfTable* t, double kx, double ky, bool att, bool write,
+// otfToVector of band `band` (measured multi-band OTFs; estimates have one band)
+int otf_vector_device(float2* v, int w, int h, const OtfTable* t, int band, double kx, double ky, bool att, bool write,
                       cudaStream_t st);
 int separate_device(const SepArgs& a, size_t n, cudaStream_t st);
 

@@ -12,19 +12,27 @@
 
 namespace fsim {
 
-constexpr int OTF_SAMPLES = 512;  // OtfProvider.samplesLateral for estimates
+constexpr int OTF_SAMPLES = 512;          // OtfProvider.samplesLateral for estimates
+constexpr int OTF_MAX_MEASURED = 1024;    // samples per band of a measured OTF
 
 struct OtfTable {
   double cutoff;          // cycles/micron, 1000/(lambda/na/2)
-  double cycles_per_sample;  // OtfProvider.cyclesPerMicron = cutoff/512
+  double cycles_per_sample;  // OtfProvider.cyclesPerMicron (estimates: cutoff/512)
   double vec_cpm;         // vector pixel size (SimParam cyclesPerMicron = 1/(w*pxl))
-  float vals[OTF_SAMPLES];
+  float vals[OTF_SAMPLES];   // estimate: one real band
   float vals_att[OTF_SAMPLES];
   float only_att[OTF_SAMPLES];
+  // measured OTF (OtfProvider.loadFromConfig with band data): complex bands
+  int measured, multi_band, n_bands, n_samples;
+  float2 mvals[FSIM_MAX_BANDS][OTF_MAX_MEASURED];
+  float2 mvals_att[FSIM_MAX_BANDS][OTF_MAX_MEASURED];
+  float monly_att[FSIM_MAX_BANDS][OTF_MAX_MEASURED];
 };
 
-// host: OtfProvider.fromEstimate + setAttenuation (OtfProvider.java:96-127, 276-287)
+// host: OtfProvider.fromEstimate or the measured bands, + setAttenuation
+// (OtfProvider.java:96-127, 588-621, 276-287)
 void build_otf_table(const fsim_sim_param* p, OtfTable* t);
+inline bool otf_measured(const fsim_sim_param* p) { return p->otf_data && p->otf_samples > 0; }
 double ideal_otf_host(double d);
 
 __device__ __forceinline__ double d_hypot_java(double x, double y) {  // MTool.fhypot
@@ -50,6 +58,35 @@ __device__ __forceinline__ float att_val(const OtfTable& t, double cycl) {
   const float v = t.only_att[l];
   return __fadd_rn(__fmul_rn(v, f), __fmul_rn(v, __fsub_rn(1.f, f)));
 }
+// Band-aware complex lookups (measured OTFs; estimates give (otf_val, 0)): getOtfVal with
+// the band index (bands collapse to 0 unless the OTF is multi-band) and the floor-indexed
+// v*(1-f) + v*f per component (Cplx.add(v.mult(1-f), v.mult(f)))
+__device__ __forceinline__ float2 otf_val_c(const OtfTable& t, int band, double cycl, bool att) {
+  if (!t.measured) return make_float2(otf_val(t, cycl, att), 0.f);
+  if (!t.multi_band) band = 0;
+  if (cycl >= t.cutoff) return make_float2(0.f, 0.f);
+  const double pos = cycl / t.cycles_per_sample;
+  if (ceil(pos) >= (double)t.n_samples) return make_float2(0.f, 0.f);
+  const int l = (int)floor(pos);
+  const float f = (float)(pos - (double)l), g = __fsub_rn(1.f, f);
+  const float2 v = att ? t.mvals_att[band][l] : t.mvals[band][l];
+  return make_float2(__fadd_rn(__fmul_rn(v.x, g), __fmul_rn(v.x, f)), __fadd_rn(__fmul_rn(v.y, g), __fmul_rn(v.y, f)));
+}
+// getAttVal with the band index; a position beyond a measured table (the reference indexes
+// outside its arrays there) reads as no attenuation
+__device__ __forceinline__ float att_val_b(const OtfTable& t, int band, double cycl) {
+  if (!t.measured) return att_val(t, cycl);
+  if (!t.multi_band) band = 0;
+  if (cycl >= t.cutoff) return 1.f;
+  const double pos = cycl / t.cycles_per_sample;
+  const int l = (int)floor(pos);
+  if (l >= t.n_samples) return 1.f;
+  const float f = (float)(pos - (double)l);
+  const float v = t.monly_att[band][l];
+  return __fadd_rn(__fmul_rn(v, f), __fmul_rn(v, __fsub_rn(1.f, f)));
+}
+__device__ __forceinline__ float abs_sq(float2 v) { return __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y)); }
+
 // otfToVector's per-pixel value at frequency (xh, yh) for an OTF centred at (kx, ky);
 // returns false where the reference writes zero (cycl > cutOff).
 __device__ __forceinline__ bool otf_at(const OtfTable& t, double xh, double yh, double kx, double ky, bool att,
@@ -58,6 +95,15 @@ __device__ __forceinline__ bool otf_at(const OtfTable& t, double xh, double yh, 
   const double cycl = __dmul_rn(rad, t.vec_cpm);
   if (cycl > t.cutoff) return false;
   *val = otf_val(t, cycl, att);
+  return true;
+}
+
+__device__ __forceinline__ bool otf_at_c(const OtfTable& t, int band, double xh, double yh, double kx, double ky,
+                                         bool att, float2* val) {
+  const double rad = d_hypot_java(__dsub_rn(xh, kx), __dsub_rn(yh, ky));
+  const double cycl = __dmul_rn(rad, t.vec_cpm);
+  if (cycl > t.cutoff) return false;
+  *val = otf_val_c(t, band, cycl, att);
   return true;
 }
 

@@ -194,6 +194,8 @@ int fsim_plan_create(fsim_plan** out, const fsim_sim_param* p, int path, int inp
   FSIM_REQUIRE(p->nr_phases <= FSIM_MAX_PHASES && 2 * p->nr_bands - 1 <= 7, FSIM_EINVAL, "too many phases/bands");
   FSIM_REQUIRE(p->filter_style == FSIM_FILTER_WIENER, FSIM_EINVAL,
                "fused plans apply the Wiener filter; RL filter styles run through fsim_run_reconstruction");
+  FSIM_REQUIRE(!otf_measured(p), FSIM_EINVAL,
+               "fused plans take estimated OTFs; measured OTFs run through fsim_run_reconstruction");
   NEED_INIT();
   fsim_plan* pl = new fsim_plan();
   pl->prm = *p;
@@ -219,8 +221,8 @@ int fsim_plan_update(fsim_plan* plan, const fsim_sim_param* p) {
   FSIM_REQUIRE(p->w == plan->prm.w && p->nr_dirs == plan->prm.nr_dirs && p->nr_bands == plan->prm.nr_bands &&
                    p->nr_phases == plan->prm.nr_phases,
                FSIM_EINVAL, "plan_update: geometry (size, dirs, bands, phases) must not change");
-  FSIM_REQUIRE(p->filter_style == FSIM_FILTER_WIENER, FSIM_EINVAL,
-               "fused plans apply the Wiener filter; RL filter styles run through fsim_run_reconstruction");
+  FSIM_REQUIRE(p->filter_style == FSIM_FILTER_WIENER && !otf_measured(p), FSIM_EINVAL,
+               "fused plans apply the Wiener filter with an estimated OTF");
   // callers may have work in flight that reads the old tables
   FSIM_CUDA(cudaDeviceSynchronize());
   plan->prm = *p;

@@ -164,6 +164,15 @@ int validate_param(const fsim_sim_param* p) {
     set_error("SimParam: bad image size %d / pixel size %g", p->w, p->microns_per_pixel);
     return FSIM_EINVAL;
   }
+  if (p->otf_data && p->otf_samples > 0) {
+    // measured OTF: getOtfVal throws for a band beyond a multi-band table (OtfProvider.java:192-193)
+    if (p->otf_bands < 1 || p->otf_bands > FSIM_MAX_BANDS || p->otf_samples > 1024 || !(p->otf_cycles > 0) ||
+        (p->otf_bands > 1 && p->nr_bands > p->otf_bands)) {
+      set_error("SimParam: bad measured OTF (%d bands, %d samples, %g cycles/micron per sample)", p->otf_bands,
+                p->otf_samples, p->otf_cycles);
+      return FSIM_EINVAL;
+    }
+  }
   if (p->filter_style < FSIM_FILTER_WIENER || p->filter_style > FSIM_FILTER_RL_BOTH ||
       (p->filter_style != FSIM_FILTER_WIENER && p->rl_iterations < 0)) {
     set_error("SimParam: bad filter style %d / RL iterations %d", p->filter_style, p->rl_iterations);

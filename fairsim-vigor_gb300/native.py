@@ -9,6 +9,8 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
+
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libfairsim_gb300.so")
 HEADER = os.path.join(_HERE, "..", "include", "fairsim_gb300.h")
@@ -75,6 +77,10 @@ class SimParamC(C.Structure):
         ("phases", (C.c_double * MAXP) * MAXD),
         ("filter_style", C.c_int32),
         ("rl_iterations", C.c_int32),
+        ("otf_data", C.c_void_p),
+        ("otf_bands", C.c_int32),
+        ("otf_samples", C.c_int32),
+        ("otf_cycles", C.c_double),
     ]
 
 
@@ -144,10 +150,14 @@ def to_c_param(p) -> SimParamC:
     """SimParam mirror (or dict) -> the C record."""
     g = (lambda k: p[k]) if isinstance(p, dict) else (lambda k: getattr(p, k))
     otf = None if isinstance(p, dict) else p.otf()
-    if otf is not None and not getattr(otf, "isEstimate", True):
-        raise NotImplementedError("measured (data) OTFs are not supported by the device path; "
-                                  "only OtfProvider.fromEstimate OTFs are")
     c = SimParamC()
+    m = getattr(otf, "measured", None) if otf is not None else None
+    if m is not None:  # measured OTF bands (OtfProvider.loadFromConfig with data)
+        arr = np.ascontiguousarray([[(z.real, z.imag) for z in band] for band in m["bands"]], dtype=np.float32)
+        c._keep = arr  # the record points into it; it lives as long as the record
+        c.otf_data = arr.ctypes.data
+        c.otf_bands, c.otf_samples = arr.shape[0], arr.shape[1]
+        c.otf_cycles = float(m["cycles"])
     c.w = g("w")
     c.nr_dirs, c.nr_bands, c.nr_phases = g("nrDirs"), g("nrBands"), g("nrPhases")
     c.microns_per_pixel = g("micronsPerPixel")

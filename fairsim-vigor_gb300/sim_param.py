@@ -66,6 +66,18 @@ class OtfProvider:
     measured = None  # dict(bands=[[complex, ...], ...], cycles=float) or None
 
     @staticmethod
+    def fromMeasured(na: float, em_wavelength: float, bands, cycles_per_sample: float) -> "OtfProvider":
+        """A measured OTF as loadFromConfig builds it from band data (S/OtfProvider.java:588-621):
+        ``bands`` holds one sequence of complex samples per band, ``cycles_per_sample`` their
+        spacing in cycles/micron; attenuation defaults 0.99 / 1.2, switched off."""
+        ret = OtfProvider.__new__(OtfProvider)
+        ret.na, ret.emWavelength, ret.a = float(na), float(em_wavelength), 1.0
+        ret.attStrength, ret.attFWHM, ret.useAttenuation = 0.99, 1.2, False
+        ret.isEstimate = False
+        ret.measured = dict(bands=[[complex(z) for z in b] for b in bands], cycles=float(cycles_per_sample))
+        return ret
+
+    @staticmethod
     def loadFromConfig(cfg) -> "OtfProvider":
         """OtfProvider.loadFromConfig (S/OtfProvider.java:575-633): the "otf2d" folder;
         an estimate (NA, emission, a-estimate) or measured band data, then attenuation."""
@@ -76,19 +88,14 @@ class OtfProvider:
             ret = OtfProvider.fromEstimate(fld.getDbl("NA").val(), fld.getInt("emission").val(),
                                            fld.getDbl("a-estimate").val())
         else:
-            ret = OtfProvider.__new__(OtfProvider)
-            ret.na = fld.getDbl("NA").val()
-            ret.emWavelength = float(fld.getInt("emission").val())
-            ret.a = 1.0
-            ret.attStrength, ret.attFWHM, ret.useAttenuation = 0.99, 1.2, False
             data = fld.cd("data")
             nb, ns = data.getInt("bands").val(), data.getInt("samples").val()
             bands = []
             for b in range(nb):
                 v = from_bytes(data.getData("band-%d" % b).val())
                 bands.append([complex(v[2 * i], v[2 * i + 1]) for i in range(ns)])
-            ret.isEstimate = False
-            ret.measured = dict(bands=bands, cycles=data.getDbl("cycles").val())
+            ret = OtfProvider.fromMeasured(fld.getDbl("NA").val(), fld.getInt("emission").val(), bands,
+                                           data.getDbl("cycles").val())
         if fld.contains("attenuation"):
             att = fld.cd("attenuation")
             ret.setAttenuation(att.getDbl("strength").val(), att.getDbl("FWHM").val())

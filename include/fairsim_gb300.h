@@ -82,6 +82,14 @@ typedef struct fsim_sim_param {
    * SimParam.getRLiterations (the reference's default is 5) */
   int32_t filter_style;
   int32_t rl_iterations;
+  /* Measured OTF (OtfProvider.loadFromConfig with band data, OtfProvider.java:588-621):
+   * otf_bands x otf_samples complex values (re, im) in host memory, otf_cycles cycles/micron
+   * per sample; read when the call is made. NULL / 0 samples: OtfProvider.fromEstimate
+   * (na, em_wavelength, otf_a). The op-by-op path and the parameter fit take both; the fused
+   * plans take estimates only. */
+  const float* otf_data;
+  int32_t otf_bands, otf_samples; /* otf_samples <= 1024 */
+  double otf_cycles;
 } fsim_sim_param;
 #define FSIM_FILTER_WIENER 0
 #define FSIM_FILTER_RL_IN 1

@@ -628,12 +628,17 @@ inline T val_attenuation(double dist, double str, double fwhm) {
 
 template <class T>
 struct Otf {
-  static constexpr int samples = 512;
+  // estimates: one real band of 512 samples up to the cutoff (OtfProvider.fromEstimate,
+  // S/OtfProvider.java:96-127); measured: maxBand complex bands of samplesLateral samples at
+  // cyclesPerMicron spacing (loadFromConfig with band data, :588-621)
   double na = 0, lambda = 0, cutOff = 0, cyclesPerMicron = 0, a = 1;
   double attStrength = .99, attFWHM = 1.2;
   bool useAtt = false;
+  bool isMultiBand = false;
+  int maxBand = 1, samplesLateral = 512;
   double vecCyclesPerMicron = -1;
-  std::vector<T> vals, valsAtt, valsOnlyAtt;  // vals are real (estimate)
+  std::vector<std::vector<C<T>>> vals, valsAtt;
+  std::vector<std::vector<T>> valsOnlyAtt;
 
   static Otf fromEstimate(double na, double lambda, double a) {
     if (a < 0 || a > 1 || na < 0.3 || na > 2.2 || lambda < 300 || lambda > 1500)
@@ -643,51 +648,83 @@ struct Otf {
     o.lambda = lambda;
     o.a = a;
     o.cutOff = 1000 / (lambda / na / 2);
-    o.cyclesPerMicron = o.cutOff / samples;
-    o.vals.resize(samples);
-    o.valsAtt.resize(samples);
-    o.valsOnlyAtt.resize(samples);
-    for (int i = 0; i < samples; i++) {
-      double v = i / (double)samples;
-      o.vals[i] = rnd<T>(val_ideal_otf(v) * std::pow(a, v));
+    o.samplesLateral = 512;
+    o.cyclesPerMicron = o.cutOff / o.samplesLateral;
+    o.alloc(1);
+    for (int i = 0; i < o.samplesLateral; i++) {
+      double v = i / (double)o.samplesLateral;
+      o.vals[0][i] = {rnd<T>(val_ideal_otf(v) * std::pow(a, v)), T(0)};
     }
     o.setAttenuation(o.attStrength, o.attFWHM);
     o.useAtt = false;
     return o;
   }
-  void setAttenuation(double str, double fwhm) {
+  // loadFromConfig with a "data" folder: data = bands x samples complex (re, im) floats
+  static Otf fromData(double na, double lambda, int bands, int samples, double cycles, const float* data) {
+    if (bands < 1 || samples < 1 || cycles <= 0) throw std::runtime_error("bad OTF data");
+    Otf o;
+    o.na = na;
+    o.lambda = lambda;
+    o.cutOff = 1000 / (lambda / na / 2);
+    o.samplesLateral = samples;
+    o.cyclesPerMicron = cycles;
+    o.isMultiBand = bands > 1;
+    o.alloc(bands);
+    for (int b = 0; b < bands; b++)
+      for (int i = 0; i < samples; i++)
+        o.vals[b][i] = {(T)data[2 * ((size_t)b * samples + i)], (T)data[2 * ((size_t)b * samples + i) + 1]};
+    o.setAttenuation(o.attStrength, o.attFWHM);
+    o.useAtt = false;
+    return o;
+  }
+  void alloc(int bands) {
+    maxBand = bands;
+    vals.assign(bands, std::vector<C<T>>(samplesLateral));
+    valsAtt.assign(bands, std::vector<C<T>>(samplesLateral));
+    valsOnlyAtt.assign(bands, std::vector<T>(samplesLateral));
+  }
+  void setAttenuation(double str, double fwhm) {  // :276-287
     attStrength = str;
     attFWHM = fwhm;
-    for (int v = 0; v < samples; v++) {
-      double dist = v * cyclesPerMicron;
-      valsOnlyAtt[v] = val_attenuation<T>(dist, attStrength, attFWHM);
-      valsAtt[v] = vals[v] * valsOnlyAtt[v];
-    }
+    for (int b = 0; b < maxBand; b++)
+      for (int v = 0; v < samplesLateral; v++) {
+        double dist = v * cyclesPerMicron;
+        valsOnlyAtt[b][v] = val_attenuation<T>(dist, attStrength, attFWHM);
+        valsAtt[b][v] = {vals[b][v].re * valsOnlyAtt[b][v], vals[b][v].im * valsOnlyAtt[b][v]};
+      }
+  }
+  int bandIdx(int band) const {
+    if (!isMultiBand) band = 0;
+    if (band >= maxBand || band < 0) throw std::runtime_error("band idx too high or <0");
+    return band;
   }
   // getOtfVal: floor-indexed, "interpolation" weights both on lPos (S/OtfProvider.java:189-222)
-  T getOtfVal(double cycl, bool att) const {
-    if (cycl >= cutOff) return 0;
+  C<T> getOtfVal(int band, double cycl, bool att) const {
+    band = bandIdx(band);
+    if (cycl < 0) throw std::runtime_error("cylc negative!");
+    if (cycl >= cutOff) return {0, 0};
     const double pos = cycl / cyclesPerMicron;
-    if (std::ceil(pos) >= samples) return 0;
+    if (std::ceil(pos) >= samplesLateral) return {0, 0};
     int lPos = (int)std::floor(pos);
     T f = (T)(pos - lPos);
-    T v = att ? valsAtt[lPos] : vals[lPos];
-    T retl = v * (T(1) - f);
-    T reth = v * f;
-    return retl + reth;
+    C<T> v = att ? valsAtt[band][lPos] : vals[band][lPos];
+    T g = T(1) - f;
+    return {v.re * g + v.re * f, v.im * g + v.im * f};  // Cplx.add(v.mult(1-f), v.mult(f))
   }
-  T getAttVal(double cycl) const {
+  // getAttVal (:246-269); beyond the table the reference indexes out of its arrays
+  T getAttVal(int band, double cycl) const {
+    band = bandIdx(band);
     if (cycl >= cutOff) return T(1);
     double pos = cycl / cyclesPerMicron;
     int lPos = (int)std::floor(pos);
+    if (lPos >= samplesLateral) throw std::runtime_error("attenuation beyond the OTF table");
     T f = (T)(pos - lPos);
-    T retl = valsOnlyAtt[lPos] * f;
-    T reth = valsOnlyAtt[lPos] * (T(1) - f);
+    T retl = valsOnlyAtt[band][lPos] * f;
+    T reth = valsOnlyAtt[band][lPos] * (T(1) - f);
     return retl + reth;
   }
-  // otfToVector (S/OtfProvider.java:331-373). The OTF is real, so conj(val) = val
-  // and the complex multiply reduces to Cplx.Float.mult with im 0 (same float ops).
-  void otfToVector(CVec<T>& vec, double kx, double ky, bool att, bool write) const {
+  // otfToVector (S/OtfProvider.java:331-373): write the OTF, or multiply by its conjugate
+  void otfToVector(CVec<T>& vec, int band, double kx, double ky, bool att, bool write) const {
     if (vecCyclesPerMicron <= 0) throw std::runtime_error("Vector pixel size not initialized");
     const int w = vec.w, h = vec.h;
     pfor(0, h, [&](int y) {
@@ -699,22 +736,24 @@ struct Otf {
         if (cycl > cutOff) {
           vec.set(x, y, {0, 0});
         } else {
-          T val = getOtfVal(cycl, att);
+          C<T> val = getOtfVal(band, cycl, att);
           if (!write) {
             C<T> a = vec.get(x, y);
-            C<T> b{val, -T(0)};  // conj of (val, 0)
+            C<T> b{val.re, -val.im};  // val.conj()
             vec.set(x, y, cmul(a, b));
           } else {
-            vec.set(x, y, {val, 0});
+            vec.set(x, y, val);
           }
         }
       }
     });
   }
-  void applyOtf(CVec<T>& vec, double kx, double ky) const { otfToVector(vec, kx, ky, useAtt, false); }
-  void writeOtfVector(CVec<T>& vec, double kx, double ky) const { otfToVector(vec, kx, ky, false, true); }
-  void writeOtfWithAttVector(CVec<T>& vec, double kx, double ky) const {
-    otfToVector(vec, kx, ky, useAtt, true);
+  void applyOtf(CVec<T>& vec, int band, double kx, double ky) const { otfToVector(vec, band, kx, ky, useAtt, false); }
+  void writeOtfVector(CVec<T>& vec, int band, double kx, double ky) const {
+    otfToVector(vec, band, kx, ky, false, true);
+  }
+  void writeOtfWithAttVector(CVec<T>& vec, int band, double kx, double ky) const {
+    otfToVector(vec, band, kx, ky, useAtt, true);
   }
   // writeApoVector, real form (S/OtfProvider.java:469-492)
   void writeApoVector(RVec<T>& vec, double bend, double cutoffFac) const {
@@ -824,11 +863,11 @@ inline void add_wiener_denominator(const SimParam<T>& sp, RVec<T>& vec, int d, i
       double yh = (y < h / 2) ? -y : h - y;
       double rad1 = fhypot(xh - dir.px(b), yh - dir.py(b)) * cyclMicron;
       double rad2 = fhypot(xh + dir.px(b), yh + dir.py(b)) * cyclMicron;
-      T o1 = sp.otf.getOtfVal(rad1, false), o2 = sp.otf.getOtfVal(rad2, false);
-      T v1 = o1 * o1, v2 = o2 * o2;  // Cplx.Float.absSq with im 0
+      C<T> o1 = sp.otf.getOtfVal(b, rad1, false), o2 = sp.otf.getOtfVal(b, rad2, false);
+      T v1 = o1.re * o1.re + o1.im * o1.im, v2 = o2.re * o2.re + o2.im * o2.im;  // Cplx.Float.absSq
       if (useAtt) {
-        v1 *= sp.otf.getAttVal(rad1);
-        v2 *= sp.otf.getAttVal(rad2);
+        v1 *= sp.otf.getAttVal(b, rad1);
+        v2 *= sp.otf.getAttVal(b, rad2);
       }
       vec.at(x, y) = vec.at(x, y) + v1 + v2;
     }
@@ -952,7 +991,7 @@ inline RVec<T> run_reconstruction(const SimParam<T>& param, const std::vector<st
   CVec<T> inputOtf;  // zero-band OTF for RL on the input (:313-321)
   if (param.useRLonInput()) {
     inputOtf = CVec<T>(w, h);
-    otf.writeOtfVector(inputOtf, 0, 0);
+    otf.writeOtfVector(inputOtf, 0, 0, 0);
   }
   for (int a = 0; a < param.nrDirs; a++) {
     const Dir& par = param.dirs[a];
@@ -969,7 +1008,7 @@ inline RVec<T> run_reconstruction(const SimParam<T>& param, const std::vector<st
       separate_bands(inFFT[a], sep, par.getPhases(), par.nrBands, par.getModulations());
     }
     if (otfBeforeShift && useWiener)
-      for (int i = 0; i < nc; i++) otf.applyOtf(sep[i], 0, 0);
+      for (int i = 0; i < nc; i++) otf.applyOtf(sep[i], (i + 1) / 2, 0, 0);
     std::vector<CVec<T>> shifted(std::max(5, nc), CVec<T>(2 * w, 2 * h));
     paste_freq(shifted[0], sep[0], 0, 0);
     for (int b = 1; b < par.nrBands; b++) {
@@ -980,11 +1019,11 @@ inline RVec<T> run_reconstruction(const SimParam<T>& param, const std::vector<st
       sim_fourier_shift(shifted[neg], -par.px(b), -par.py(b));
     }
     if (useWiener && !otfBeforeShift) {
-      otf.applyOtf(shifted[0], 0, 0);
+      otf.applyOtf(shifted[0], 0, 0, 0);
       for (int b = 1; b < par.nrBands; b++) {
         int pos = b * 2, neg = b * 2 - 1;
-        otf.applyOtf(shifted[pos], par.px(b), par.py(b));
-        otf.applyOtf(shifted[neg], -par.px(b), -par.py(b));
+        otf.applyOtf(shifted[pos], b, par.px(b), par.py(b));
+        otf.applyOtf(shifted[neg], b, -par.px(b), -par.py(b));
       }
     } else if (useWiener) {
       // the reference passes (angIdx, component) as the mask centre (S/SimAlgorithm.java:407-409)
@@ -1000,8 +1039,8 @@ inline RVec<T> run_reconstruction(const SimParam<T>& param, const std::vector<st
     for (int a = 0; a < param.nrDirs; a++) {
       const Dir& par = param.dirs[a];
       for (int b = 0; b < par.nrBands; b++) {
-        otf.writeOtfVector(pos, par.px(b), par.py(b));
-        otf.writeOtfVector(neg, -par.px(b), -par.py(b));
+        otf.writeOtfVector(pos, b, par.px(b), par.py(b));
+        otf.writeOtfVector(neg, b, -par.px(b), -par.py(b));
         if (b == 0) {
           v_scal(pos, rnd<T>(1.0 / param.nrDirs));
           v_add(otfSim, pos);
@@ -1072,10 +1111,10 @@ inline void widefield_outputs(const SimParam<T>& param, const std::vector<std::v
   if (param.useRLonOutput()) {
     // RL styles: the widefield deconvolved with the zero-order OTF (S/SimAlgorithm.java:669-672)
     CVec<T> zeroOrderOtf(2 * w, 2 * h);
-    param.otf.writeOtfVector(zeroOrderOtf, 0, 0);
+    param.otf.writeOtfVector(zeroOrderOtf, 0, 0, 0);
     rl_deconvolve(low, zeroOrderOtf, param.rlIterations, true);
   } else {
-    param.otf.otfToVector(low, 0, 0, false, false);
+    param.otf.otfToVector(low, 0, 0, 0, false, false);
     v_times_real(low, widefield_denominator(param, param.wiener));
     param.otf.maskOtf(low, 0, 0);
   }
@@ -1107,14 +1146,14 @@ inline C<double> auto_correlation(const CVec<T>& inV, double kx, double ky) {
 // Correlation (S/Correlation.java:43-288)
 // ---------------------------------------------------------------------------
 template <class T>
-inline void common_region(CVec<T>& band0, CVec<T>& band1, const Otf<T>& otf, double kx, double ky,
+inline void common_region(CVec<T>& band0, CVec<T>& band1, int bn0, int bn1, const Otf<T>& otf, double kx, double ky,
                           double dist, double weightLimit, bool divideByOtf) {
   const int w = band0.w, h = band0.h;
   CVec<T> weight0(w, h), weight1(w, h), wt0(w, h), wt1(w, h);
-  otf.writeOtfVector(weight0, 0, 0);
-  otf.writeOtfVector(weight1, 0, 0);
-  otf.writeOtfVector(wt0, kx, ky);
-  otf.writeOtfVector(wt1, -kx, -ky);
+  otf.writeOtfVector(weight0, bn0, 0, 0);
+  otf.writeOtfVector(weight1, bn1, 0, 0);
+  otf.writeOtfVector(wt0, bn0, kx, ky);
+  otf.writeOtfVector(wt1, bn1, -kx, -ky);
   for (int y = 0; y < h; y++)
     for (int x = 0; x < w; x++) {
       double rad = std::sqrt((double)(((x < w / 2) ? (x * x) : ((x - w) * (x - w))) +
@@ -1168,12 +1207,12 @@ inline void locate_peak(const CVec<T>& vec, double kMin, double out[4]) {
 // fitPeak: 3 iterations of a 10x10 grid search (S/Correlation.java:43-136).
 // grid_out (optional) receives 3*100*2 doubles: corr[iter][yi][xi] (re,im).
 template <class T>
-inline void fit_peak(const CVec<T>& band0, const CVec<T>& band1, const Otf<T>& otf, double kx, double ky,
-                     double weightLimit, double search, double out[4], double* grid_out = nullptr) {
+inline void fit_peak(const CVec<T>& band0, const CVec<T>& band1, int bn0, int bn1, const Otf<T>& otf, double kx,
+                     double ky, double weightLimit, double search, double out[4], double* grid_out = nullptr) {
   double resPhase = 0, resMag = 0;
   for (int iter = 0; iter < 3; iter++) {
     CVec<T> b0 = band0, b1 = band1;
-    common_region(b0, b1, otf, kx, ky, 0.15, weightLimit, true);
+    common_region(b0, b1, bn0, bn1, otf, kx, ky, 0.15, weightLimit, true);
     fft2d(b0, true);
     fft2d(b1, true);
     C<double> corr[10][10];
@@ -1217,10 +1256,10 @@ inline void fit_peak(const CVec<T>& band0, const CVec<T>& band1, const Otf<T>& o
 
 // getPeak (S/Correlation.java:183-209)
 template <class T>
-inline C<double> get_peak(const CVec<T>& band0, const CVec<T>& band1, const Otf<T>& otf, double kx, double ky,
-                          double weightLimit) {
+inline C<double> get_peak(const CVec<T>& band0, const CVec<T>& band1, int bn0, int bn1, const Otf<T>& otf, double kx,
+                          double ky, double weightLimit) {
   CVec<T> b0 = band0, b1 = band1;
-  common_region(b0, b1, otf, kx, ky, 0.15, weightLimit, true);
+  common_region(b0, b1, bn0, bn1, otf, kx, ky, 0.15, weightLimit, true);
   fft2d(b0, true);
   fft2d(b1, true);
   fourier_shift(b1, kx, -ky);
@@ -1270,20 +1309,20 @@ inline void estimate_parameters(SimParam<T>& param, const std::vector<std::vecto
       coarse_out[2 * a + 1] = peak[1];
     }
     double fit[4];
-    fit_peak(sep[0], sep[fb], otfPr, -peak[0], -peak[1], 0.05, 2.5, fit);
+    fit_peak(sep[0], sep[fb], 0, fitBand, otfPr, -peak[0], -peak[1], 0.05, 2.5, fit);
     if (lb != hb) {
       if (fitBand == 1) {
         fit[0] *= 2;
         fit[1] *= 2;
       }
-      C<double> p1 = get_peak(sep[0], sep[lb], otfPr, fit[0] / 2, fit[1] / 2, 0.05);
-      C<double> p2 = get_peak(sep[0], sep[hb], otfPr, fit[0], fit[1], 0.05);
+      C<double> p1 = get_peak(sep[0], sep[lb], 0, 1, otfPr, fit[0] / 2, fit[1] / 2, 0.05);
+      C<double> p2 = get_peak(sep[0], sep[hb], 0, 2, otfPr, fit[0], fit[1], 0.05);
       dir.setPxPy(-fit[0], -fit[1]);
       dir.phaOff = std::atan2(p1.im, p1.re);
       dir.modul[1] = std::hypot(p1.re, p1.im);
       dir.modul[2] = std::hypot(p2.re, p2.im);
     } else {
-      C<double> p1 = get_peak(sep[0], sep[1], otfPr, fit[0], fit[1], 0.05);
+      C<double> p1 = get_peak(sep[0], sep[1], 0, 1, otfPr, fit[0], fit[1], 0.05);
       dir.setPxPy(-fit[0], -fit[1]);
       dir.phaOff = std::atan2(p1.im, p1.re);
       dir.modul[1] = std::hypot(p1.re, p1.im);
@@ -1318,7 +1357,7 @@ inline LiveFilters<T> live_setup_filters(SimParam<T>& sp, bool useAtt, double at
   f.otfV = CVec<T>(w, w);
   sp.otf.setAttenuation(attStr, attFWHM);
   sp.otf.useAtt = useAtt;
-  sp.otf.writeOtfWithAttVector(f.otfV, 0, 0);
+  sp.otf.writeOtfWithAttVector(f.otfV, 0, 0, 0);
   f.wien = wiener_denominator(sp, wienParam);
   f.apo = RVec<T>(2 * w, 2 * w);
   sp.otf.writeApoVector(f.apo, 1, 2);
@@ -1410,8 +1449,8 @@ inline void live_refit(SimParam<T>& sp, const uint16_t* raw, double* peaks_out =
     double peak[4];
     locate_peak(c1, minDist, peak);
     double fit[4];
-    fit_peak(sep[0], sep[hb], otfPr, -peak[0], -peak[1], 0.05, 2.5, fit);
-    C<double> p1 = get_peak(sep[0], sep[lb], otfPr, fit[0] / nBand, fit[1] / nBand, 0.05);
+    fit_peak(sep[0], sep[hb], 0, 1, otfPr, -peak[0], -peak[1], 0.05, 2.5, fit);
+    C<double> p1 = get_peak(sep[0], sep[lb], 0, 1, otfPr, fit[0] / nBand, fit[1] / nBand, 0.05);
     par.setPxPy(-fit[0], -fit[1]);
     par.phaOff = std::atan2(p1.im, p1.re);
     par.modul[1] = std::hypot(p1.re, p1.im);

@@ -45,6 +45,10 @@ class RefParam(C.Structure):
         ("phases", (C.c_double * MAXP) * MAXD),
         ("filterStyle", C.c_int),
         ("rlIterations", C.c_int),
+        ("otfData", C.c_void_p),
+        ("otfBands", C.c_int),
+        ("otfSamples", C.c_int),
+        ("otfCycles", C.c_double),
     ]
 
 
@@ -117,6 +121,14 @@ def make_param(p) -> RefParam:
         r.filterStyle, r.rlIterations = int(p.get("filterStyle", 0)), int(p.get("rlIterations", 5))
     else:
         r.filterStyle, r.rlIterations = int(getattr(p, "filterStyle", 0)), int(getattr(p, "rlIterations", 5))
+        otf = p.otf() if callable(getattr(p, "otf", None)) else None
+        m = getattr(otf, "measured", None) if otf is not None else None
+        if m is not None:  # measured OTF bands (OtfProvider.loadFromConfig with data)
+            arr = np.array([[(z.real, z.imag) for z in band] for band in m["bands"]], dtype=np.float32)
+            r._keep = arr
+            r.otfData = arr.ctypes.data
+            r.otfBands, r.otfSamples = arr.shape[0], arr.shape[1]
+            r.otfCycles = float(m["cycles"])
     return r
 
 
@@ -195,11 +207,13 @@ def separate_bands(p, d, spectra, dtype=np.float32):
     return from_interleaved(out)
 
 
-def otf_vector(p, vec, kx=0.0, ky=0.0, which=0, dtype=np.float32):
+def otf_vector(p, vec, kx=0.0, ky=0.0, which=0, dtype=np.float32, band=0):
+    """which: 0 writeOtfVector, 1 writeOtfWithAttVector, 2 applyOtf, 3 maskOtf (of `band`)."""
     r = make_param(p)
     d = as_cplx_planes(vec, dtype)
     h, w = d.shape[0], d.shape[1]
-    _chk(getattr(lib(), "ref_otf_vector_" + _suf(dtype))(C.byref(r), _ptr(d), w, h, C.c_double(kx), C.c_double(ky), which))
+    _chk(getattr(lib(), "ref_otf_vector_" + _suf(dtype))(C.byref(r), _ptr(d), w, h, C.c_double(kx), C.c_double(ky), which,
+                                                         int(band)))
     return from_interleaved(d)
 
 

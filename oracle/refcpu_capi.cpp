@@ -27,6 +27,9 @@ typedef struct {
   double phases[REF_MAXD][REF_MAXP];
   int filterStyle;   // SimParam.FilterStyle ordinal
   int rlIterations;
+  const float* otfData;  // measured OTF: otfBands x otfSamples complex (re, im); NULL = estimate
+  int otfBands, otfSamples;
+  double otfCycles;
 } ref_param;
 }
 
@@ -42,7 +45,9 @@ static ref::SimParam<T> make_param(const ref_param* p) {
   sp.apoCutOff = p->apoCutoff;
   sp.filterStyle = p->filterStyle;
   sp.rlIterations = p->rlIterations;
-  sp.otf = ref::Otf<T>::fromEstimate(p->na, p->lambda, p->otfA);
+  sp.otf = (p->otfData && p->otfSamples > 0)
+               ? ref::Otf<T>::fromData(p->na, p->lambda, p->otfBands, p->otfSamples, p->otfCycles, p->otfData)
+               : ref::Otf<T>::fromEstimate(p->na, p->lambda, p->otfA);
   sp.otf.setAttenuation(p->attStr, p->attFWHM);
   sp.otf.useAtt = p->useAtt != 0;
   sp.setPxlSize(p->w, p->micronsPerPixel);
@@ -211,14 +216,15 @@ int ref_matrix_inverse(const double* in, int n, double* out, int pseudo, int m) 
     })                                                                                                \
   }                                                                                                   \
   /* which: 0 writeOtfVector, 1 writeOtfWithAttVector, 2 applyOtf (multiply), 3 maskOtf */            \
-  int ref_otf_vector_##SUF(const ref_param* p, T* vec, int vw, int vh, double kx, double ky, int which) { \
+  int ref_otf_vector_##SUF(const ref_param* p, T* vec, int vw, int vh, double kx, double ky, int which,  \
+                           int band) {                                                                \
     GUARD({                                                                                           \
       ref::SimParam<T> sp = make_param<T>(p);                                                         \
       ref::CVec<T> v(vw, vh);                                                                         \
       std::copy(vec, vec + (size_t)2 * vw * vh, v.d.begin());                                         \
-      if (which == 0) sp.otf.writeOtfVector(v, kx, ky);                                               \
-      if (which == 1) sp.otf.writeOtfWithAttVector(v, kx, ky);                                        \
-      if (which == 2) sp.otf.applyOtf(v, kx, ky);                                                     \
+      if (which == 0) sp.otf.writeOtfVector(v, band, kx, ky);                                         \
+      if (which == 1) sp.otf.writeOtfWithAttVector(v, band, kx, ky);                                  \
+      if (which == 2) sp.otf.applyOtf(v, band, kx, ky);                                               \
       if (which == 3) sp.otf.maskOtf(v, kx, ky);                                                      \
       std::copy(v.d.begin(), v.d.end(), vec);                                                         \
     })                                                                                                \
@@ -318,7 +324,7 @@ int ref_matrix_inverse(const double* in, int n, double* out, int pseudo, int m) 
       ref::CVec<T> v0(w, w), v1(w, w);                                                                \
       std::copy(b0, b0 + (size_t)2 * w * w, v0.d.begin());                                           \
       std::copy(b1, b1 + (size_t)2 * w * w, v1.d.begin());                                            \
-      ref::common_region(v0, v1, sp.otf, kx, ky, dist, wl, divide != 0);                              \
+      ref::common_region(v0, v1, 0, 1, sp.otf, kx, ky, dist, wl, divide != 0);                              \
       std::copy(v0.d.begin(), v0.d.end(), b0);                                                        \
       std::copy(v1.d.begin(), v1.d.end(), b1);                                                        \
     })                                                                                                \
@@ -338,7 +344,7 @@ int ref_matrix_inverse(const double* in, int n, double* out, int pseudo, int m) 
       ref::CVec<T> v0(w, w), v1(w, w);                                                                \
       std::copy(band0, band0 + (size_t)2 * w * w, v0.d.begin());                                      \
       std::copy(band1, band1 + (size_t)2 * w * w, v1.d.begin());                                      \
-      ref::fit_peak(v0, v1, sp.otf, kx, ky, wl, search, out4, grid);                                  \
+      ref::fit_peak(v0, v1, 0, 1, sp.otf, kx, ky, wl, search, out4, grid);                                  \
     })                                                                                                \
   }                                                                                                   \
   int ref_get_peak_##SUF(const ref_param* p, const T* band0, const T* band1, double kx, double ky,    \
@@ -349,7 +355,7 @@ int ref_matrix_inverse(const double* in, int n, double* out, int pseudo, int m) 
       ref::CVec<T> v0(w, w), v1(w, w);                                                                \
       std::copy(band0, band0 + (size_t)2 * w * w, v0.d.begin());                                      \
       std::copy(band1, band1 + (size_t)2 * w * w, v1.d.begin());                                      \
-      ref::C<double> r = ref::get_peak(v0, v1, sp.otf, kx, ky, wl);                                   \
+      ref::C<double> r = ref::get_peak(v0, v1, 0, 1, sp.otf, kx, ky, wl);                                   \
       out2[0] = r.re;                                                                                 \
       out2[1] = r.im;                                                                                 \
     })                                                                                                \

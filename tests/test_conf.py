@@ -70,7 +70,7 @@ def test_sim_param_and_otf_roundtrip(fs, tmp_path):
     assert (o.attStrength, o.attFWHM) == (0.98, 1.3)
 
 
-def test_measured_otf_roundtrip_and_device_refusal(fs, tmp_path):
+def test_measured_otf_roundtrip_and_fused_refusal(fs, tmp_path):
     cfg = fs.conf.Conf("fairsim")
     fld = cfg.r().mk("otf2d")
     fld.newDbl("NA").setVal(1.4)
@@ -94,8 +94,10 @@ def test_measured_otf_roundtrip_and_device_refusal(fs, tmp_path):
     d2 = cfg2.r().cd("otf2d").cd("data")
     assert d2.getData("band-1").val() == fs.conf.to_bytes(bands[1])
     sp = fs.SimParam.create(2, 3, 3, 256, 0.08, otf)
-    with pytest.raises(NotImplementedError):  # the device path takes estimated OTFs only
-        fs.native.to_c_param(sp)
+    c = fs.native.to_c_param(sp)  # the record carries the bands to the library
+    assert (c.otf_bands, c.otf_samples, c.otf_cycles) == (2, 4, 0.0125)
+    with pytest.raises(ValueError):  # the fused plans take estimated OTFs only
+        fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
 
 
 @pytest.mark.skipif(not os.path.isdir(REF), reason="reference configuration files not present")

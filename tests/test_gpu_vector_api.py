@@ -309,3 +309,57 @@ def test_run_reconstruction_rl_styles_vs_oracle(fs, oracle, V, style):
     assert rel_l2(out, exp64) < 1e-4
     with pytest.raises(ValueError):  # the fused plans apply the Wiener filter only
         fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+
+
+def measured_otf(fs, samples=300, bands=2, spacing=256, na=1.4, lam=525.0, a=0.3):
+    """A complex multi-band measured OTF (OtfProvider with band data): the estimate's shape
+    with a per-band gain and a slow phase, `spacing` samples up to the cutoff."""
+    cut = 1000 / (lam / na / 2)
+    v = np.clip(np.arange(samples) / spacing, 0, 1)
+    base = (2 / np.pi) * (np.arccos(v) - v * np.sqrt(1 - v * v)) * a ** v
+    b = [(base * (1 - 0.1 * k) * np.exp(1j * 0.3 * (k + 1) * v)).tolist() for k in range(bands)]
+    return fs.OtfProvider.fromMeasured(na, lam, b, cut / spacing)
+
+
+@pytest.mark.parametrize("samples", [300, 200])
+def test_measured_otf_reconstruction_and_filters_vs_oracle(V, oracle, fs, samples):
+    """Measured two-band complex OTFs (OtfProvider.loadFromConfig with band data) through the
+    op-by-op path: the band-1 OTF vector with and without attenuation, the Wiener
+    denominator and the reconstruction against the oracle."""
+    n = 128
+    raw, truth = fs.synth.make_dataset(n=n, seed=41)
+    sp = fs.synth.sim_param_for(truth, n)
+    sp.setOtf(measured_otf(fs, samples=samples))
+    sp.otf().setAttenuation(0.97, 1.1)
+    sp.otf().switchAttenuation(True)
+    for which, att in ((0, False), (1, True)):  # writeOtfVector, writeOtfWithAttVector
+        v = V.Vec2dCplx(2 * n, 2 * n)
+        fs.algorithm.OtfVectors.otfToVector(sp, v, 1, 10.5, -3.25, att, True)
+        exp = oracle.otf_vector(sp, np.zeros((2 * n, 2 * n), complex), 10.5, -3.25, which=which, band=1)
+        assert rel_l2(v.vectorData(), exp) < 1e-6
+    # getAttVal reads past a table that ends inside the cutoff (the reference throws there)
+    sp.otf().switchAttenuation(samples * sp.otf().measured["cycles"] >= sp.otf().getCutoff())
+    wd = fs.algorithm.WienerFilter(sp).getDenominator(sp.wiener)
+    assert rel_l2(wd.vectorData(), oracle.wiener_denominator(sp)) < 1e-6
+    spec = oracle.prepare_raw(sp, raw)
+    inFFT = [[cvec(V, spec[a * 3 + p]) for p in range(3)] for a in range(3)]
+    out = fs.algorithm.SimAlgorithm.runReconstruction(sp, inFFT, False, 0).vectorData()
+    assert rel_l2(out, oracle.recon(sp, spec)) < 1e-4
+    assert rel_l2(out, oracle.recon(sp, spec.astype(np.complex128), dtype=np.float64)) < 1e-5
+
+
+def test_measured_otf_estimation_vs_oracle(V, oracle, fs):
+    """estimateParameters with a measured two-band OTF: commonRegion weights and divisions
+    by the complex band-0 / band-1 values; the same fitted k0 as the oracle."""
+    n = 256
+    raw, truth = fs.synth.make_dataset(n=n, seed=42)
+    sp = fs.synth.sim_param_for(truth, n, known=False)
+    sp.setOtf(measured_otf(fs))
+    spec = oracle.prepare_raw(sp, raw)
+    est, _, _ = oracle.estimate(sp, spec, 1, 0.6)
+    inFFT = [[cvec(V, spec[a * 3 + p]) for p in range(3)] for a in range(3)]
+    fs.algorithm.SimAlgorithm.estimateParameters(sp, inFFT, 1, 0.6)
+    for d in range(3):
+        assert abs(sp.dir(d).pX - est["pX"][d]) < 1e-9 and abs(sp.dir(d).pY - est["pY"][d]) < 1e-9
+        assert abs(sp.dir(d).phaOff - est["phaOff"][d]) < 1e-4
+        assert abs(sp.dir(d).modul[1] - est["modulations"][d][1]) < 1e-4

@@ -231,3 +231,46 @@ def test_rl_filter_styles_float_vs_fp64(oracle, fs, style):
     assert err < 1e-4
     sp.setFilterStyle(0)
     assert rel_l2(f64, oracle.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)) > 1e-2
+
+
+def measured_bands(na=1.4, lam=525.0, samples=300, bands=2, a=0.3, spacing=256):
+    """Synthetic measured OTF bands: the estimate's shape with a per-band gain and a slow
+    complex phase (as a bead measurement gives), `spacing` samples up to the cutoff."""
+    cut = 1000 / (lam / na / 2)
+    v = np.arange(samples) / spacing
+    vc = np.clip(v, 0, 1)
+    base = (2 / np.pi) * (np.arccos(vc) - vc * np.sqrt(1 - vc * vc)) * a ** vc
+    return [(base * (1 - 0.1 * b) * np.exp(1j * 0.3 * (b + 1) * vc)).tolist() for b in range(bands)], cut / spacing
+
+
+def test_measured_otf_equal_to_estimate_gives_estimate_result(oracle, fs):
+    """OtfProvider built from band data (S/OtfProvider.java:588-621) holding the estimate's own
+    512 samples reconstructs like the estimate: the measured-OTF code path is the estimate's."""
+    n = 64
+    raw, truth = fs.synth.make_dataset(n=n, seed=33)
+    sp = fs.synth.sim_param_for(truth, n)
+    est = oracle.recon_raw(sp, raw, fade=10, dtype=np.float64)
+    o = sp.otf()
+    v = np.arange(512) / 512
+    vals = (2 / np.pi) * (np.arccos(v) - v * np.sqrt(1 - v * v)) * o.a ** v
+    sp2 = sp.duplicate()
+    sp2.setOtf(fs.OtfProvider.fromMeasured(o.na, o.emWavelength, [vals.astype(np.float32).tolist()],
+                                           o.getCutoff() / 512))
+    meas = oracle.recon_raw(sp2, raw, fade=10, dtype=np.float64)
+    assert rel_l2(meas, est) < 1e-6
+
+
+@pytest.mark.parametrize("samples", [300, 200])
+def test_measured_multiband_otf_float_vs_fp64(oracle, fs, samples):
+    """A complex two-band measured OTF (200 samples ends the table inside the cutoff): the
+    float oracle within the parity bound of FP64, and different from the estimate."""
+    n = 64
+    raw, truth = fs.synth.make_dataset(n=n, seed=34)
+    sp = fs.synth.sim_param_for(truth, n)
+    bands, cyc = measured_bands(samples=samples)
+    est = oracle.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+    sp.setOtf(fs.OtfProvider.fromMeasured(1.4, 525.0, bands, cyc))
+    f32 = oracle.recon_raw(sp, raw, fade=10)
+    f64 = oracle.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+    assert rel_l2(f32, f64) < 1e-4
+    assert rel_l2(f64, est) > 1e-3
