@@ -49,10 +49,12 @@ def _compile(src, verbose=False, extra=()):
 
 
 def build(verbose: bool = False, jobs: int | None = None, ptxas_info: bool = False) -> str:
+    """FSIM_NVCC_FLAGS (environment) adds nvcc flags to every translation unit, e.g. the
+    register budgets -DFSIM_PA_REGS=80 (every unit is then recompiled)."""
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = _sources()
-    extra = ("-Xptxas", "-v") if ptxas_info else ()
+    extra = (("-Xptxas", "-v") if ptxas_info else ()) + tuple(os.environ.get("FSIM_NVCC_FLAGS", "").split())
     jobs = jobs or min(len(srcs), max(2, os.cpu_count() or 2))
     objs, logs = [], []
     with cf.ThreadPoolExecutor(jobs) as ex:

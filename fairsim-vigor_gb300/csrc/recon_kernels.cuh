@@ -19,6 +19,17 @@
 #include "otf.cuh"
 #include "recon.cuh"
 
+// Register budgets (registers per thread) of passes A, B1 and B2 at 8 elements per thread.
+#ifndef FSIM_PA_REGS
+#define FSIM_PA_REGS 64
+#endif
+#ifndef FSIM_B1_REGS
+#define FSIM_B1_REGS 64
+#endif
+#ifndef FSIM_B2_REGS
+#define FSIM_B2_REGS 64
+#endif
+
 namespace fsim {
 
 // ---- launch configuration (variants picked per size by the autotuner) --------------------
@@ -63,13 +74,13 @@ __device__ __forceinline__ int paste_src(int X) {
 // 64-thread row blocks of 8 elements, 64 for longer rows at 8 elements, 96 at 12 elements.
 template <int T, int EN>
 __host__ __device__ constexpr int pass_a_min_blocks() {
-  return EN <= 8 ? (T == 64 ? 16 : (65536 / (T * 64) > 0 ? 65536 / (T * 64) : 1))
+  return EN <= 8 ? (65536 / (T * FSIM_PA_REGS) > 0 ? 65536 / (T * FSIM_PA_REGS) : 1)
                  : (EN == 12 ? (65536 / (T * 96) > 0 ? 65536 / (T * 96) : 1) : 1);
 }
 // The column passes: 64 registers per thread at 8 elements, 80 at 12.
-template <int THREADS, int EN>
+template <int THREADS, int EN, int REGS8 = 64>
 __host__ __device__ constexpr int col_min_blocks() {
-  return EN <= 8 ? (65536 / (THREADS * 64) > 0 ? 65536 / (THREADS * 64) : 1)
+  return EN <= 8 ? (65536 / (THREADS * REGS8) > 0 ? 65536 / (THREADS * REGS8) : 1)
                  : (EN == 12 ? (65536 / (THREADS * 80) > 0 ? 65536 / (THREADS * 80) : 1) : 1);
 }
 template <int N, int ENV>
@@ -260,7 +271,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T) k_pass_g(const JobDesc* __rest
 // row window go to Tw in quad layout; for neg columns also d' = -2i conj(Z[N/2]).
 template <int N, int ENV, int CBV>
 __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
-                                  col_min_blocks<Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T, Cfg<N, ENV, CBV>::EN>())
+                                  col_min_blocks<Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T, Cfg<N, ENV, CBV>::EN,
+                                                 FSIM_B1_REGS>())
     k_pass_b1(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N, ENV, CBV>;
   constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN;
@@ -350,7 +362,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
 // (the identity of pass A along y, plus pass G's column for the x term).
 template <int N, int ENV, int CBV>
 __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
-                                  col_min_blocks<Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T, Cfg<N, ENV, CBV>::EN>())
+                                  col_min_blocks<Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T, Cfg<N, ENV, CBV>::EN,
+                                                 FSIM_B2_REGS>())
     k_pass_b2(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N, ENV, CBV>;
   constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN;
