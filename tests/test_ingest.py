@@ -256,3 +256,51 @@ def test_broken_header_closes_stream_until_reset(fs):
     with pytest.raises(ValueError):
         ig.SequenceExtractor([1], 9, W, H, sync_mode=2)
     x.close()
+
+
+def test_concurrent_receivers_and_consumer(fs):
+    """One receiving thread per channel pushing frames while a consumer pops stacks (the
+    reference's ImageSorter / PerChannelBuffer / JoinedChannelBuffer threads): every stack
+    comes out once, in order, identical to the single-threaded result."""
+    import threading
+
+    ig = ingest(fs)
+    nraw = 9
+    rng = np.random.default_rng(17)
+    frames = build_stream(rng, nraw, 1, 0, n_groups=20, unknown=False)
+    by_ch = {c: [f for f in frames if seqx_ref.parse_header(f, W, H)["pos1"] == c] for c in CHANNELS}
+    ref = ig.SequenceExtractor(CHANNELS, nraw, W, H)
+    for f in frames:
+        ref.push(f)
+    expected = drain_lib(ref)
+    x = ig.SequenceExtractor(CHANNELS, nraw, W, H)
+    got, done = [], threading.Event()
+
+    def consumer():
+        while True:
+            finished = done.is_set()  # read before the pop: nothing arrives after it is set
+            r = x.pop(with_seq=True)
+            if r is not None:
+                got.append(r)
+            elif finished:
+                return
+
+    def receiver(c):
+        for f in by_ch[c]:
+            x.push(f)
+
+    cons = threading.Thread(target=consumer)
+    cons.start()
+    recv = [threading.Thread(target=receiver, args=(c,)) for c in CHANNELS]
+    for t in recv:
+        t.start()
+    for t in recv:
+        t.join()
+    done.set()
+    cons.join(timeout=30)
+    assert not cons.is_alive()
+    assert len(got) == len(expected) >= 5
+    for (s1, f1), (s2, f2) in zip(got, expected):
+        assert f1 == f2 and np.array_equal(s1, s2)
+    x.close()
+    ref.close()
