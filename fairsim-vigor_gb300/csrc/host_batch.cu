@@ -101,6 +101,11 @@ extern "C" int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int 
   }
   chunk = std::min(chunk, n_jobs);
   std::lock_guard<std::mutex> lock(g_pipe.mu);
+  struct FoldOff {  // per-angle band 0 for this call's chunks
+    bool prev = band0_fold_off();
+    FoldOff() { band0_fold_off() = true; }
+    ~FoldOff() { band0_fold_off() = prev; }
+  } fold_off;
   HostPipe& P = g_pipe;
   rc = init_pipe(P);
   if (rc) return rc;

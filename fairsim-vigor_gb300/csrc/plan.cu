@@ -411,6 +411,11 @@ int fsim_profile_read(float* ms, int max_passes, int* n_passes) {
 int fsim_recon_host(fsim_plan* plan, const void* raw_host, float* out_host) {
   NEED_INIT();
   FSIM_REQUIRE(plan && raw_host && out_host, FSIM_EINVAL, "recon_host: null argument");
+  struct FoldOff {  // host-buffer calls keep band 0 per angle, as fsim_recon_batch_host
+    bool prev = band0_fold_off();
+    FoldOff() { band0_fold_off() = true; }
+    ~FoldOff() { band0_fold_off() = prev; }
+  } fold_off;
   cudaStream_t st = ctx().stream;
   const int N = plan->prm.w, W = 2 * N;
   const size_t raw_bytes = (size_t)N * N * plan->prm.nr_dirs * plan->prm.nr_phases *

@@ -91,16 +91,54 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   const int y = blockIdx.x, a = blockIdx.y, t = threadIdx.x;
   __shared__ JobDesc J;
   __shared__ float2 bz[smem_line_elems(N, 1)], bh[smem_line_elems(N, 1)];
-  __shared__ float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
+  __shared__ float2 coef[FSIM_MAX_DIRS * FSIM_MAX_PHASES];
   const float2* twN = g_stw + stw_offset(N, EN);  // stage table, read through L1
   const float2* twW = g_tw + tw_offset(W);
   load_job(&J, jobs + blockIdx.z, t, T);
   __syncthreads();
-  if (a >= J.nA) return;  // uniform per block
-  const int nP = J.nP, nC = J.nC, nPair = (nC - 1) / 2, nS = 1 + nPair;  // I slots per angle
+  if (a > J.nA || (a == J.nA && !J.fold0)) return;  // uniform per block
+  const int nA = J.nA, nP = J.nP, nC = J.nC, nPair = (nC - 1) / 2, nS = 1 + nPair;  // I slots per angle
+  const size_t frame = (size_t)N * N, row = (size_t)y * N;
+  if (a == nA) {
+    // Band 0 is summed over the angles before the column pass, and its band separation
+    // and row FFT are linear: one block per row mixes the band-0 rows of every angle and
+    // transforms the sum once into slot 0 (band 0 has no shift: one window for all angles).
+    const int nF = nA * nP;
+    for (int i = t; i < nF; i += T) coef[i] = J.coef[((i / nP) * nC) * nP + i % nP];
+    __syncthreads();
+    float2 x[EN];
+#pragma unroll
+    for (int i = 0; i < EN; i++) x[i] = make_float2(0.f, 0.f);
+    for (int f = 0; f < nF; f++) {
+      const float2 c = coef[f];
+#pragma unroll
+      for (int i = 0; i < EN; i++) {
+        const size_t at = f * frame + row + t + i * T;
+        float v = J.input_u16 ? (float)__ldg((const uint16_t*)J.raw + at) : __ldg((const float*)J.raw + at);
+        if (J.bgr != 0.f) {  // background clip and border damping, as below
+          v = v - J.bgr;
+          if (v < 0) v = 0;
+        }
+        if (J.damp) v = v * __ldg(J.damp + row + t + i * T);
+        x[i].x += c.x * v;
+        x[i].y += c.y * v;
+      }
+    }
+    line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
+#pragma unroll
+    for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
+    __syncthreads();
+    const int Xs = J.win[0];
+    for (int xl = t; xl < J.nWin; xl += T) {
+      int X = Xs + xl;
+      if (X >= W) X -= W;
+      const int m = paste_src<N>(X);
+      J.I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = m >= 0 ? bh[sidx(m)] : make_float2(0.f, 0.f);
+    }
+    return;
+  }
   for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
   __syncthreads();
-  const size_t frame = (size_t)N * N, row = (size_t)y * N;
   auto raw_at = [&](int p, int x) {  // background clip and border damping of one raw pixel
     const size_t at = (size_t)(a * nP + p) * frame + row + x;
     float v = J.input_u16 ? (float)__ldg((const uint16_t*)J.raw + at) : __ldg((const float*)J.raw + at);
@@ -126,6 +164,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   // component's row transform follows from the neg one's (below). A line stays in
   // registers from one transform to the next (x[i] = element t + i*T), bz and bh serve as
   // scratch.
+  // the band pairs of this block's angle, and (band 0 not folded) this angle's band 0
+  const bool own0 = !J.fold0;
   float2 x[EN], zk[EN];  // zk: the first pair's neg component, kept for the even-sample product
 #pragma unroll
   for (int i = 0; i < EN; i++) {
@@ -133,21 +173,23 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     float2 z0 = make_float2(0.f, 0.f), zn = make_float2(0.f, 0.f);
     for (int p = 0; p < nP; p++) {
       const float v = raw_at(p, xx);
-      const float2 m0 = coef[p], mn = coef[nP + p];
-      z0.x += m0.x * v;
-      z0.y += m0.y * v;
+      const float2 mn = coef[nP + p];
       zn.x += mn.x * v;
       zn.y += mn.y * v;
+      if (own0) {
+        const float2 m0 = coef[p];
+        z0.x += m0.x * v;
+        z0.y += m0.y * v;
+      }
     }
     x[i] = z0;
     zk[i] = zn;
   }
-  // band 0: Z0 = FFT_N(z0), pasteFreq only; keep the OTF-support window in quad layout
-  line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
+  if (own0) {  // uniform per block: Z0 = FFT_N(z0) of this angle, window into its own slot
+    line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
 #pragma unroll
-  for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
-  __syncthreads();
-  {
+    for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
+    __syncthreads();
     const int Xs = J.win[2 * (a * nC)];
     float2* I = J.I + (size_t)(a * nS) * J.nWin * N;
     for (int xl = t; xl < J.nWin; xl += T) {
@@ -292,17 +334,22 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   const size_t quad = ((size_t)(xl >> 2) * N) * 4 + (xl & 3);
   float2* out = J.Tw + (size_t)comp * nWin * nWin + ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3);
   float2 x[EN];  // element t + i*T of this lane's column, in registers through the transforms
-  if (comp == 0) {
+  if (comp == 0) {  // band 0: summed over the angles in pass A (slot 0), or here
+    if (J.fold0) {
 #pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int k = t + i * T;
-      float2 v = make_float2(0.f, 0.f);
-      for (int a = 0; a < J.nA; a++) {
-        const float2 u = J.I[(size_t)a * nS * nWin * N + quad + (size_t)k * 4];
-        v.x += u.x;
-        v.y += u.y;
+      for (int i = 0; i < EN; i++) x[i] = J.I[quad + (size_t)(t + i * T) * 4];
+    } else {
+#pragma unroll
+      for (int i = 0; i < EN; i++) {
+        const int k = t + i * T;
+        float2 v = make_float2(0.f, 0.f);
+        for (int a = 0; a < J.nA; a++) {
+          const float2 u = J.I[(size_t)a * nS * nWin * N + quad + (size_t)k * 4];
+          v.x += u.x;
+          v.y += u.y;
+        }
+        x[i] = v;
       }
-      x[i] = v;
     }
     line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);
 #pragma unroll
@@ -501,8 +548,10 @@ __global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::TC) k_pass_c(const JobDesc
 template <int N, int ENA>
 static void launch_a(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, cudaStream_t st) {
   using PA = Cfg<N, ENA>;
-  k_pass_a<N, ENA><<<dim3(N, maxA, njobs), PA::T, 0, st>>>(d_jobs);
+  // blockIdx.y: the angles' band pairs, then (y == nA) the band-0 row of all angles
+  k_pass_a<N, ENA><<<dim3(N, maxA + 1, njobs), PA::T, 0, st>>>(d_jobs);
 }
+
 template <int N, int ENA>
 static void launch_g(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, cudaStream_t st) {
   using PA = Cfg<N, ENA>;

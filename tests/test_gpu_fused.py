@@ -13,6 +13,22 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
+def device_alone(fs, torch, plan, raw, widefield=False, filtered=False):
+    """One job alone through the device batch entry (fsim_recon_batch): the reference bits
+    for device batches and graphs (band 0 of all angles folded into one row pass). The
+    host-buffer entries keep band 0 per angle; both agree to float rounding."""
+    n = plan.w
+    d_raw = torch.from_numpy(raw.view(np.int16) if raw.dtype == np.uint16 else raw).cuda()
+    dev = lambda: torch.zeros((2 * n, 2 * n), dtype=torch.float32, device="cuda")  # noqa: E731
+    out, wf, fwf = dev(), dev() if widefield else None, dev() if filtered else None
+    ws = torch.empty(fs.plan.batch_workspace_bytes([plan]), dtype=torch.uint8, device="cuda")
+    ptr = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+    fs.plan.recon_batch([(plan, d_raw.data_ptr(), out.data_ptr(), ptr(wf), ptr(fwf))], ws.data_ptr(), ws.numel())
+    torch.cuda.synchronize()
+    res = [t.cpu().numpy() if t is not None else None for t in (out, wf, fwf)]
+    return res[0] if not (widefield or filtered) else res
+
+
 def make(fs, n, seed, **kw):
     raw, truth = fs.synth.make_dataset(n=n, seed=seed, **kw)
     sp = fs.synth.sim_param_for(truth, n, n_dirs=kw.get("n_dirs", 3), n_phases=kw.get("n_phases", 3),
@@ -90,7 +106,9 @@ def test_batched_mixed_sizes_identical_to_single(fs, torch_cuda):
         p = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
         plans.append(p)
         raws.append(raw)
-        singles.append(p.reconstruct_host(raw))
+        singles.append(device_alone(fs, torch, p, raw))
+        # the host-buffer entry (band 0 per angle) agrees to float rounding
+        assert rel_l2(p.reconstruct_host(raw), singles[-1]) < 1e-6
     d_raw = [torch.from_numpy(r).cuda() for r in raws]
     d_out = [torch.empty((2 * p.w, 2 * p.w), dtype=torch.float32, device="cuda") for p in plans]
     ws = torch.empty(fs.plan.batch_workspace_bytes(plans), dtype=torch.uint8, device="cuda")
@@ -207,8 +225,8 @@ def test_batch_graph_replays_match_batch(fs, torch_cuda):
     plans[1].update(sp3)
     g.launch()
     torch.cuda.synchronize()
-    assert np.array_equal(d_out[0].cpu().numpy(), plans[0].reconstruct_host(raw2))
-    assert np.array_equal(d_out[1].cpu().numpy(), plans[1].reconstruct_host(raws[1]))
+    assert np.array_equal(d_out[0].cpu().numpy(), device_alone(fs, torch, plans[0], raw2))
+    assert np.array_equal(d_out[1].cpu().numpy(), device_alone(fs, torch, plans[1], raws[1]))
     g.close()
 
 
@@ -361,7 +379,7 @@ def test_widefield_in_batches_and_graphs(fs, torch_cuda):
     fs.plan.recon_batch(jobs, ws.data_ptr(), ws.numel())
     torch.cuda.synchronize()
     for i, (p, r) in enumerate(zip(plans, raws)):
-        img, wf, fwf = p.reconstruct_host_widefield(r)
+        img, wf, fwf = device_alone(fs, torch, p, r, widefield=True, filtered=True)
         assert np.array_equal(d_out[i].cpu().numpy(), img)
         if d_wf[i] is not None:
             assert np.array_equal(d_wf[i].cpu().numpy(), wf)
