@@ -175,8 +175,8 @@ def run_reference(args):
 # DRAM bytes (read + write) per dataset of each pass at 512^2 3x3, from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum) of this program's passes on a 16-dataset
 # batch (raw 151 MB, larger than L2); per-launch traffic = this x the batch size.
-TRAFFIC_PER_DATASET = {"k_pass_a<512>": 18.81e6, "k_pass_g+k_pass_b1<512>": 15.56e6, "k_pass_b2<512>": 22.86e6,
-                       "k_pass_c<512>": 10.69e6}
+TRAFFIC_PER_DATASET = {"k_pass_a<512>": 15.98e6, "k_pass_g+k_pass_b1<512>": 11.16e6, "k_pass_b2<512>": 22.86e6,
+                       "k_pass_c<512>": 10.70e6}
 
 
 def pass_bytes(n=N, n_dirs=NA, n_phases=NP, n_bands=NB, na=1.4, lam=525.0, pxl=0.08):
