@@ -15,7 +15,8 @@
 // Three passes per dataset, run after pass C in the job's own (then free) workspace:
 //   WA rows:    band-0 mix over all frames, FFT_N along x            -> Wf [N][N]
 //   WB columns: FFT_N along y, (filter), even/odd inverse along y    -> V_o [W][N], o = 0, 1
-//   WC rows:    even/odd inverse along x, real part, 1/W^2           -> widefield / fwf [W][W]
+//   WC rows:    even/odd inverse along x (one transform: the two real parts
+//               from the Hermitian halves), 1/W^2                     -> widefield / fwf [W][W]
 // Algorithmic bytes per dataset (f32 raw): nA nP 4N^2 + 8N^2 | 8N^2 + 4N^2 + 2 x 16N^2 |
 // 2 x (16N^2 + 16N^2).
 #include "common.cuh"
@@ -155,22 +156,32 @@ __global__ void __launch_bounds__(WfCfg<N>::G* WfCfg<N>::T) k_wf_out(const JobDe
   const float2* twW = g_tw + tw_offset(W);
   const float2* V = J.Wf + (size_t)N * N + (size_t)o * W * N + (size_t)Y * N;
   float2* s = sm + g * SL;
+  // Only the real parts of iFFT_N(a) (even columns, a = v) and iFFT_N(b) (odd columns,
+  // b = v * s) are kept. Re(iFFT(a)) = iFFT(Ha), Ha[k] = (a[k] + conj(a[-k]))/2 is real, so
+  // one transform of Ha + i Hb gives both: even columns in its real part, odd in its imaginary.
   float2 v[E], y[E];
-  float ev[E];
 #pragma unroll
-  for (int i = 0; i < E; i++) v[i] = V[t + i * T];
+  for (int i = 0; i < E; i++) {
+    v[i] = V[t + i * T];
+    s[sidx(t + i * T)] = v[i];
+  }
+  __syncthreads();
 #pragma unroll
-  for (int i = 0; i < E; i++) y[i] = v[i];
-  line_fft_reg<N, T, 1, true>(y, s, 0, t, twN);
-#pragma unroll
-  for (int i = 0; i < E; i++) ev[i] = y[i].x;
-#pragma unroll
-  for (int i = 0; i < E; i++) y[i] = cmul(v[i], wf_half_shift<N>(twW, t + i * T));
+  for (int i = 0; i < E; i++) {
+    const int k = t + i * T, km = k == 0 ? 0 : N - k;
+    const float2 vm = s[sidx(km)];
+    const float2 a = v[i], am = vm;
+    const float2 b = cmul(v[i], wf_half_shift<N>(twW, k)), bm = cmul(vm, wf_half_shift<N>(twW, km));
+    const float2 ha = make_float2(0.5f * (a.x + am.x), 0.5f * (a.y - am.y));  // (a + conj(a_-k)) / 2
+    const float2 hb = make_float2(0.5f * (b.x + bm.x), 0.5f * (b.y - bm.y));
+    y[i] = make_float2(ha.x - hb.y, ha.y + hb.x);  // ha + i hb
+  }
+  __syncthreads();  // the mirrored reads are done before the transform writes the scratch
   line_fft_reg<N, T, 1, true>(y, s, 0, t, twN);
   const float sc = (float)(1.0 / ((double)W * (double)W));
   float2* orow = reinterpret_cast<float2*>(out + (size_t)Y * W);
 #pragma unroll
-  for (int i = 0; i < E; i++) orow[t + i * T] = make_float2(ev[i] * sc, y[i].x * sc);
+  for (int i = 0; i < E; i++) orow[t + i * T] = make_float2(y[i].x * sc, y[i].y * sc);
 }
 
 // The filtered widefield's filter on the N grid, built once per plan: conj(OTF_0) (the OTF
