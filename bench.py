@@ -194,7 +194,7 @@ def pass_bytes(n=N, n_dirs=NA, n_phases=NP, n_bands=NB, na=1.4, lam=525.0, pxl=0
     W = 2 * n
     R = (2 * na / (lam / 1000.0)) / (1.0 / (n * pxl))
     nwin = min(W, ((2 * int(np.ceil(R)) + 6) // 4) * 4 + 4)
-    I = (1 + n_dirs * npair) * nwin * n * 8  # band 0 folded over the angles (device batches)
+    I = (1 + n_dirs * npair) * nwin * n * 8  # band 0 summed over the angles in pass A
     D = n_dirs * npair * n * 8
     G = n_dirs * npair * nwin * 8
     Tw = (1 + n_dirs * npair) * nwin * nwin * 8

@@ -4,13 +4,15 @@
 // org/fairsim/accel/AccelVectorReal.java:218-247, then one JNI op per step). Here a whole
 // batch of host stacks is reconstructed in chunks that flow through three library-owned
 // streams: the upload of chunk i+1, the passes of chunk i and the download of chunk i-1 run
-// at the same time. Two slots of device buffers (raw frames, outputs, workspace) alternate
-// between chunks; events order each slot's reuse:
-//   upload(i)   waits for passes(i-2)    (raw slot free)
-//   passes(i)   waits for upload(i), download(i-2) (out slot free)
+// at the same time. A ring of FSIM_HOST_SLOTS slots of device buffers (raw frames, outputs,
+// workspace) serves the chunks in turn; events order each slot's reuse (K = slots):
+//   upload(i)   waits for passes(i-K)    (raw slot free)
+//   passes(i)   waits for upload(i), download(i-K) (out slot free)
 //   download(i) waits for passes(i)
-// The host fills chunk i's job table only after passes(i-2) finished with it, so the host
-// runs at most two chunks ahead. The call returns when every output is in host memory.
+// The host carves chunk i's slot only after passes(i-K) finished with it, so the host runs
+// at most K chunks ahead. The job tables travel as kernel parameters: a table upload on the
+// compute stream would queue behind the raw-frame uploads on the one host-to-device copy
+// engine and serialize the passes with them. The call returns when every output is in host memory.
 // Host buffers that are page-locked (cudaHostAlloc / cudaHostRegister) are copied by DMA
 // directly; pageable ones make each copy synchronous on the host.
 #include <algorithm>
@@ -21,14 +23,18 @@
 #include "recon.cuh"
 #include "runtime.cuh"
 
+// three slots: 17.1k against 16.7k reconstructions/s with two (512^2 3x3, chunks of 4, GB300)
+#ifndef FSIM_HOST_SLOTS
+#define FSIM_HOST_SLOTS 3
+#endif
+static_assert(FSIM_HOST_SLOTS >= 2 && FSIM_HOST_SLOTS <= 8, "host pipeline: 2..8 slots");
+
 namespace fsim {
 namespace {
 
 struct Slot {
   char* dev = nullptr;  // raw | out | widefields | workspace
   size_t bytes = 0;
-  JobDesc* table = nullptr;  // pinned job table of the chunk in this slot
-  int table_cap = 0;
   cudaEvent_t up = nullptr, done = nullptr, down = nullptr;
   bool used = false;
 };
@@ -37,7 +43,7 @@ struct HostPipe {
   std::mutex mu;
   bool ready = false;
   cudaStream_t s_up = nullptr, s_comp = nullptr, s_down = nullptr;
-  Slot slot[2];
+  Slot slot[FSIM_HOST_SLOTS];
 };
 HostPipe g_pipe;
 
@@ -95,21 +101,17 @@ extern "C" int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int 
   if (chunk <= 0) {
     // about 40 MiB of raw frames per chunk (four 512^2 3x3 stacks): the host link, not
     // the passes, bounds a host-buffer batch, and short chunks keep both copy directions
-    // busy from the start (measured on GB300: 4 stacks 13.0k/s, 10 12.0k/s, 64 9.1k/s)
+    // busy from the start (measured on GB300, 64 stacks: chunks of 2 14.3k/s, 4 17.1k/s,
+    // 8 16.3k/s, 16 14.9k/s)
     const size_t rb = raw_bytes(reinterpret_cast<const Plan*>(jobs[0].plan));
     chunk = (int)std::max<size_t>(1, ((size_t)40 << 20) / std::max<size_t>(rb, 1));
   }
   chunk = std::min(chunk, n_jobs);
   std::lock_guard<std::mutex> lock(g_pipe.mu);
-  struct FoldOff {  // per-angle band 0 for this call's chunks
-    bool prev = band0_fold_off();
-    FoldOff() { band0_fold_off() = true; }
-    ~FoldOff() { band0_fold_off() = prev; }
-  } fold_off;
   HostPipe& P = g_pipe;
   rc = init_pipe(P);
   if (rc) return rc;
-  // size both slots for the largest chunk of this batch (the previous call has finished)
+  // size every slot for the largest chunk of this batch (the previous call has finished)
   size_t need = 0;
   for (int k0 = 0; k0 < n_jobs; k0 += chunk) need = std::max(need, chunk_bytes(jobs, k0, std::min(n_jobs, k0 + chunk)));
   for (auto& s : P.slot) {
@@ -120,22 +122,16 @@ extern "C" int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int 
       FSIM_CUDA(fsim::dev_alloc(&s.dev, need));
       s.bytes = need;
     }
-    if (s.table_cap < chunk) {
-      if (s.table) cudaFreeHost(s.table);
-      s.table = nullptr;
-      s.table_cap = 0;
-      FSIM_CUDA(cudaMallocHost(&s.table, sizeof(JobDesc) * chunk));
-      s.table_cap = chunk;
-    }
     s.used = false;
   }
   std::vector<fsim_job> dj(chunk);
+  std::vector<JobDesc> table(chunk);  // consumed at launch (kernel parameters)
   int c = 0;
   for (int k0 = 0; k0 < n_jobs; k0 += chunk, c++) {
     const int k1 = std::min(n_jobs, k0 + chunk), m = k1 - k0;
-    Slot& S = P.slot[c & 1];
+    Slot& S = P.slot[c % FSIM_HOST_SLOTS];
     if (S.used) {
-      // the table and raw buffers of chunk c-2 must be consumed, and its outputs downloaded
+      // the raw buffers of chunk c-K must be consumed, and its outputs downloaded
       FSIM_CUDA(cudaEventSynchronize(S.done));
       FSIM_CUDA(cudaStreamWaitEvent(P.s_up, S.done, 0));
       FSIM_CUDA(cudaStreamWaitEvent(P.s_comp, S.down, 0));
@@ -165,7 +161,7 @@ extern "C" int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int 
     }
     FSIM_CUDA(cudaEventRecord(S.up, P.s_up));
     FSIM_CUDA(cudaStreamWaitEvent(P.s_comp, S.up, 0));
-    rc = recon_batch(dj.data(), m, cur, S.bytes - (size_t)(cur - S.dev), P.s_comp, S.table, true);
+    rc = recon_batch(dj.data(), m, cur, S.bytes - (size_t)(cur - S.dev), P.s_comp, table.data(), true);
     if (rc) {
       cudaStreamSynchronize(P.s_up);
       cudaStreamSynchronize(P.s_comp);

@@ -377,7 +377,6 @@ void Plan::fill_job_live(JobDesc& j, const void* raw, float* out, float* wf, cha
   j.fwf = nullptr;
   j.wff = nullptr;
   j.Wf = nullptr;
-  j.fold0 = 0;
   size_t I = (size_t)prm.nr_dirs * nC * N * N * sizeof(float2);
   j.I = (float2*)ws;
   j.O = (float2*)(ws + ((I + 255) & ~(size_t)255));

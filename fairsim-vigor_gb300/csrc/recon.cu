@@ -276,7 +276,6 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, float* f
   j.widefield = wf;
   j.fwf = fwf;
   j.wff = d_wff;
-  j.fold0 = band0_fold_off() ? 0 : 1;
   j.Wf = (float2*)ws;
   j.input_u16 = input_type == FSIM_INPUT_U16;
   j.nA = prm.nr_dirs;

@@ -31,7 +31,6 @@ struct JobDesc {
   float* fwf;              // W*W filtered widefield, nullable (widefield: W*W offline, N*N live)
   const float* wff;        // N*N filter of the filtered widefield (resident, k_build_wff)
   float2* Wf;              // workspace (reused after pass C): N*N band-0 rows, then 2 x [W][N] columns
-  int fold0;               // band 0 of all angles mixed and transformed once per row (pass A)
 };
 
 struct Plan {
@@ -73,14 +72,6 @@ struct Plan {
 // event array to record into, or nullptr when profiling is off.
 cudaEvent_t* profile_events();
 void profile_mark(int n_passes);
-// Band 0 of every angle summed in one row block of pass A (JobDesc.fold0): on for device
-// batches and graphs (29.9k against 28.4k reconstructions/s at 512^2 3x3 on GB300); off
-// on this thread while set, which the host-buffer pipeline does (its chunks measured 13.3k
-// per-angle against 12.0k folded).
-inline bool& band0_fold_off() {
-  static thread_local bool off = false;
-  return off;
-}
 
 bool offline_size_supported(int n);
 int offline_variants(int pass);

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   const float2* twW = g_tw + tw_offset(W);
   load_job(&J, jobs + blockIdx.z, t, T);
   __syncthreads();
-  if (a > J.nA || (a == J.nA && !J.fold0)) return;  // uniform per block
+  if (a > J.nA) return;  // uniform per block
   const int nA = J.nA, nP = J.nP, nC = J.nC, nPair = (nC - 1) / 2, nS = 1 + nPair;  // I slots per angle
   const size_t frame = (size_t)N * N, row = (size_t)y * N;
   if (a == nA) {
@@ -137,6 +137,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     }
     return;
   }
+  if (nPair == 0) return;  // one band: the band-0 block above is the whole row pass
   for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
   __syncthreads();
   auto raw_at = [&](int p, int x) {  // background clip and border damping of one raw pixel
@@ -164,41 +165,10 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   // component's row transform follows from the neg one's (below). A line stays in
   // registers from one transform to the next (x[i] = element t + i*T), bz and bh serve as
   // scratch.
-  // the band pairs of this block's angle, and (band 0 not folded) this angle's band 0
-  const bool own0 = !J.fold0;
+  // the band pairs of this block's angle (band 0 of every angle is the blockIdx.y == nA block's)
   float2 x[EN], zk[EN];  // zk: the first pair's neg component, kept for the even-sample product
 #pragma unroll
-  for (int i = 0; i < EN; i++) {
-    const int xx = t + i * T;
-    float2 z0 = make_float2(0.f, 0.f), zn = make_float2(0.f, 0.f);
-    for (int p = 0; p < nP; p++) {
-      const float v = raw_at(p, xx);
-      const float2 mn = coef[nP + p];
-      zn.x += mn.x * v;
-      zn.y += mn.y * v;
-      if (own0) {
-        const float2 m0 = coef[p];
-        z0.x += m0.x * v;
-        z0.y += m0.y * v;
-      }
-    }
-    x[i] = z0;
-    zk[i] = zn;
-  }
-  if (own0) {  // uniform per block: Z0 = FFT_N(z0) of this angle, window into its own slot
-    line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
-#pragma unroll
-    for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
-    __syncthreads();
-    const int Xs = J.win[2 * (a * nC)];
-    float2* I = J.I + (size_t)(a * nS) * J.nWin * N;
-    for (int xl = t; xl < J.nWin; xl += T) {
-      int X = Xs + xl;
-      if (X >= W) X -= W;
-      const int m = paste_src<N>(X);
-      I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = m >= 0 ? bh[sidx(m)] : make_float2(0.f, 0.f);
-    }
-  }
+  for (int i = 0; i < EN; i++) zk[i] = mix(1, t + i * T);
   // pair (neg, pos): only the neg component is transformed and stored. With
   // z_pos = conj(z_neg) and opposite shifts (ro_pos = conj(ro_neg), re_pos = conj(re_neg)):
   //   E_pos[m] = conj(E_neg[-m]),
@@ -334,23 +304,9 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   const size_t quad = ((size_t)(xl >> 2) * N) * 4 + (xl & 3);
   float2* out = J.Tw + (size_t)comp * nWin * nWin + ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3);
   float2 x[EN];  // element t + i*T of this lane's column, in registers through the transforms
-  if (comp == 0) {  // band 0: summed over the angles in pass A (slot 0), or here
-    if (J.fold0) {
+  if (comp == 0) {  // band 0: summed over the angles and row-transformed in pass A (slot 0)
 #pragma unroll
-      for (int i = 0; i < EN; i++) x[i] = J.I[quad + (size_t)(t + i * T) * 4];
-    } else {
-#pragma unroll
-      for (int i = 0; i < EN; i++) {
-        const int k = t + i * T;
-        float2 v = make_float2(0.f, 0.f);
-        for (int a = 0; a < J.nA; a++) {
-          const float2 u = J.I[(size_t)a * nS * nWin * N + quad + (size_t)k * 4];
-          v.x += u.x;
-          v.y += u.y;
-        }
-        x[i] = v;
-      }
-    }
+    for (int i = 0; i < EN; i++) x[i] = J.I[quad + (size_t)(t + i * T) * 4];
     line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);
 #pragma unroll
     for (int i = 0; i < EN; i++) bh[sidx((t + i * T) * CB + lane)] = x[i];

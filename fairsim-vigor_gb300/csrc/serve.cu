@@ -152,8 +152,6 @@ struct fsim_server {
   uint64_t next_ticket = 1;
   std::vector<cudaStream_t> streams;
   std::vector<void*> ws;
-  std::vector<JobDesc*> tables;
-  std::vector<cudaEvent_t> table_ev;
   size_t ws_bytes = 0;
   int rr = 0;
   cudaStream_t refit_stream = nullptr;
@@ -214,8 +212,6 @@ static void worker_loop(fsim_server* s) {
       s->rr = (s->rr + 1) % (int)s->streams.size();
     }
     cudaStream_t st = s->streams[si];
-    // the job table of this stream is rewritten only after its previous upload ran
-    cudaEventSynchronize(s->table_ev[si]);
     std::vector<fsim_job> jobs(batch.size());
     std::vector<int> used_plan(batch.size());
     std::vector<int> refit_now;
@@ -237,8 +233,10 @@ static void worker_loop(fsim_server* s) {
       auto& sl = s->slots[i];
       cudaMemcpyAsync(sl.d_raw, sl.h_raw, s->ch[sl.channel].raw_bytes, cudaMemcpyHostToDevice, st);
     }
-    int rc = recon_batch(jobs.data(), (int)jobs.size(), s->ws[si], s->ws_bytes, st, s->tables[si], true);
-    cudaEventRecord(s->table_ev[si], st);
+    // the job table goes to the device as launch parameters (no copy engine, so the passes
+    // never wait behind another stream's uploads)
+    std::vector<JobDesc> table(batch.size());
+    int rc = recon_batch(jobs.data(), (int)jobs.size(), s->ws[si], s->ws_bytes, st, table.data(), true);
     for (size_t k = 0; k < batch.size(); k++) {
       auto& sl = s->slots[batch[k]];
       auto& c = s->ch[sl.channel];
@@ -420,13 +418,9 @@ static int serve_setup(fsim_server* s, const fsim_serve_config* cfg, const fsim_
   }
   s->streams.resize(cfg->streams);
   s->ws.resize(cfg->streams);
-  s->tables.resize(cfg->streams);
-  s->table_ev.resize(cfg->streams);
   for (int k = 0; k < cfg->streams; k++) {
     FSIM_CUDA(cudaStreamCreateWithFlags(&s->streams[k], cudaStreamNonBlocking));
     FSIM_CUDA(fsim::dev_alloc(&s->ws[k], s->ws_bytes));
-    FSIM_CUDA(cudaMallocHost(&s->tables[k], sizeof(JobDesc) * cfg->max_batch));
-    FSIM_CUDA(cudaEventCreateWithFlags(&s->table_ev[k], cudaEventDisableTiming));
   }
   FSIM_CUDA(cudaStreamCreateWithFlags(&s->refit_stream, cudaStreamNonBlocking));
   FSIM_CUDA(cudaDeviceSynchronize());
@@ -584,8 +578,6 @@ int fsim_serve_close(fsim_server* s) {
   }
   for (size_t k = 0; k < s->streams.size(); k++) {
     if (s->ws[k]) cudaFree(s->ws[k]);
-    if (s->tables[k]) cudaFreeHost(s->tables[k]);
-    if (s->table_ev[k]) cudaEventDestroy(s->table_ev[k]);
     if (s->streams[k]) cudaStreamDestroy(s->streams[k]);
   }
   for (auto& c : s->ch) {

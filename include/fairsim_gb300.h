@@ -210,10 +210,11 @@ typedef struct fsim_job {
 } fsim_job;
 /* Reconstruct n_jobs datasets (mixed sizes and plans allowed) with one set of launches per
  * size class; the size classes run side by side on library-owned streams forked from and
- * joined back into `stream`. workspace: device memory of at least the sum of
- * fsim_plan_workspace_bytes plus 256 bytes per job. Not for use inside a caller's stream
- * capture (its job table is staged through reused pinned buffers): record a batch with
- * fsim_batch_graph_create instead. */
+ * joined back into `stream`. workspace: 256-byte aligned device memory of at least the sum
+ * of fsim_plan_workspace_bytes plus 256 bytes per job. The job table travels as a kernel
+ * parameter (no copy engine: the passes never wait behind other streams' uploads). Not for
+ * use inside a caller's stream capture (the fork onto library streams is not capturable
+ * there): record a batch with fsim_batch_graph_create instead. */
 int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t workspace_bytes,
                      void* stream);
 /* Host-buffer batch (replaces the per-op Java-array copies of the accel vectors,
