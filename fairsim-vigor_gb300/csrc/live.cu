@@ -73,21 +73,36 @@ __global__ void __launch_bounds__(LCfg<N>::GA* LCfg<N>::TN) k_live_a(const JobDe
   const float* rawf = (const float*)J.raw;
   const uint16_t* rawu = (const uint16_t*)J.raw;
   const int nA = J.nA, nP = J.nP, nC = J.nC;
-  auto px = [&](int f, int x) {  // setFrom16bitPixels + times(dampBorder)
-    const size_t at = (size_t)f * frame + row + x;
-    float v = J.input_u16 ? (float)__ldg(&rawu[at]) : __ldg(&rawf[at]);
-    if (J.damp) v = __fmul_rn(v, __ldg(&J.damp[row + x]));
-    return v;
+  // setFrom16bitPixels + times(dampBorder) of the row of frame f at this thread's elements
+  // t + i*T; frames outer and elements inner, so that a row's E loads are in flight at once
+  auto px_row = [&](int f, float (&v)[E]) {
+    const size_t at = (size_t)f * frame + row + t;
+    if (J.input_u16) {
+#pragma unroll
+      for (int i = 0; i < E; i++) v[i] = (float)__ldg(&rawu[at + i * T]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < E; i++) v[i] = __ldg(&rawf[at + i * T]);
+    }
+    if (J.damp) {
+#pragma unroll
+      for (int i = 0; i < E; i++) v[i] = __fmul_rn(v[i], __ldg(&J.damp[row + t + i * T]));
+    }
   };
   if (J.widefield) {
     const float sc = 1.f / (float)(nA * nP);
+    float wf[E];
 #pragma unroll
-    for (int i = 0; i < E; i++) {
-      const int x = t + i * T;
-      float wf = 0.f;
-      for (int f = 0; f < nA * nP; f++) wf = __fadd_rn(wf, px(f, x));
-      J.widefield[row + x] = __fmul_rn(wf, sc);
+    for (int i = 0; i < E; i++) wf[i] = 0.f;
+#pragma unroll 1
+    for (int f = 0; f < nA * nP; f++) {
+      float v[E];
+      px_row(f, v);
+#pragma unroll
+      for (int i = 0; i < E; i++) wf[i] = __fadd_rn(wf[i], v[i]);
     }
+#pragma unroll
+    for (int i = 0; i < E; i++) J.widefield[row + t + i * T] = __fmul_rn(wf[i], sc);
   }
   __syncthreads();  // the twiddle table is staged
   for (int a = 0; a < nA; a++)
@@ -95,16 +110,17 @@ __global__ void __launch_bounds__(LCfg<N>::GA* LCfg<N>::TN) k_live_a(const JobDe
       const float2* coef = J.coef + (a * nC + c) * nP;
       float2 xv[E];  // element t + i*T of the line, in registers through the transform
 #pragma unroll
-      for (int i = 0; i < E; i++) {
-        const int x = t + i * T;
-        float2 z = make_float2(0.f, 0.f);
-        for (int p = 0; p < nP; p++) {
-          const float v = px(a * nP + p, x);
-          const float2 m = coef[p];
-          z.x += m.x * v;
-          z.y += m.y * v;
+      for (int i = 0; i < E; i++) xv[i] = make_float2(0.f, 0.f);
+#pragma unroll 1
+      for (int p = 0; p < nP; p++) {
+        float v[E];
+        px_row(a * nP + p, v);
+        const float2 m = coef[p];
+#pragma unroll
+        for (int i = 0; i < E; i++) {
+          xv[i].x += m.x * v[i];
+          xv[i].y += m.y * v[i];
         }
-        xv[i] = z;
       }
       line_fft_reg<N, T, 1, false>(xv, s, 0, t, tw);
       float2* X = J.I + (size_t)(a * nC + c) * frame + row;

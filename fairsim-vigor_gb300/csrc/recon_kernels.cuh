@@ -83,6 +83,33 @@ __host__ __device__ constexpr int col_min_blocks() {
   return EN <= 8 ? (65536 / (THREADS * REGS8) > 0 ? 65536 / (THREADS * REGS8) : 1)
                  : (EN == 12 ? (65536 / (THREADS * 80) > 0 ? 65536 / (THREADS * 80) : 1) : 1);
 }
+// Raw pixels fo + row + t + i*T (frame offset fo, row start row) with the background clip
+// and the border damping applied: all EN loads of the row are issued before any is used.
+template <int EN, int T>
+__device__ __forceinline__ void raw_row(const JobDesc& J, size_t fo, size_t row, int t, float (&v)[EN]) {
+  if (J.input_u16) {
+    const uint16_t* r = (const uint16_t*)J.raw + fo + row + t;
+#pragma unroll
+    for (int i = 0; i < EN; i++) v[i] = (float)__ldg(r + i * T);
+  } else {
+    const float* r = (const float*)J.raw + fo + row + t;
+#pragma unroll
+    for (int i = 0; i < EN; i++) v[i] = __ldg(r + i * T);
+  }
+  if (J.bgr != 0.f) {
+#pragma unroll
+    for (int i = 0; i < EN; i++) {
+      v[i] = v[i] - J.bgr;
+      if (v[i] < 0) v[i] = 0;
+    }
+  }
+  if (J.damp) {
+    const float* d = J.damp + row + t;
+#pragma unroll
+    for (int i = 0; i < EN; i++) v[i] = v[i] * __ldg(d + i * T);
+  }
+}
+
 template <int N, int ENV>
 __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>::T, Cfg<N, ENV>::EN>())
     k_pass_a(const JobDesc* __restrict__ jobs) {
@@ -109,19 +136,15 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     float2 x[EN];
 #pragma unroll
     for (int i = 0; i < EN; i++) x[i] = make_float2(0.f, 0.f);
+#pragma unroll 3
     for (int f = 0; f < nF; f++) {
+      float v[EN];
+      raw_row<EN, T>(J, f * frame, row, t, v);
       const float2 c = coef[f];
 #pragma unroll
       for (int i = 0; i < EN; i++) {
-        const size_t at = f * frame + row + t + i * T;
-        float v = J.input_u16 ? (float)__ldg((const uint16_t*)J.raw + at) : __ldg((const float*)J.raw + at);
-        if (J.bgr != 0.f) {  // background clip and border damping, as below
-          v = v - J.bgr;
-          if (v < 0) v = 0;
-        }
-        if (J.damp) v = v * __ldg(J.damp + row + t + i * T);
-        x[i].x += c.x * v;
-        x[i].y += c.y * v;
+        x[i].x += c.x * v[i];
+        x[i].y += c.y * v[i];
       }
     }
     line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
@@ -140,25 +163,24 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   if (nPair == 0) return;  // one band: the band-0 block above is the whole row pass
   for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
   __syncthreads();
-  auto raw_at = [&](int p, int x) {  // background clip and border damping of one raw pixel
-    const size_t at = (size_t)(a * nP + p) * frame + row + x;
-    float v = J.input_u16 ? (float)__ldg((const uint16_t*)J.raw + at) : __ldg((const float*)J.raw + at);
-    if (J.bgr != 0.f) {
-      v = v - J.bgr;
-      if (v < 0) v = 0;
-    }
-    if (J.damp) v = v * __ldg(J.damp + row + x);
-    return v;
-  };
-  auto mix = [&](int cm, int x) {  // band separation in real space (pairs after the first)
-    float2 z = make_float2(0.f, 0.f);
+  // band separation in real space of component cm for this thread's elements t + i*T: the
+  // phases outer, so that every element's load of a phase row is in flight at once (pass A
+  // 0.61 ms per 64 datasets of 512^2 3x3, 0.94 ms with the elements outer and one load in
+  // flight; 0.63 ms with three phase rows per round, which spills)
+  auto mix = [&](int cm, float2 (&z)[EN]) {
+#pragma unroll
+    for (int i = 0; i < EN; i++) z[i] = make_float2(0.f, 0.f);
+#pragma unroll 1
     for (int p = 0; p < nP; p++) {
+      float v[EN];
+      raw_row<EN, T>(J, (size_t)(a * nP + p) * frame, row, t, v);
       const float2 m = coef[cm * nP + p];
-      const float v = raw_at(p, x);
-      z.x += m.x * v;
-      z.y += m.y * v;
+#pragma unroll
+      for (int i = 0; i < EN; i++) {
+        z[i].x += m.x * v[i];
+        z[i].y += m.y * v[i];
+      }
     }
-    return z;
   };
   // Components: band 0, then per band b the pair neg = 2b-1, pos = 2b. The separation
   // coefficients of a pair are complex conjugates, so z_pos = conj(z_neg): the pos
@@ -167,8 +189,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   // scratch.
   // the band pairs of this block's angle (band 0 of every angle is the blockIdx.y == nA block's)
   float2 x[EN], zk[EN];  // zk: the first pair's neg component, kept for the even-sample product
-#pragma unroll
-  for (int i = 0; i < EN; i++) zk[i] = mix(1, t + i * T);
+  mix(1, zk);
   // pair (neg, pos): only the neg component is transformed and stored. With
   // z_pos = conj(z_neg) and opposite shifts (ro_pos = conj(ro_neg), re_pos = conj(re_neg)):
   //   E_pos[m] = conj(E_neg[-m]),
@@ -179,10 +200,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   // forms it from the neg windows (mirror images of the pos windows) and d, kept here.
   for (int b = 1; b <= nPair; b++) {
     const int cn = 2 * b - 1;
-    if (b > 1) {
-#pragma unroll
-      for (int i = 0; i < EN; i++) zk[i] = mix(cn, t + i * T);
-    }
+    if (b > 1) mix(cn, zk);
 #pragma unroll
     for (int i = 0; i < EN; i++) x[i] = zk[i];
     __syncthreads();  // the previous window reads of bh and bz are done
