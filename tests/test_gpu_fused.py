@@ -229,6 +229,38 @@ def test_batch_graph_replays_match_batch(fs, torch_cuda):
     g.close()
 
 
+def test_job_table_over_several_parameter_blocks(fs, torch_cuda):
+    """A batch whose job table exceeds one launch-parameter block (400 jobs, about 70 KB of
+    descriptors) is written by several table launches: every job's result equals its
+    result alone, through the batch entry and through a recorded graph."""
+    torch = torch_cuda
+    n, n_jobs = 64, 400
+    plans, raws = [], []
+    for seed in (150, 151, 152):
+        raw, truth, sp = make(fs, n, seed)
+        plans.append(fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=4))
+        raws.append(raw)
+    alone = [device_alone(fs, torch, p, r) for p, r in zip(plans, raws)]
+    d_raw = [torch.from_numpy(r).cuda() for r in raws]
+    d_out = torch.zeros((n_jobs, 2 * n, 2 * n), dtype=torch.float32, device="cuda")
+    job_plans = [plans[k % 3] for k in range(n_jobs)]
+    ws = torch.empty(fs.plan.batch_workspace_bytes(job_plans), dtype=torch.uint8, device="cuda")
+    jobs = [(job_plans[k], d_raw[k % 3].data_ptr(), d_out[k].data_ptr()) for k in range(n_jobs)]
+    fs.plan.recon_batch(jobs, ws.data_ptr(), ws.numel())
+    torch.cuda.synchronize()
+    out = d_out.cpu().numpy()
+    for k in range(n_jobs):
+        assert np.array_equal(out[k], alone[k % 3]), k
+    d_out.zero_()
+    g = fs.plan.BatchGraph(jobs, ws.data_ptr(), ws.numel())
+    g.launch()
+    torch.cuda.synchronize()
+    out = d_out.cpu().numpy()
+    for k in range(n_jobs):
+        assert np.array_equal(out[k], alone[k % 3]), k
+    g.close()
+
+
 @pytest.mark.parametrize("pinned", [True, False])
 def test_recon_batch_host_matches_single(fs, torch_cuda, pinned):
     """Host-buffer batches (overlapped upload / passes / download in chunks) give the same
