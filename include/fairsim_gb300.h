@@ -233,7 +233,8 @@ typedef struct fsim_host_job {
 } fsim_host_job;
 int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int chunk);
 /* A fixed batch recorded once as a CUDA graph (no reference counterpart): the job-table
- * copy and every size class's passes, with the classes on parallel branches. Replays
+ * write (the table is a parameter of the recorded launch) and every size class's passes,
+ * with the classes on parallel branches. Replays
  * (fsim_batch_graph_launch) reconstruct the same jobs' current raw buffers into the same
  * outputs. Plans, raw/out buffers and the workspace must stay allocated while the graph
  * exists; fsim_plan_update keeps a plan's table addresses, so replays pick up new
