@@ -325,16 +325,16 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   if (comp == 0) {  // band 0: summed over the angles and row-transformed in pass A (slot 0)
 #pragma unroll
     for (int i = 0; i < EN; i++) x[i] = J.I[quad + (size_t)(t + i * T) * 4];
-    line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);
+    line_fft_reg<N, T, CB, false, true>(x, bh, lane, t, twN);
 #pragma unroll
-    for (int i = 0; i < EN; i++) bh[sidx((t + i * T) * CB + lane)] = x[i];
+    for (int i = 0; i < EN; i++) bh[sidx_t<true>((t + i * T) * CB + lane)] = x[i];
     __syncthreads();
     const int Ys = J.win[1];
     for (int yl = t; yl < nWin; yl += T) {
       int Y = Ys + yl;
       if (Y >= W) Y -= W;
       const int m = paste_src<N>(Y);
-      out[(size_t)yl * 4] = m >= 0 ? bh[sidx(m * CB + lane)] : make_float2(0.f, 0.f);
+      out[(size_t)yl * 4] = m >= 0 ? bh[sidx_t<true>(m * CB + lane)] : make_float2(0.f, 0.f);
     }
     return;
   }
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   const float2* I = J.I + (size_t)(a * nS + b) * nWin * N + quad;
 #pragma unroll
   for (int i = 0; i < EN; i++) x[i] = I[(size_t)(t + i * T) * 4];
-  line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);  // Z along y
+  line_fft_reg<N, T, CB, false, true>(x, bh, lane, t, twN);  // Z along y
   if (t == (N / 2) % T) {
     const float2 z = x[(N / 2) / T];
     J.Dy[(size_t)(comp - 1) * nWin + xl] = make_float2(-2.f * z.y, -2.f * z.x);
@@ -352,25 +352,25 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   // odd samples, iFFT_N(Z * s), times the odd-sample ramp, FFT: O
 #pragma unroll
   for (int i = 0; i < EN; i++) x[i] = cmul(x[i], half_shift<N>(twW, t + i * T));
-  line_fft_reg<N, T, CB, true>(x, bh, lane, t, twN);
+  line_fft_reg<N, T, CB, true, true>(x, bh, lane, t, twN);
 #pragma unroll
   for (int i = 0; i < EN; i++) x[i] = cmul(x[i], __ldg(ro + t + i * T));
-  line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);
+  line_fft_reg<N, T, CB, false, true>(x, bh, lane, t, twN);
 #pragma unroll
-  for (int i = 0; i < EN; i++) bh[sidx((t + i * T) * CB + lane)] = x[i];
+  for (int i = 0; i < EN; i++) bh[sidx_t<true>((t + i * T) * CB + lane)] = x[i];
   // even samples (the column again, from L2) times the even-sample ramp, FFT: E
 #pragma unroll
   for (int i = 0; i < EN; i++) x[i] = cmul(I[(size_t)(t + i * T) * 4], __ldg(re + t + i * T));
-  line_fft_reg<N, T, CB, false>(x, bz, lane, t, twN);
+  line_fft_reg<N, T, CB, false, true>(x, bz, lane, t, twN);
 #pragma unroll
-  for (int i = 0; i < EN; i++) bz[sidx((t + i * T) * CB + lane)] = x[i];
+  for (int i = 0; i < EN; i++) bz[sidx_t<true>((t + i * T) * CB + lane)] = x[i];
   __syncthreads();
   const int Yn = J.win[2 * (a * nC + cn) + 1];
   for (int yl = t; yl < nWin; yl += T) {
     int Y = Yn + yl;
     if (Y >= W) Y -= W;
     const int m = Y < N ? Y : Y - N;
-    out[(size_t)yl * 4] = cadd(bz[sidx(m * CB + lane)], cmul(twW[Y], bh[sidx(m * CB + lane)]));
+    out[(size_t)yl * 4] = cadd(bz[sidx_t<true>(m * CB + lane)], cmul(twW[Y], bh[sidx_t<true>(m * CB + lane)]));
   }
 }
 
@@ -482,8 +482,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
     xe[i] = cadd(u0, u1);
     xo[i] = cmul(csub(u0, u1), cconjf(twW[k]));
   }
-  line_fft_reg<N, T, CB, true>(xe, bz, lane, t, twN);
-  line_fft_reg<N, T, CB, true>(xo, bh, lane, t, twN);
+  line_fft_reg<N, T, CB, true, true>(xe, bz, lane, t, twN);
+  line_fft_reg<N, T, CB, true, true>(xo, bh, lane, t, twN);
 #pragma unroll
   for (int i = 0; i < EN; i++) {
     const int k = t + i * T;
