@@ -12,7 +12,8 @@
 // The host carves chunk i's slot only after passes(i-K) finished with it, so the host runs
 // at most K chunks ahead. The job tables travel as kernel parameters: a table upload on the
 // compute stream would queue behind the raw-frame uploads on the one host-to-device copy
-// engine and serialize the passes with them. The call returns when every output is in host memory.
+// engine and serialize the passes with them. The call returns when every output is in host
+// memory.
 // Host buffers that are page-locked (cudaHostAlloc / cudaHostRegister) are copied by DMA
 // directly; pageable ones make each copy synchronous on the host.
 #include <algorithm>
