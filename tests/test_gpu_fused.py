@@ -229,6 +229,23 @@ def test_batch_graph_replays_match_batch(fs, torch_cuda):
     g.close()
 
 
+def test_misaligned_workspace_refused_before_device_work(fs, torch_cuda):
+    """The job table is written to the workspace head with 16-byte stores: a workspace that
+    is not 256-byte aligned is refused (EINVAL) before anything is launched."""
+    torch = torch_cuda
+    raw, truth, sp = make(fs, 64, 160)
+    plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=4)
+    d_raw = torch.from_numpy(raw).cuda()
+    d_out = torch.zeros((128, 128), dtype=torch.float32, device="cuda")
+    need = fs.plan.batch_workspace_bytes([plan])
+    ws = torch.empty(need + 256, dtype=torch.uint8, device="cuda")
+    with pytest.raises(ValueError, match="aligned"):
+        fs.plan.recon_batch([(plan, d_raw.data_ptr(), d_out.data_ptr())], ws.data_ptr() + 16, need + 240)
+    fs.plan.recon_batch([(plan, d_raw.data_ptr(), d_out.data_ptr())], ws.data_ptr(), need + 256)
+    torch.cuda.synchronize()
+    assert np.array_equal(d_out.cpu().numpy(), device_alone(fs, torch, plan, raw))
+
+
 def test_job_table_over_several_parameter_blocks(fs, torch_cuda):
     """A batch whose job table exceeds one launch-parameter block (400 jobs, about 70 KB of
     descriptors) is written by several table launches: every job's result equals its
