@@ -121,3 +121,21 @@ def test_band_zero_sum_over_angles_is_one_transform():
     per_angle = sum(np.fft.fft(np.tensordot(c0[a], raw[a], axes=1)) for a in range(nA))
     folded = np.fft.fft(np.einsum("ap,apn->n", c0, raw))
     assert np.allclose(per_angle, folded, atol=1e-12)
+
+
+@pytest.mark.parametrize("N", [16, 48, 64])
+def test_real_output_row_from_hermitian_halves(N):
+    """The widefield output pass (csrc/widefield.cu, WC) keeps only the real part of the
+    2N-point inverse of a pasted row V: its even samples are Re(iFFT_N(a))/2 with a = V, its
+    odd samples Re(iFFT_N(b))/2 with b = V * s. Re(iFFT(a)) = iFFT(Ha) with the Hermitian
+    half Ha[k] = (a[k] + conj(a[-k]))/2, so one transform of Ha + i Hb gives both rows."""
+    rng = np.random.default_rng(5)
+    V = rng.normal(size=N) + 1j * rng.normal(size=N)
+    m = np.arange(N)
+    s = np.exp(1j * np.pi * np.where(m < N // 2, m, m - N) / N)
+    full = np.real(np.fft.ifft(paste(V, N)))
+    a, b = V, V * s
+    herm = lambda c: (c + np.conj(c[(-m) % N])) / 2  # noqa: E731
+    y = np.fft.ifft(herm(a) + 1j * herm(b)) / 2
+    assert np.allclose(full[0::2], y.real, atol=1e-13)
+    assert np.allclose(full[1::2], y.imag, atol=1e-13)
