@@ -317,7 +317,7 @@ def main():
         e2e_step()
     e2e_steps = max(3, args.steps // 2)
     # three timed repetitions, the median reported: single wall-clock runs of the host path
-    # occasionally lose half their rate to the host (seen on this pool: 6.7k and 7.6k
+    # occasionally lose half their rate to the host (measured on GB300: 6.7k and 7.6k
     # between neighbours at 13.3-13.7k)
     e2e_runs = sorted(wall(e2e_step, e2e_steps) for _ in range(3))
     e2e_ms = e2e_runs[1]
