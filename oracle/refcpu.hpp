@@ -2,7 +2,7 @@
 //
 // CPU restatement of fairSIM's 2D SIM reconstruction path (the Java code under
 // org/fairsim/{linalg,sim_algorithm,livemode}), used by the tests, by smoke() and by
-// the CPU-baseline leg of bench.py as the checker. The GPU library never links it.
+// the CPU-baseline leg of bench.py to compare against. The GPU library never links it.
 //
 // Two instantiations:
 //   T = float   reproduces the reference's single-precision semantics: float vectors,

@@ -1,7 +1,7 @@
 """ORACLE - test infrastructure only (tests/ and nothing else import it).
 
-A plain-Python restatement of the reference's live-stream ingest, used as the checker of
-the library's fsim_livesim_* / fsim_seqx_* entry points:
+A plain-Python restatement of the reference's live-stream ingest, the oracle the tests
+compare the library's fsim_livesim_* / fsim_seqx_* entry points against:
 
 * LIVESIM header write / parse: org/fairsim/transport/ImageWrapper.java:418-478
   (little endian, header-definition.md), pixels: getPixels (:265-278, Java's signed byte
