@@ -102,6 +102,159 @@ class OtfProvider:
             ret.switchAttenuation(True)
         return ret
 
+    # ---- the reference's instance API: sample tables, scalar lookups, vector writers ------
+
+    SAMPLES_ESTIMATE = 512  # samplesLateral of an estimated OTF (S/OtfProvider.java:45)
+    vecCyclesPerMicron = -1.0
+
+    @staticmethod
+    def valIdealOTF(dist: float) -> float:
+        """OtfProvider.valIdealOTF (S/OtfProvider.java:74-78): the OTF of an aberration-free
+        lens with a circular pupil, dist in [0, 1] of the cutoff (0 outside)."""
+        if dist < 0 or dist > 1:
+            return 0.0
+        return (2 / math.pi) * (math.acos(dist) - dist * math.sqrt(1 - dist * dist))
+
+    @staticmethod
+    def valAttenuation(dist: float, strength: float, fwhm: float) -> float:
+        """OtfProvider.valAttenuation (S/OtfProvider.java:238-240), a float in the reference."""
+        import numpy as np
+
+        return float(np.float32(1 - strength * math.exp(-(dist ** 2) / (2 * (fwhm / 2.355) ** 2))))
+
+    def setPixelSize(self, cyclesPerMicron: float) -> None:
+        """OtfProvider.setPixelSize (S/OtfProvider.java:226-230): frequency spacing of the
+        vectors the writers below fill, in cycles/micron."""
+        if cyclesPerMicron <= 0:
+            raise ValueError("pxl size must be positive")
+        self.vecCyclesPerMicron = float(cyclesPerMicron)
+
+    def setAttenuationStrength(self, strength: float) -> None:
+        self.setAttenuation(strength, self.attFWHM)
+
+    def setAttenuationFWHM(self, fwhm: float) -> None:
+        self.setAttenuation(self.attStrength, fwhm)
+
+    def getAttStr(self, band: int = 0) -> float:
+        return self.attStrength
+
+    def getAttFWHM(self, band: int = 0) -> float:
+        return self.attFWHM
+
+    def isMultiBand(self) -> bool:
+        return self.measured is not None and len(self.measured["bands"]) > 1
+
+    def _tables(self):
+        """(cycles per sample, vals, valsOnlyAtt, valsAtt) as float32 arrays [band][sample]:
+        fromEstimate's samples (S/OtfProvider.java:105-120) or the measured bands, and the
+        attenuation cache of setAttenuation (:276-287)."""
+        import numpy as np
+
+        if self.measured is None:
+            ns = self.SAMPLES_ESTIMATE
+            cps = self.getCutoff() / ns
+            v = np.array([[np.float32(self.valIdealOTF(i / ns) * (self.a ** (i / ns))) for i in range(ns)]],
+                         dtype=np.complex64)
+        else:
+            cps = self.measured["cycles"]
+            v = np.array(self.measured["bands"], dtype=np.complex64)
+        only = np.array([[self.valAttenuation(i * cps, self.attStrength, self.attFWHM) for i in range(v.shape[1])]],
+                        dtype=np.float32).repeat(v.shape[0], axis=0)
+        att = (v.real * only + 1j * (v.imag * only)).astype(np.complex64)
+        return cps, v, only, att
+
+    def _band(self, band: int, nbands: int) -> int:
+        if not self.isMultiBand():
+            band = 0
+        if band >= nbands or band < 0:
+            raise IndexError("band idx too high or <0")
+        return band
+
+    def getOtfVal(self, band: int, cycl: float, att: bool) -> complex:
+        """OtfProvider.getOtfVal (S/OtfProvider.java:189-222): the sample at floor(pos)
+        (its 'interpolation' weighs the lower sample twice: (1-f)*v + f*v in float)."""
+        import numpy as np
+
+        cps, v, _, va = self._tables()
+        band = self._band(band, v.shape[0])
+        if cycl < 0:
+            raise IndexError("cylc negative!")
+        if cycl >= self.getCutoff():
+            return 0j
+        pos = cycl / cps
+        if math.ceil(pos) >= v.shape[1]:
+            return 0j
+        lpos = int(math.floor(pos))
+        f = np.float32(pos - lpos)
+        z = (va if att else v)[band][lpos]
+        lo = np.complex64(complex(np.float32(z.real * (np.float32(1) - f)), np.float32(z.imag * (np.float32(1) - f))))
+        hi = np.complex64(complex(np.float32(z.real * f), np.float32(z.imag * f)))
+        return complex(np.float32(lo.real + hi.real), np.float32(lo.imag + hi.imag))
+
+    def getAttVal(self, band: int, cycl: float) -> float:
+        """OtfProvider.getAttVal (S/OtfProvider.java:246-269): 1 beyond the cutoff, else the
+        attenuation sample at floor(pos) weighed f + (1-f) in float."""
+        import numpy as np
+
+        cps, v, only, _ = self._tables()
+        band = self._band(band, v.shape[0])
+        if cycl < 0:
+            raise IndexError("cylc negative!")
+        if cycl >= self.getCutoff():
+            return 1.0
+        pos = cycl / cps
+        lpos = int(math.floor(pos))
+        f = np.float32(pos - lpos)
+        s = only[band][lpos]
+        return float(np.float32(np.float32(s * f) + np.float32(s * (np.float32(1) - f))))
+
+    def printState(self, html: bool = False) -> str:
+        """OtfProvider.printState (S/OtfProvider.java:165-176)."""
+        lam = "λ<sub>em</sub>" if html else "lambda"
+        ret = "NA %4.2f, %s %4.0f, " % (self.na, lam, self.emWavelength)
+        return ret + ("(est., a=%4.2f)" % self.a if self.isEstimate else "(from file)")
+
+    def _vector_param(self, vec):
+        """A parameter record that gives the library this OTF and a vector frequency spacing
+        of vecCyclesPerMicron (the library's spacing is 1/(w * micronsPerPixel))."""
+        if self.vecCyclesPerMicron <= 0:
+            raise RuntimeError("Vector pixel size not initialized")
+        nb = max(2, len(self.measured["bands"]) if self.isMultiBand() else 2)
+        return SimParam.create(nb, 1, 2 * nb - 1, vec.w, 1.0 / (vec.w * self.vecCyclesPerMicron), self)
+
+    def otfToVector(self, vec, band: int, kx: float, ky: float, useAtt: bool, write: bool) -> None:
+        """OtfProvider.otfToVector (S/OtfProvider.java:331-373), in the library."""
+        from .algorithm import OtfVectors
+
+        OtfVectors.otfToVector(self._vector_param(vec), vec, band, kx, ky, useAtt, write)
+
+    def applyOtf(self, vec, band: int, kx: float = 0.0, ky: float = 0.0) -> None:
+        self.otfToVector(vec, band, kx, ky, self.useAttenuation, False)
+
+    def writeOtfVector(self, vec, band: int, kx: float, ky: float) -> None:
+        self.otfToVector(vec, band, kx, ky, False, True)
+
+    def writeOtfWithAttVector(self, vec, band: int, kx: float, ky: float) -> None:
+        self.otfToVector(vec, band, kx, ky, self.useAttenuation, True)
+
+    def writeApoVector(self, vec, bend: float, cutOff: float) -> None:
+        """OtfProvider.writeApoVector (S/OtfProvider.java:437-492), in the library."""
+        from .algorithm import OtfVectors
+
+        OtfVectors.writeApoVector(self._vector_param(vec), vec, bend, cutOff)
+
+    def writeAttenuationVector(self, vec, strength: float, fwhm: float, kx: float, ky: float) -> None:
+        """OtfProvider.writeAttenuationVector (S/OtfProvider.java:503-529), in the library."""
+        from .algorithm import OtfVectors
+
+        OtfVectors.writeAttenuationVector(self._vector_param(vec), vec, strength, fwhm, kx, ky)
+
+    def maskOtf(self, vec, kx: float, ky: float) -> None:
+        """OtfProvider.maskOtf (S/OtfProvider.java:538-559), in the library."""
+        from .algorithm import OtfVectors
+
+        OtfVectors.maskOtf(self._vector_param(vec), vec, kx, ky)
+
     def saveConfig(self, cfg) -> None:
         """OtfProvider.saveConfig (S/OtfProvider.java:636-676) into folder ``cfg``."""
         from .conf import to_bytes
