@@ -336,6 +336,39 @@ class Dir:
     def nrComp(self) -> int:
         return 2 * self.nrBands - 1
 
+    def nrBand(self) -> int:
+        return self.nrBands
+
+    def nrPha(self) -> int:
+        return self.nrPhases
+
+    def _fail_band(self, b: int) -> None:
+        if b < 0 or b >= self.nrBands:  # Dir.failBand (S/SimParam.java:429-432)
+            raise IndexError("Wrong band index")
+
+    def getPhase(self, i: int) -> float:
+        """Phase i without the offset (S/SimParam.java:485-487)."""
+        base = self.phases or [(2 * math.pi / self.nrPhases) * k for k in range(self.nrPhases)]
+        return base[i]
+
+    def resetPhases(self) -> None:
+        """Back to equidistant phases (S/SimParam.java:463-467)."""
+        self.phases = None
+
+    def getPxPyAngle(self, band: int) -> float:
+        """atan2 of band's shift (S/SimParam.java:573-576)."""
+        self._fail_band(band)
+        return math.atan2(self.pY * band, self.pX * band)
+
+    def getPxPyLen(self, band: int) -> float:
+        """Length of band's shift (S/SimParam.java:584-587)."""
+        self._fail_band(band)
+        return math.hypot(self.pY * band, self.pX * band)
+
+    def getRawModulations(self) -> List[float]:
+        """Modulations without the [0.3, 1.1] clamp (S/SimParam.java:609-613)."""
+        return list(self.modul)
+
 
 class SimParam:
     """2D subset of ``SimParam`` (S/SimParam.java:31-615)."""
@@ -357,6 +390,7 @@ class SimParam:
         self.filterStyle = FILTER_WIENER  # SimParam.FilterStyle ordinal
         self.rlIterations = 5
         self.imgSeq = "PAZ"  # IMGSEQ name (input order of the raw frames, stored only)
+        self.clipScale = "BOTH"  # CLIPSCALE name (BOTH, CLIP, NONE), stored only (S/SimParam.java:62-63)
         self.paramDate = 0   # "timestamp" of the parameter set, ms since 1970
 
     @staticmethod
@@ -386,6 +420,27 @@ class SimParam:
 
     def getFilterStyle(self) -> int:
         return self.filterStyle
+
+    def getImgSeq(self) -> str:
+        return self.imgSeq
+
+    def setImgSeq(self, seq: str) -> "SimParam":
+        """SimParam.setImgSeq: "PAZ", "PZA" or "ZAP" (S/SimParam.java:223-226, 753-756)."""
+        if seq not in ("PAZ", "PZA", "ZAP"):
+            raise ValueError("unknown image order %r" % (seq,))
+        self.imgSeq = seq
+        return self
+
+    def getClipScale(self) -> str:
+        return self.clipScale
+
+    def setClipScale(self, mode: str) -> "SimParam":
+        """SimParam.setClipScale: "BOTH", "CLIP" or "NONE" (S/SimParam.java:234-237, 735-738);
+        runReconstruction takes it as 2 / 1 / 0."""
+        if mode not in ("BOTH", "CLIP", "NONE"):
+            raise ValueError("unknown clip/scale mode %r" % (mode,))
+        self.clipScale = mode
+        return self
 
     def useWienerFilter(self) -> bool:
         return self.filterStyle in (FILTER_WIENER, FILTER_RL_IN)

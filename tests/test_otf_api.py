@@ -96,3 +96,30 @@ def test_vector_writers_need_a_pixel_size(fs):
 def test_print_state(fs):
     otf = fs.OtfProvider.fromEstimate(1.4, 525, 0.3)
     assert otf.printState() == "NA 1.40, lambda  525, (est., a=0.30)"
+
+
+def test_dir_and_param_accessors(fs):
+    """SimParam.Dir's shift, phase and modulation accessors (S/SimParam.java:429-613) and the
+    stored image order / clip-scale settings (:219-237)."""
+    sp = param(fs)
+    d = sp.dir(0)
+    d.setPxPy(30.0, -40.0)  # stored per band step: /(nBands - 1)
+    assert (d.nrBand(), d.nrPha(), d.nrComp()) == (2, 3, 3)
+    assert d.getPxPyLen(1) == pytest.approx(50.0) and d.getPxPyAngle(1) == pytest.approx(math.atan2(-40, 30))
+    assert d.getPxPyLen(0) == 0.0
+    with pytest.raises(IndexError):
+        d.getPxPyLen(2)
+    d.setPhaOff(0.5)
+    assert d.getPhase(1) == pytest.approx(2 * math.pi / 3) and d.getPhases()[1] == pytest.approx(2 * math.pi / 3 + 0.5)
+    d.setPhases([0.1, 2.0, 4.1], False)
+    assert d.getPhase(2) == 4.1
+    d.resetPhases()
+    assert d.getPhase(2) == pytest.approx(4 * math.pi / 3)
+    d.setModulation(1, 1.7)
+    assert d.getRawModulations() == [1.0, 1.7] and d.getModulations() == [1.0, 1.1]
+    assert sp.getImgSeq() == "PAZ" and sp.getClipScale() == "BOTH"
+    assert sp.setImgSeq("ZAP").getImgSeq() == "ZAP" and sp.setClipScale("NONE").getClipScale() == "NONE"
+    with pytest.raises(ValueError):
+        sp.setImgSeq("XYZ")
+    with pytest.raises(ValueError):
+        sp.setClipScale("SOME")
