@@ -65,6 +65,30 @@ class WienerFilter:
 
 class BandSeparation:
     @staticmethod
+    def createSeparationMatrix(phases, bands, fac=None) -> np.ndarray:
+        """createSeparationMatrix (BandSeparation.java:40-114): the inverse (or pseudo-inverse)
+        phase matrix, (2*bands-1) x nPhases complex. ``phases``: the phases of band 1, or the
+        reference's per-band rows [bands-1][nPhases], whose band-b row must be b times the
+        first (the only form separateBands builds)."""
+        ph = np.asarray(phases, dtype=np.float64)
+        if ph.ndim == 2:
+            if ph.shape[0] != bands - 1:
+                raise ValueError("#factors or #phases+1 != #bands")
+            for b in range(1, bands - 1):
+                if not np.allclose(ph[b], (b + 1) * ph[0], rtol=0, atol=1e-12):
+                    raise ValueError("band %d phases are not %d times the first band's" % (b + 1, b + 1))
+            ph = ph[0]
+        ph = np.ascontiguousarray(ph)
+        if fac is not None and len(fac) != bands:
+            raise ValueError("#factors or #phases+1 != #bands")
+        fa = None if fac is None else np.ascontiguousarray(fac, dtype=np.float64)
+        out = np.zeros((2 * bands - 1, len(ph), 2), dtype=np.float64)
+        N.check(N.lib().fsim_separation_matrix(ph.ctypes.data_as(C.c_void_p), len(ph), int(bands),
+                                               None if fa is None else fa.ctypes.data_as(C.c_void_p),
+                                               out.ctypes.data_as(C.c_void_p)))
+        return out[..., 0] + 1j * out[..., 1]
+
+    @staticmethod
     def separateBands(inp, out, phases, bands, fac=None):
         """separateBands(in, out, phases[] | phaOff, bands, fac) (BandSeparation.java:131-197)."""
         if np.isscalar(phases):

@@ -182,3 +182,30 @@ int validate_param(const fsim_sim_param* p) {
 }
 
 }  // namespace fsim
+
+// BandSeparation.createSeparationMatrix (S/BandSeparation.java:40-114) for the phases of
+// band 1 (band b's phases are b times them): the inverse (nP == 2*bands-1) or pseudo-inverse
+// of the phase matrix, [component][phase] interleaved complex doubles. Host-only.
+extern "C" int fsim_separation_matrix(const double* phases, int n_phases, int bands, const double* fac,
+                                      double* out) {
+  if (!phases || !out) {
+    fsim::set_error("separation_matrix: null argument");
+    return FSIM_EINVAL;
+  }
+  if (bands < 2 || bands > FSIM_MAX_BANDS) {
+    fsim::set_error("#bands < 2, not useful");
+    return FSIM_EINVAL;
+  }
+  if (n_phases < 2 * bands - 1 || n_phases > FSIM_MAX_PHASES) {
+    fsim::set_error("not enough phases for #bands");
+    return FSIM_EINVAL;
+  }
+  std::vector<double> ph(phases, phases + n_phases), fc;
+  if (fac) fc.assign(fac, fac + bands);
+  const std::vector<fsim::cd> m = fsim::separation_matrix(ph, bands, fc);
+  for (size_t i = 0; i < m.size(); i++) {
+    out[2 * i] = m[i].real();
+    out[2 * i + 1] = m[i].imag();
+  }
+  return FSIM_OK;
+}

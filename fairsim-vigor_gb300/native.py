@@ -231,6 +231,7 @@ _SIGS = {
     "fsim_mask_otf": (I32, [VP, VP, F64, F64]),
     "fsim_wiener_denominator": (I32, [VP, VP, F64]),
     "fsim_separate_bands": (I32, [VP, I32, VP, I32, VP, I32, VP]),
+    "fsim_separation_matrix": (I32, [VP, I32, I32, VP, VP]),
     "fsim_common_region": (I32, [VP, VP, VP, F64, F64, F64, F64, I32]),
     "fsim_locate_peak": (I32, [VP, F64, VP]),
     "fsim_fit_peak": (I32, [VP, VP, VP, F64, F64, F64, F64, VP, VP]),

@@ -148,6 +148,11 @@ int fsim_attenuation_vector(fsim_vec* v, const fsim_sim_param* p, double str, do
 int fsim_mask_otf(fsim_vec* v, const fsim_sim_param* p, double kx, double ky);                /* :538-559 */
 /* WienerFilter.getDenominator (WienerFilter.java:88-122): out is real 2w x 2w */
 int fsim_wiener_denominator(fsim_vec* out, const fsim_sim_param* p, double wiener);
+/* BandSeparation.createSeparationMatrix (BandSeparation.java:40-114) for the phases of band 1
+ * (band b at b times them), fac (bands entries) nullable: the inverse or, with more phases
+ * than components, the pseudo-inverse, out = (2*bands-1) x n_phases complex doubles
+ * (re, im interleaved, component-major). Host-only: needs no device. */
+int fsim_separation_matrix(const double* phases, int n_phases, int bands, const double* fac, double* out);
 /* BandSeparation.separateBands (BandSeparation.java:131-165), phases of band 1, fac nullable */
 int fsim_separate_bands(fsim_vec* const* in, int n_in, fsim_vec* const* out, int n_out,
                         const double* phases, int bands, const double* fac);

@@ -123,3 +123,19 @@ def test_dir_and_param_accessors(fs):
         sp.setImgSeq("XYZ")
     with pytest.raises(ValueError):
         sp.setClipScale("SOME")
+
+
+@pytest.mark.parametrize("n_pha,bands,fac", [(3, 2, None), (5, 2, [1.0, 0.7]), (5, 3, [1.0, 0.8, 0.6])])
+def test_separation_matrix_host_entry_vs_oracle(fs, oracle, n_pha, bands, fac):
+    """BandSeparation.createSeparationMatrix through the host-only C entry (no device):
+    equal to the oracle's restatement, and its inverse property."""
+    rng = np.random.default_rng(11)
+    phases = [2 * math.pi * i / n_pha + 0.3 + 0.01 * rng.normal() for i in range(n_pha)]
+    got = fs.algorithm.BandSeparation.createSeparationMatrix(phases, bands, fac)
+    exp = oracle.separation_matrix(phases, bands, fac)
+    assert got.shape == (2 * bands - 1, n_pha)
+    assert np.allclose(got, exp, rtol=0, atol=1e-12)
+    per_band = [[(b + 1) * p for p in phases] for b in range(bands - 1)]  # the reference's 2D form
+    assert np.array_equal(fs.algorithm.BandSeparation.createSeparationMatrix(per_band, bands, fac), got)
+    with pytest.raises(ValueError):
+        fs.algorithm.BandSeparation.createSeparationMatrix(phases[:2 * bands - 2], bands, fac)
