@@ -270,7 +270,8 @@ extern "C" {
 
 int fsim_otf_to_vector(fsim_vec* v, const fsim_sim_param* p, int band, double kx, double ky, int use_att, int write) {
   NEED_INIT();
-  (void)band;  // single-band estimate OTF: the band index is ignored (OtfProvider.java:191-192)
+  // band: a measured multi-band table's band; an estimated (single-band) OTF ignores it
+  // (OtfProvider.java:191-192)
   FSIM_REQUIRE(v && v->cplx, FSIM_EINVAL, "otfToVector: complex vector required");
   int rc = validate_param(p);
   if (rc) return rc;
