@@ -82,9 +82,13 @@ __global__ void k_times_cr(float2* __restrict__ y, const float* __restrict__ x, 
 __global__ void k_times_rr(float* __restrict__ y, const float* __restrict__ x, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) y[i] *= x[i];
 }
+// AbstractVectorCplx.scal(Cplx.Float): multReal / multImag with separate roundings
+// (L/AbstractVectorCplx.java:228-236,402-408; no FMA contraction)
 __global__ void k_scal_c(float2* y, size_t n, float re, float im) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    y[i] = cmul(make_float2(re, im), y[i]);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float2 v = y[i];
+    y[i] = make_float2(__fsub_rn(__fmul_rn(re, v.x), __fmul_rn(im, v.y)), __fadd_rn(__fmul_rn(im, v.x), __fmul_rn(re, v.y)));
+  }
 }
 __global__ void k_scal_r(float* y, size_t n, float a) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) y[i] *= a;

@@ -215,6 +215,23 @@ def test_run_reconstruction_op_by_op_vs_oracle(V, oracle, fs, n):
     assert rel_l2(out, exp64) < 1e-5   # vs the FP64 oracle
 
 
+@pytest.mark.parametrize("clip", [1, 2])
+def test_run_reconstruction_clip_scale_vs_oracle(V, oracle, fs, clip):
+    """runReconstruction's CLIPSCALE.CLIP and .BOTH outputs (SimUtils.spatial ->
+    clipAndScale, S/SimUtils.java:146-153,244-264; BOTH is the reference's default)."""
+    n = 256
+    raw, truth = fs.synth.make_dataset(n=n, seed=19)
+    sp = fs.synth.sim_param_for(truth, n)
+    spec = oracle.prepare_raw(sp, raw)
+    exp = oracle.recon(sp, spec, clip_scale=clip)
+    inFFT = [[cvec(V, spec[a * 3 + p]) for p in range(3)] for a in range(3)]
+    out = fs.algorithm.SimAlgorithm.runReconstruction(sp, inFFT, False, clip).vectorData()
+    assert out.min() >= 0
+    assert rel_l2(out, exp) < 1e-4
+    if clip == 2:
+        assert abs(out.max() - 255.0) < 1e-3 and abs(exp.max() - 255.0) < 1e-3
+
+
 def test_accel_natives_set_get_reshape_plan_buffers(fs, V):
     """The remaining accel natives: nativeSet/nativeGet (element access), vectors allocated
     by element count and shaped by the call that needs a shape, nativeCreatePlan2d, and
@@ -363,3 +380,58 @@ def test_measured_otf_estimation_vs_oracle(V, oracle, fs):
         assert abs(sp.dir(d).pX - est["pX"][d]) < 1e-9 and abs(sp.dir(d).pY - est["pY"][d]) < 1e-9
         assert abs(sp.dir(d).phaOff - est["phaOff"][d]) < 1e-4
         assert abs(sp.dir(d).modul[1] - est["modulations"][d][1]) < 1e-4
+
+
+def test_vector_ops_vs_reference_stdc_fixture(V):
+    """The device kernels against the reference's own standard-C vector backend
+    (accel/stdC_cplx.c, accel/stdC_real.c; outputs in tests/golden/stdc_vector_ops.npz, made
+    by tests/golden/make_stdc_golden.py): element-wise ops and pasteFreq bit for bit,
+    reductions to float-square rounding, fourierShift to the reference's float-phase
+    rounding."""
+    import os
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden"))
+    import make_stdc_golden as G
+    fx = dict(np.load(os.path.join(here, "golden", "stdc_vector_ops.npz")))
+    a, b, r, s = fx["a"], fx["b"], fx["r"], fx["s"]
+
+    def run_c(op):
+        v = cvec(V, a)
+        op(v)
+        return v.vectorData()
+
+    assert np.array_equal(run_c(lambda v: v.add(cvec(V, b))), fx["c_add"])
+    assert np.array_equal(run_c(lambda v: v.axpy(G.AXPY_A, cvec(V, b))), fx["c_axpy"])
+    assert np.array_equal(run_c(lambda v: v.times(cvec(V, b))), fx["c_times"])
+    assert np.array_equal(run_c(lambda v: v.timesConj(cvec(V, b))), fx["c_times_conj"])
+    assert np.array_equal(run_c(lambda v: v.times(rvec(V, r))), fx["c_times_real"])
+    assert np.array_equal(run_c(lambda v: v.scal(G.SCAL_A)), fx["c_scal"])
+    # squares in float as AbstractVectorCplx.norm2 (linalg/AbstractVectorCplx.java:241-247);
+    # the stdC backend squares in double
+    assert abs(cvec(V, a).norm2() - fx["c_norm2"]) <= 1e-6 * fx["c_norm2"]
+    vc = V.Vec2dCplx(a.shape[1], a.shape[0])
+    vc.copy(rvec(V, r))
+    assert np.array_equal(vc.vectorData(), fx["c_from_real"])
+
+    def run_r(op):
+        v = rvec(V, r)
+        op(v)
+        return v.vectorData()
+
+    assert np.array_equal(run_r(lambda v: v.add(rvec(V, s))), fx["r_add"])
+    assert np.array_equal(run_r(lambda v: v.axpy(G.REAL_A, rvec(V, s))), fx["r_axpy"])
+    assert np.array_equal(run_r(lambda v: v.times(rvec(V, s))), fx["r_times"])
+    assert np.array_equal(run_r(lambda v: v.scal(G.REAL_A)), fx["r_scal"])
+    assert abs(rvec(V, r).sumElements() - fx["r_sum"]) <= 1e-9 * np.abs(r).sum()
+    assert abs(rvec(V, r).norm2() - fx["r_norm2"]) <= 1e-6 * fx["r_norm2"]
+    for i, (wi, wo, xo, yo) in enumerate(G.PASTE):
+        out = V.Vec2dCplx(wo, wo)
+        out.pasteFreq(cvec(V, fx["paste_in_%d" % i]), xo, yo)
+        assert np.array_equal(out.vectorData(), fx["paste_out_%d" % i]), i
+    for i, (N, kx, ky) in enumerate(G.SHIFTS):
+        v = cvec(V, fx["shift_in_%d" % i])
+        v.fourierShift(kx, ky)
+        # the library reduces the phase modulo one turn in double; the reference rounds it
+        # to float first (an error that grows with |k|)
+        assert rel_l2(v.vectorData(), fx["shift_out_%d" % i]) < 1e-5, i
