@@ -3,14 +3,13 @@
 // S/SimAlgorithm.java:37-159; the live refit of LM/ReconstructionRunner.java:642-746).
 //
 // The 10x10 sub-pixel grid of fitPeak is evaluated in two passes instead of 100 shifted
-// vector copies: the shift phase ramp is separable, so
-//   corr(xi, yi) = sum_y ty[yi](y) * sum_x tx[xi](x) * b1(x,y) * conj(b0(x,y)),
-// first 10 row sums per image row (one block per row), then the 100 column sums.
-// Both passes accumulate in FP64 in a fixed order (deterministic).
+// vector copies (corr_grid.cuh): row sums per image row, then the column sums, in a fixed
+// order (deterministic).
 #include <cmath>
 #include <vector>
 
 #include "common.cuh"
+#include "corr_grid.cuh"
 #include "estimate.cuh"
 #include "filters.cuh"
 #include "otf.cuh"
@@ -137,78 +136,6 @@ __global__ void k_peak_partial(const float2* __restrict__ v, int w, int h, doubl
   }
 }
 
-// ---- correlation grid ---------------------------------------------------------------------
-// ramp tables: tx[j][x] = exp(+2 pi i * kxj * x / N), ty[j][y] = exp(+2 pi i * kyj * y / N)
-// (fourierShift(xpos, -ypos) => ky_j = -ypos_j), phases reduced modulo one turn in double.
-__global__ void k_ramp_table(float2* __restrict__ tab, const double* __restrict__ k, int nk, int N) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  if (x >= N || j >= nk) return;
-  double f = k[j] * (double)x / (double)N;
-  f -= floor(f);
-  double s, c;
-  sincospi(2.0 * f, &s, &c);
-  tab[(size_t)j * N + x] = make_float2((float)c, (float)s);
-}
-
-// pass 1: Q[j][y] = sum_x b1(x,y) conj(b0(x,y)) tx[j][x], one block per row
-template <int NK>
-__global__ void k_corr_rows(const float2* __restrict__ b0, const float2* __restrict__ b1, const float2* __restrict__ tx,
-                            int N, double2* __restrict__ Q) {
-  const int y = blockIdx.x;
-  double2 acc[NK];
-#pragma unroll
-  for (int j = 0; j < NK; j++) acc[j] = make_double2(0, 0);
-  for (int x = threadIdx.x; x < N; x += blockDim.x) {
-    size_t i = (size_t)y * N + x;
-    float2 p = cmulc(b1[i], b0[i]);  // b1 * conj(b0)
-#pragma unroll
-    for (int j = 0; j < NK; j++) {
-      float2 r = cmul(p, tx[(size_t)j * N + x]);
-      acc[j].x += r.x;
-      acc[j].y += r.y;
-    }
-  }
-  __shared__ double2 red[NK][32];
-#pragma unroll
-  for (int j = 0; j < NK; j++) {
-    double a = acc[j].x, b = acc[j].y;
-    for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_down_sync(0xffffffffu, a, o);
-      b += __shfl_down_sync(0xffffffffu, b, o);
-    }
-    if (threadIdx.x % 32 == 0) red[j][threadIdx.x / 32] = make_double2(a, b);
-  }
-  __syncthreads();
-  if (threadIdx.x < NK) {
-    double a = 0, b = 0;
-    for (int k = 0; k < (int)(blockDim.x / 32); k++) {
-      a += red[threadIdx.x][k].x;
-      b += red[threadIdx.x][k].y;
-    }
-    Q[(size_t)threadIdx.x * N + y] = make_double2(a, b);
-  }
-}
-
-// pass 2: corr[jy][jx] = sum_y Q[jx][y] * ty[jy][y], one warp per output
-__global__ void k_corr_cols(const double2* __restrict__ Q, const float2* __restrict__ ty, int N, int nkx, int nky,
-                            double scal, double2* __restrict__ out) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
-  if (warp >= nkx * nky) return;
-  const int jx = warp % nkx, jy = warp / nkx;
-  double a = 0, b = 0;
-  for (int y = lane; y < N; y += 32) {
-    double2 q = Q[(size_t)jx * N + y];
-    float2 t = ty[(size_t)jy * N + y];
-    a += q.x * t.x - q.y * t.y;
-    b += q.x * t.y + q.y * t.x;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_down_sync(0xffffffffu, a, o);
-    b += __shfl_down_sync(0xffffffffu, b, o);
-  }
-  if (lane == 0) out[warp] = make_double2(a * scal, b * scal);  // Cplx.mult(sum, (scal,0))
-}
-
 // ---- host side ------------------------------------------------------------------------------
 int common_region_device(float2* b0, float2* b1, int w, int h, const OtfTable* t, double kx, double ky, double dist,
                          double wl, bool divide, cudaStream_t st, int bn0, int bn1) {
@@ -296,18 +223,13 @@ void EstScratch::free(cudaStream_t st) {
 // sign flip of ky) on real-space b0/b1 already prepared; out[yi*nx + xi].
 int corr_grid_device(const float2* b0, const float2* b1, int N, const double* kxs, int nx, const double* kys, int ny,
                      double scal, EstScratch& s, cudaStream_t st, std::vector<std::complex<double>>& out) {
-  double k[20];
+  FSIM_REQUIRE(nx >= 1 && nx <= CORR_MAX_K && ny >= 1 && ny <= CORR_MAX_K, FSIM_EINVAL,
+               "correlation grid: %d x %d beyond %d x %d", nx, ny, CORR_MAX_K, CORR_MAX_K);
+  double k[2 * CORR_MAX_K] = {0};
   for (int i = 0; i < nx; i++) k[i] = kxs[i];
-  for (int i = 0; i < ny; i++) k[10 + i] = -kys[i];
-  FSIM_CUDA(cudaMemcpyAsync(s.kbuf, k, sizeof(double) * 20, cudaMemcpyHostToDevice, st));
-  k_ramp_table<<<dim3(div_up(N, 128), nx), 128, 0, st>>>(s.tx, s.kbuf, nx, N);
-  k_ramp_table<<<dim3(div_up(N, 128), ny), 128, 0, st>>>(s.ty, s.kbuf + 10, ny, N);
-  if (nx == 10)
-    k_corr_rows<10><<<N, 256, 0, st>>>(b0, b1, s.tx, N, s.Q);
-  else
-    k_corr_rows<1><<<N, 256, 0, st>>>(b0, b1, s.tx, N, s.Q);
-  int warps = nx * ny;
-  k_corr_cols<<<div_up(warps * 32, 256), 256, 0, st>>>(s.Q, s.ty, N, nx, ny, scal, s.corr);
+  for (int i = 0; i < ny; i++) k[CORR_MAX_K + i] = -kys[i];
+  FSIM_CUDA(cudaMemcpyAsync(s.kbuf, k, sizeof(k), cudaMemcpyHostToDevice, st));
+  launch_corr_grid(b0, b1, N, s.kbuf, nx, ny, scal, s.tx, s.ty, s.Q, s.corr, st);
   FSIM_CHECK_LAUNCH();
   std::vector<double2> h(nx * ny);
   FSIM_CUDA(cudaMemcpyAsync(h.data(), s.corr, sizeof(double2) * nx * ny, cudaMemcpyDeviceToHost, st));

@@ -2,25 +2,26 @@
 // allocation.
 //
 // Some callers cannot allocate device memory while they run this step: a real-time
-// acquisition thread whose latency budget has no room for the allocator, code that is
-// being captured into a CUDA graph, or a host process (for example a JVM behind JNI) whose
-// device memory was partitioned up front. The regular fit (fsim_fit_peak and the
+// acquisition thread, whose latency budget has no room for the allocator and its
+// synchronisation, or a host process (for example a JVM behind JNI) whose device memory
+// was partitioned up front, so that an allocation in the middle of a run could fail or
+// take memory another component counts on. The regular fit (fsim_fit_peak and the
 // estimation entry points) allocates its scratch per call; this entry point keeps that
 // scratch in one file-scope device array instead and touches no allocator.
 //
 // It evaluates, for real-space bands b0, b1 (the inverse FFTs of the common-region bands,
 // as Correlation.fitPeak prepares them), the grid
 //   out[yi][xi] = scal * sum_{x,y} b1(x,y) conj(b0(x,y)) exp(+2 pi i (kx[xi] x - ky[yi] y)/n)
-// with the same kernels' arithmetic as the allocating fit (separable phase ramps reduced
-// modulo one turn in double; row sums, then column sums, accumulated in FP64 in a fixed
-// order), so its results equal the allocating path's bit for bit.
+// with the allocating fit's kernels (corr_grid.cuh), so its results equal the allocating
+// path's bit for bit.
 //
 // Limits and sharing: n <= 2048, 1 <= nx, ny <= 10. The scratch (about 0.66 MB) is one
 // static array per GPU that loads the library and stays allocated until the process
 // exits. Every call reuses it and it keeps the previous call's contents; nothing in it
 // needs to start at zero (each call rewrites every entry it reads). Calls whose work
 // overlaps on the GPU (two host threads, or two streams in flight) race on the scratch and
-// must be serialised by the caller.
+// must be serialised by the caller. The call is synchronous: it returns once the grid is
+// in `out`.
 //
 // Set-up: the first call on a device (with that device current) looks up the array's
 // device address with cudaGetSymbolAddress and caches it per device; make that first call
@@ -29,11 +30,12 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "corr_grid.cuh"
 
 namespace {
 
 constexpr int NA_MAX_N = 2048;
-constexpr int NA_MAX_K = 10;
+constexpr int NA_MAX_K = fsim::CORR_MAX_K;
 constexpr size_t NA_TX = 0;                                              // float2 [K][N]
 constexpr size_t NA_TY = NA_TX + sizeof(float2) * NA_MAX_K * NA_MAX_N;   // float2 [K][N]
 constexpr size_t NA_Q = NA_TY + sizeof(float2) * NA_MAX_K * NA_MAX_N;    // double2 [K][N]
@@ -45,73 +47,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
 std::mutex g_na_mu;
 void* g_na_addr[64] = {nullptr};
-
-__global__ void k_na_ramp(float2* __restrict__ tab, const double* __restrict__ k, int nk, int n) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  if (x >= n || j >= nk) return;
-  double f = k[j] * (double)x / (double)n;
-  f -= floor(f);
-  double s, c;
-  sincospi(2.0 * f, &s, &c);
-  tab[(size_t)j * n + x] = make_float2((float)c, (float)s);
-}
-
-template <int NK>
-__global__ void k_na_rows(const float2* __restrict__ b0, const float2* __restrict__ b1, const float2* __restrict__ tx,
-                          int n, double2* __restrict__ Q) {
-  const int y = blockIdx.x;
-  double2 acc[NK];
-#pragma unroll
-  for (int j = 0; j < NK; j++) acc[j] = make_double2(0, 0);
-  for (int x = threadIdx.x; x < n; x += blockDim.x) {
-    const size_t i = (size_t)y * n + x;
-    const float2 p = fsim::cmulc(b1[i], b0[i]);
-#pragma unroll
-    for (int j = 0; j < NK; j++) {
-      const float2 r = fsim::cmul(p, tx[(size_t)j * n + x]);
-      acc[j].x += r.x;
-      acc[j].y += r.y;
-    }
-  }
-  __shared__ double2 red[NK][32];
-#pragma unroll
-  for (int j = 0; j < NK; j++) {
-    double a = acc[j].x, b = acc[j].y;
-    for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_down_sync(0xffffffffu, a, o);
-      b += __shfl_down_sync(0xffffffffu, b, o);
-    }
-    if (threadIdx.x % 32 == 0) red[j][threadIdx.x / 32] = make_double2(a, b);
-  }
-  __syncthreads();
-  if (threadIdx.x < NK) {
-    double a = 0, b = 0;
-    for (int k = 0; k < (int)(blockDim.x / 32); k++) {
-      a += red[threadIdx.x][k].x;
-      b += red[threadIdx.x][k].y;
-    }
-    Q[(size_t)threadIdx.x * n + y] = make_double2(a, b);
-  }
-}
-
-__global__ void k_na_cols(const double2* __restrict__ Q, const float2* __restrict__ ty, int n, int nkx, int nky,
-                          double scal, double2* __restrict__ out) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
-  if (warp >= nkx * nky) return;
-  const int jx = warp % nkx, jy = warp / nkx;
-  double a = 0, b = 0;
-  for (int y = lane; y < n; y += 32) {
-    const double2 q = Q[(size_t)jx * n + y];
-    const float2 t = ty[(size_t)jy * n + y];
-    a += q.x * t.x - q.y * t.y;
-    b += q.x * t.y + q.y * t.x;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_down_sync(0xffffffffu, a, o);
-    b += __shfl_down_sync(0xffffffffu, b, o);
-  }
-  if (lane == 0) out[warp] = make_double2(a * scal, b * scal);
-}
 
 }  // namespace
 
@@ -154,18 +89,11 @@ extern "C" int fsim_corr_grid_noalloc(const void* b0, const void* b1, int n, con
   double2* corr = reinterpret_cast<double2*>(s + NA_CORR);
   double* kv = reinterpret_cast<double*>(s + NA_KV);
   // fourierShift(xpos, -ypos): the y ramp uses -ky
-  double k[2 * NA_MAX_K];
+  double k[2 * NA_MAX_K] = {0};
   for (int i = 0; i < nx; i++) k[i] = kx[i];
   for (int i = 0; i < ny; i++) k[NA_MAX_K + i] = -ky[i];
   FSIM_CUDA(cudaMemcpyAsync(kv, k, sizeof(k), cudaMemcpyHostToDevice, st));
-  k_na_ramp<<<dim3((n + 127) / 128, nx), 128, 0, st>>>(tx, kv, nx, n);
-  k_na_ramp<<<dim3((n + 127) / 128, ny), 128, 0, st>>>(ty, kv + NA_MAX_K, ny, n);
-  // grids of 2..9 columns run the 10-wide kernel; the unused rows of Q are never read
-  if (nx == 1)
-    k_na_rows<1><<<n, 256, 0, st>>>((const float2*)b0, (const float2*)b1, tx, n, Q);
-  else
-    k_na_rows<10><<<n, 256, 0, st>>>((const float2*)b0, (const float2*)b1, tx, n, Q);
-  k_na_cols<<<(nx * ny * 32 + 255) / 256, 256, 0, st>>>(Q, ty, n, nx, ny, scal, corr);
+  fsim::launch_corr_grid((const float2*)b0, (const float2*)b1, n, kv, nx, ny, scal, tx, ty, Q, corr, st);
   FSIM_CHECK_LAUNCH();
   FSIM_CUDA(cudaMemcpyAsync(out, corr, sizeof(double2) * nx * ny, cudaMemcpyDeviceToHost, st));
   FSIM_CUDA(cudaStreamSynchronize(st));

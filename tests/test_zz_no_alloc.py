@@ -1,17 +1,40 @@
 """The allocation-free correlation sweep (fsim_corr_grid_noalloc), called through the C ABI.
 
-Callers that cannot allocate device memory mid-run (real-time acquisition threads, work
-captured into a CUDA graph, processes with pre-partitioned device memory) use this entry
-point; its scratch is a static device array. Its grid must equal the first iteration grid
-of the allocating fit (fsim_fit_peak) on the same bands, on two calls in a row (the second
-call reuses the scratch the first one left behind). This file is collected last so that a
-run stopping at the first failure has run every other test before it."""
+Callers that cannot allocate device memory mid-run use this entry point: a real-time
+acquisition thread, whose latency budget has no room for the allocator, or a process whose
+device memory was partitioned up front. Its scratch is a static device array. Its grid must
+equal the first iteration grid of the allocating fit (fsim_fit_peak) on the same bands, bit
+for bit, on two calls in a row (the second call reuses the scratch the first one left
+behind); smaller grids and the largest size are checked against a direct FP64 evaluation.
+This file is collected last so that a run stopping at the first failure has run every other
+test before it."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+
+def _noalloc(N_, b0_ptr, b1_ptr, n, kxs, kys, scal):
+    kxs = np.ascontiguousarray(kxs, dtype=np.float64)
+    kys = np.ascontiguousarray(kys, dtype=np.float64)
+    out = np.zeros((len(kys), len(kxs), 2))
+    rc = N_.lib().fsim_corr_grid_noalloc(
+        C.c_void_p(b0_ptr), C.c_void_p(b1_ptr), n, kxs.ctypes.data_as(C.c_void_p), len(kxs),
+        kys.ctypes.data_as(C.c_void_p), len(kys), C.c_double(scal), out.ctypes.data_as(C.c_void_p), None)
+    N_.check(rc)
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def _grid_fp64(b0, b1, kxs, kys, scal):
+    """scal * sum_{x,y} b1 conj(b0) exp(+2 pi i (kx x - ky y)/n), separably in FP64."""
+    n = b0.shape[0]
+    p = b1.astype(np.complex128) * np.conj(b0.astype(np.complex128))
+    x = np.arange(n)
+    tx = np.exp(2j * np.pi * np.outer(kxs, x) / n)   # [jx][x]
+    ty = np.exp(-2j * np.pi * np.outer(kys, x) / n)  # [jy][y]
+    return scal * (ty @ (p @ tx.T))                   # [jy][jx]
 
 
 def test_noalloc_grid_matches_fit_peak_twice(fs, oracle):
@@ -45,24 +68,48 @@ def test_noalloc_grid_matches_fit_peak_twice(fs, oracle):
     kxs = np.array([kx + ((i - 4.5) / 4.5) * search for i in range(10)])
     kys = np.array([ky + ((i - 4.5) / 4.5) * search for i in range(10)])
     for call in range(2):
-        out = np.zeros((10, 10, 2))
-        rc = N_.lib().fsim_corr_grid_noalloc(
-            C.c_void_p(b0.device_ptr()), C.c_void_p(b1.device_ptr()), n,
-            kxs.ctypes.data_as(C.c_void_p), 10, kys.ctypes.data_as(C.c_void_p), 10,
-            C.c_double(scal), out.ctypes.data_as(C.c_void_p), None)
-        N_.check(rc)
-        got = out[..., 0] + 1j * out[..., 1]
-        assert np.abs(got - expect).max() <= 1e-12 * np.abs(expect).max(), call
+        got = _noalloc(N_, b0.device_ptr(), b1.device_ptr(), n, kxs, kys, scal)
+        assert np.array_equal(got, expect), call
+    # grids narrower than 10 (1 x 1, 3 x 7) right after a 10 x 10 call, whose ramps and row
+    # sums are still in the scratch, against a direct FP64 evaluation
+    h0, h1 = b0.vectorData(), b1.vectorData()
+    for gx, gy in ((1, 1), (3, 7), (7, 3)):
+        _noalloc(N_, b0.device_ptr(), b1.device_ptr(), n, kxs, kys, scal)
+        got = _noalloc(N_, b0.device_ptr(), b1.device_ptr(), n, kxs[:gx], kys[:gy], scal)
+        ref = _grid_fp64(h0, h1, kxs[:gx], kys[:gy], scal)
+        assert got.shape == (gy, gx)
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), (gx, gy)
+
+
+def test_noalloc_largest_size_vs_fp64(fs, torch_cuda):
+    """n = 2048, the largest size the static scratch holds, twice in a row."""
+    torch = torch_cuda
+    N_ = fs.native
+    N_.init(0)
+    n = 2048
+    rng = np.random.default_rng(7)
+    b0 = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    b1 = (0.5 * np.roll(b0, (3, -5), axis=(0, 1)) + 0.1 * rng.standard_normal((n, n))).astype(np.complex64)
+    d0 = torch.from_numpy(b0.view(np.float32)).cuda()
+    d1 = torch.from_numpy(b1.view(np.float32)).cuda()
+    kxs = np.array([5.0 + (i - 4.5) / 4.5 * 0.5 for i in range(10)])
+    kys = np.array([-3.0 + (i - 4.5) / 4.5 * 0.5 for i in range(10)])
+    scal = 1.0 / float(np.sum(np.abs(b0.astype(np.complex128)) ** 2))
+    ref = _grid_fp64(b0, b1, kxs, kys, scal)
+    for call in range(2):
+        got = _noalloc(N_, d0.data_ptr(), d1.data_ptr(), n, kxs, kys, scal)
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), call
 
 
 def test_noalloc_rejects_sizes_beyond_scratch(fs):
     N_ = fs.native
     N_.init(0)
-    k = np.zeros(10)
-    out = np.zeros(200)
+    k = np.zeros(11)
+    out = np.zeros(242)
     dummy = C.c_void_p(1)
-    rc = N_.lib().fsim_corr_grid_noalloc(dummy, dummy, 4096, k.ctypes.data_as(C.c_void_p), 10,
-                                         k.ctypes.data_as(C.c_void_p), 10, C.c_double(1.0),
-                                         out.ctypes.data_as(C.c_void_p), None)
-    assert rc == N_.FSIM_EINVAL
-    assert b"static scratch" in N_.lib().fsim_last_error()
+    for n, nx, ny in ((4096, 10, 10), (256, 11, 10), (256, 10, 0)):
+        rc = N_.lib().fsim_corr_grid_noalloc(dummy, dummy, n, k.ctypes.data_as(C.c_void_p), nx,
+                                             k.ctypes.data_as(C.c_void_p), ny, C.c_double(1.0),
+                                             out.ctypes.data_as(C.c_void_p), None)
+        assert rc == N_.FSIM_EINVAL
+        assert b"static scratch" in N_.lib().fsim_last_error()
