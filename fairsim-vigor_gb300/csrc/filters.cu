@@ -178,13 +178,16 @@ __global__ void k_separate(const SepArgs a, size_t n) {
 
 // ---- host helpers ------------------------------------------------------------------------
 static std::mutex g_otf_mu;
+std::mutex& otf_table_mutex() { return g_otf_mu; }
 
+// The caller holds otf_table_mutex() from this call until the kernel that reads the table
+// is enqueued: another thread's upload waits for the device before it overwrites the
+// staging table, and only enqueued work is waited for.
 int upload_otf_table(const fsim_sim_param* p, OtfTable** dev, cudaStream_t st) {
   Ctx& c = ctx();
   static OtfTable* buf = nullptr;
   static OtfTable* host = nullptr;
   static double key[7] = {0, 0, 0, 0, 0, 0, 0};
-  std::lock_guard<std::mutex> g(g_otf_mu);
   if (!buf) FSIM_CUDA(fsim::dev_alloc(&buf, sizeof(OtfTable)));
   if (!host) FSIM_CUDA(cudaMallocHost(&host, sizeof(OtfTable)));
   const double k[7] = {p->na, p->em_wavelength, p->otf_a, p->att_strength, p->att_fwhm, (double)p->w,
@@ -275,7 +278,12 @@ int fsim_otf_to_vector(fsim_vec* v, const fsim_sim_param* p, int band, double kx
   FSIM_REQUIRE(v && v->cplx, FSIM_EINVAL, "otfToVector: complex vector required");
   int rc = validate_param(p);
   if (rc) return rc;
+  // getOtfVal's check (OtfProvider.java:191-194): a multi-band measured table indexes its
+  // bands with `band`, so it must name one of them; other tables collapse it to band 0
+  FSIM_REQUIRE(!(otf_measured(p) && p->otf_bands > 1) || (band >= 0 && band < p->otf_bands), FSIM_EINVAL,
+               "otfToVector: band idx too high or <0 (%d of %d bands)", band, p->otf_bands);
   OtfTable* t;
+  std::lock_guard<std::mutex> g(otf_table_mutex());
   rc = upload_otf_table(p, &t, ctx().stream);
   if (rc) return rc;
   return otf_vector_device(reinterpret_cast<float2*>(v->d), v->w, v->h, t, band, kx, ky, use_att != 0, write != 0,
@@ -319,6 +327,7 @@ int fsim_wiener_denominator(fsim_vec* out, const fsim_sim_param* p, double wiene
   FSIM_REQUIRE(out && !out->cplx && out->w == 2 * p->w && out->h == 2 * p->w, FSIM_EINVAL,
                "Wiener denominator: real 2w x 2w vector required");
   OtfTable* t;
+  std::lock_guard<std::mutex> g(otf_table_mutex());
   rc = upload_otf_table(p, &t, ctx().stream);
   if (rc) return rc;
   return wiener_denominator_device(out->d, p, wiener, t, true, ctx().stream);

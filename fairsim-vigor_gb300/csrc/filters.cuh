@@ -1,6 +1,8 @@
 // Internal interface of the filter builders (filters.cu).
 #pragma once
 
+#include <mutex>
+
 #include "common.cuh"
 #include "otf.cuh"
 
@@ -20,7 +22,9 @@ struct SepArgs {
   float2 coef[SEP_MAX_OUT * FSIM_MAX_PHASES];
 };
 
-// Stream-ordered upload of a SimParam's OTF table into the shared staging buffer.
+// Stream-ordered upload of a SimParam's OTF table into the shared staging buffer; the
+// caller holds otf_table_mutex() until the kernels that read the table are enqueued.
+std::mutex& otf_table_mutex();
 int upload_otf_table(const fsim_sim_param* p, OtfTable** dev, cudaStream_t st);
 int wiener_denominator_device(float* out, const fsim_sim_param* p, double wiener, const OtfTable* t, bool reciprocal,
                               cudaStream_t st);

@@ -17,7 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SHIM = os.path.join(ROOT, "fairsim-vigor_gb300", "jni", "fsim_jni.cpp")
 WRAPPER = os.path.join(ROOT, "fairsim-vigor_gb300", "jni", "org", "fairsim", "gb300", "FusedSim.java")
-REF_ACCEL = "/root/reference/org/fairsim/accel"
+# the reference project's accel sources, when a checkout is at hand (FSIM_REFERENCE_ROOT)
+REF_ACCEL = os.path.join(os.environ.get("FSIM_REFERENCE_ROOT", "/nonexistent"), "org", "fairsim", "accel")
 
 
 def exported_symbols():
@@ -70,7 +71,7 @@ def test_shim_exports_every_native_of_its_wrapper():
     assert not missing, missing
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_ACCEL), reason="reference sources not present")
+@pytest.mark.skipif(not os.path.isdir(REF_ACCEL), reason="FSIM_REFERENCE_ROOT unset or without the accel sources")
 def test_shim_exports_every_native_of_the_reference_accel_classes():
     files = [f for f in glob.glob(os.path.join(REF_ACCEL, "*.java")) if not os.path.basename(f).startswith("Test")]
     want = set()
@@ -162,7 +163,7 @@ def test_shim_signatures_match_its_wrapper():
     assert check_signatures(java) == []
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_ACCEL), reason="reference sources not present")
+@pytest.mark.skipif(not os.path.isdir(REF_ACCEL), reason="FSIM_REFERENCE_ROOT unset or without the accel sources")
 def test_shim_signatures_match_the_reference_accel_classes():
     java = {}
     for f in glob.glob(os.path.join(REF_ACCEL, "*.java")):
