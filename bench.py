@@ -174,9 +174,11 @@ def run_reference(args):
 
 # DRAM bytes (read + write) per dataset of each pass at 512^2 3x3, from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum) of this program's passes on a 16-dataset
-# batch (raw 151 MB, larger than L2); per-launch traffic = this x the batch size.
-TRAFFIC_PER_DATASET = {"k_pass_a<512>": 15.98e6, "k_pass_g+k_pass_b1<512>": 11.16e6, "k_pass_b2<512>": 22.86e6,
-                       "k_pass_c<512>": 10.70e6}
+# batch (raw 151 MB, larger than L2); per-launch traffic = this x the batch size. None where
+# the pass has not been captured in its current form.
+TRAFFIC_PER_DATASET = {"k_pass_a<512>": 15.98e6, "k_pass_g+k_pass_b1<512>": 11.16e6, "k_pass_b2<512>": None,
+                       "k_pass_c<512>": None}
+PASS_NAMES = ["k_pass_a<512>", "k_pass_g+k_pass_b1<512>", "k_pass_b2<512>", "k_pass_c<512>"]
 
 
 def pass_bytes(n=N, n_dirs=NA, n_phases=NP, n_bands=NB, na=1.4, lam=525.0, pxl=0.08):
@@ -186,10 +188,12 @@ def pass_bytes(n=N, n_dirs=NA, n_phases=NP, n_bands=NB, na=1.4, lam=525.0, pxl=0
              summed, once; each angle's pair neg components), plus one Nyquist term per row (D)
       G+B1   D in, one column per angle and pair out (G); I in, the column-transformed windows
              Tw (band 0, neg of every pair) and one Nyquist term per neg column (Dy) out
-      B2     Tw (read for the neg and, mirrored, for the pos component), OTF masks (band 0
-             once, neg and pos of every pair), Wiener x apodization, G, Dy in; the W x W
-             column-transformed plane O out
-      C      O in, the W x W image out"""
+      B2     over the Hermitian half's columns 0..N: Tw (each neg window column once: at X for
+             the neg component, at -X for the pos one; band 0 half a window), the OTF masks
+             (a pair's neg and pos windows are mirror images, so together they cover one
+             window's columns; band 0 half a window), the Wiener x apodization table, G, Dy
+             in; the W x (N+1) Hermitian half out
+      C      the Hermitian half in, the W x W image out"""
     npair = n_bands - 1
     W = 2 * n
     R = (2 * na / (lam / 1000.0)) / (1.0 / (n * pxl))
@@ -199,11 +203,12 @@ def pass_bytes(n=N, n_dirs=NA, n_phases=NP, n_bands=NB, na=1.4, lam=525.0, pxl=0
     G = n_dirs * npair * nwin * 8
     Tw = (1 + n_dirs * npair) * nwin * nwin * 8
     Dy = n_dirs * npair * nwin * 8
-    masks = (1 + 2 * n_dirs * npair) * nwin * nwin * 4
+    masks = (0.5 + n_dirs * npair) * nwin * nwin * 4
+    OH = W * (n + 1) * 8
     a = n_dirs * n_phases * n * n * 4 + I + D
     b1 = D + G + I + Tw + Dy
-    b2 = Tw + n_dirs * npair * nwin * nwin * 8 + masks + W * W * 4 + G + Dy + W * W * 8
-    c = W * W * 8 + W * W * 4
+    b2 = (0.5 + n_dirs * npair) * nwin * nwin * 8 + masks + (n + 1) * W * 4 + G + Dy + OH
+    c = OH + W * W * 4
     return [a, b1, b2, c]
 
 
@@ -347,7 +352,7 @@ def main():
     N_.check(N_.lib().fsim_profile_enable(0))
     pm = np.median(np.array(pass_ms), axis=0)
     algo = pass_bytes()
-    names = ["k_pass_a<512>", "k_pass_g+k_pass_b1<512>", "k_pass_b2<512>", "k_pass_c<512>"]
+    names = PASS_NAMES
     dom = int(np.argmax(pm))
     peak, peak_kind = peaks()
     achieved = algo[dom] * B / (pm[dom] / 1000.0) / 1e9

@@ -390,6 +390,9 @@ void Plan::fill_job_live(JobDesc& j, const void* raw, float* out, float* wf, cha
   j.G = nullptr;
   j.Tw = nullptr;
   j.Dy = nullptr;
+  j.On = nullptr;
+  j.clip_max = nullptr;
+  j.clip = 0;
   j.fwf = nullptr;
   j.wff = nullptr;
   j.Wf = nullptr;

@@ -83,6 +83,7 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
                  FSIM_EINVAL, "job %d: the filtered widefield needs an offline-path plan", i);
     FSIM_REQUIRE(((uintptr_t)jobs[i].widefield & 7) == 0 && ((uintptr_t)jobs[i].filtered_widefield & 7) == 0,
                  FSIM_EINVAL, "job %d: widefield outputs must be 8-byte aligned", i);
+    FSIM_REQUIRE(((uintptr_t)jobs[i].out & 7) == 0, FSIM_EINVAL, "job %d: the output must be 8-byte aligned", i);
     order[i] = i;
   }
   auto key = [&](int i) {
@@ -143,8 +144,11 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
     }
     // largest classes sort last; the first class stays on st, the rest spread over aux
     cudaStream_t s = (nfork > 0 && g > 0) ? aux[(g - 1) % nfork] : st;
-    rc = (p0->path == FSIM_PATH_LIVE) ? launch_live_size(p0->prm.w, d_table + k, e - k, maxA, s)
-                                      : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxPair, maxWin, s);
+    bool scale_clip = false;
+    for (int i = k; i < e; i++) scale_clip = scale_clip || static_cast<const Plan*>(jobs[order[i]].plan)->clip_scale == 2;
+    rc = (p0->path == FSIM_PATH_LIVE)
+             ? launch_live_size(p0->prm.w, d_table + k, e - k, maxA, s)
+             : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxPair, maxWin, scale_clip, s);
     if (rc == FSIM_OK && p0->path == FSIM_PATH_OFFLINE) {
       bool wf = false;
       for (int i = k; i < e; i++) wf = wf || jobs[order[i]].widefield || jobs[order[i]].filtered_widefield;
@@ -264,6 +268,16 @@ int fsim_plan_destroy(fsim_plan* plan) {
 size_t fsim_plan_workspace_bytes(const fsim_plan* plan) { return plan ? align256(plan_ws(plan)) : 0; }
 
 size_t fsim_plan_filter_bytes(const fsim_plan* plan) { return plan ? plan->filter_bytes : 0; }
+
+int fsim_plan_set_clip_scale(fsim_plan* plan, int clip_scale) {
+  FSIM_REQUIRE(plan, FSIM_EINVAL, "null plan");
+  FSIM_REQUIRE(clip_scale >= 0 && clip_scale <= 2, FSIM_EINVAL, "clip_scale %d: 0 (NONE), 1 (CLIP) or 2 (BOTH)",
+               clip_scale);
+  FSIM_REQUIRE(plan->path == FSIM_PATH_OFFLINE || clip_scale == 0, FSIM_EINVAL,
+               "clip_scale: live plans return the reference's unclipped live image");
+  plan->clip_scale = clip_scale;
+  return FSIM_OK;
+}
 
 int fsim_plan_info(const fsim_plan* plan, int* w, int* path, int* input_type) {
   FSIM_REQUIRE(plan, FSIM_EINVAL, "null plan");

@@ -251,26 +251,31 @@ int Plan::build(cudaStream_t st) {
   return FSIM_OK;
 }
 
-// workspace of one dataset: I | D | G | Tw | Dy | O (each 256-byte aligned)
-static void ws_parts(const fsim_sim_param& p, int nwin, size_t part[6]) {
+// workspace of one dataset: I | D | G | Tw | Dy | O | On | clip max (each 256-byte aligned).
+// I holds the band-0 slot (all angles summed) and one slot per angle and band pair.
+static void ws_parts(const fsim_sim_param& p, int nwin, size_t part[8]) {
   const int N = p.w, W = 2 * N, nPair = p.nr_bands - 1;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  part[0] = al((size_t)p.nr_dirs * (1 + nPair) * nwin * N * sizeof(float2));
+  part[0] = al((size_t)(1 + p.nr_dirs * nPair) * nwin * N * sizeof(float2));
   part[1] = al((size_t)p.nr_dirs * nPair * N * sizeof(float2));
   part[2] = al((size_t)p.nr_dirs * nPair * nwin * sizeof(float2));
   part[3] = al((size_t)(1 + p.nr_dirs * nPair) * nwin * nwin * sizeof(float2));
   part[4] = al((size_t)p.nr_dirs * nPair * nwin * sizeof(float2));
-  part[5] = al((size_t)W * W * sizeof(float2));
+  part[5] = al((size_t)W * N * sizeof(float2));
+  part[6] = al((size_t)W * sizeof(float2));
+  part[7] = 256;
 }
 
 size_t Plan::workspace_bytes() const {
-  size_t part[6];
+  size_t part[8];
   ws_parts(prm, nwin, part);
-  return std::max(part[0] + part[1] + part[2] + part[3] + part[4] + part[5], widefield_ws_bytes(prm.w));
+  size_t sum = 0;
+  for (size_t v : part) sum += v;
+  return std::max(sum, widefield_ws_bytes(prm.w));
 }
 
 void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, float* fwf, char* ws) const {
-  const int N = prm.w, nC = 2 * prm.nr_bands - 1;
+  const int nC = 2 * prm.nr_bands - 1;
   j.raw = raw;
   j.out = out;
   j.widefield = wf;
@@ -282,6 +287,7 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, float* f
   j.nP = prm.nr_phases;
   j.nC = nC;
   j.nWin = nwin;
+  j.clip = clip_scale;
   j.bgr = (float)bgr;
   j.damp = d_damp;
   j.coef = d_coef;
@@ -290,7 +296,7 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, float* f
   j.masks = d_masks;
   j.wa = d_wa;
   j.nyq = d_nyq;
-  size_t part[6];
+  size_t part[8];
   ws_parts(prm, nwin, part);
   char* w = ws;
   j.I = (float2*)w;
@@ -299,6 +305,8 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, float* f
   j.Tw = (float2*)(w += part[2]);
   j.Dy = (float2*)(w += part[3]);
   j.O = (float2*)(w += part[4]);
+  j.On = (float2*)(w += part[5]);
+  j.clip_max = (float*)(w += part[6]);
 }
 
 // ---- autotuned variants ------------------------------------------------------------------------
@@ -319,15 +327,15 @@ int offline_tune_get(int n, int pass) {
   return (k < 0 || pass < 0 || pass > 2) ? -1 : var_table(pass)[k];
 }
 
-extern template int launch_offline<64>(const JobDesc*, int, int, int, int, cudaStream_t);
-extern template int launch_offline<128>(const JobDesc*, int, int, int, int, cudaStream_t);
-extern template int launch_offline<192>(const JobDesc*, int, int, int, int, cudaStream_t);
-extern template int launch_offline<256>(const JobDesc*, int, int, int, int, cudaStream_t);
-extern template int launch_offline<384>(const JobDesc*, int, int, int, int, cudaStream_t);
-extern template int launch_offline<512>(const JobDesc*, int, int, int, int, cudaStream_t);
-extern template int launch_offline<768>(const JobDesc*, int, int, int, int, cudaStream_t);
-extern template int launch_offline<1024>(const JobDesc*, int, int, int, int, cudaStream_t);
-extern template int launch_offline<2048>(const JobDesc*, int, int, int, int, cudaStream_t);
+extern template int launch_offline<64>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+extern template int launch_offline<128>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+extern template int launch_offline<192>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+extern template int launch_offline<256>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+extern template int launch_offline<384>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+extern template int launch_offline<512>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+extern template int launch_offline<768>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+extern template int launch_offline<1024>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+extern template int launch_offline<2048>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
 
 #define FSIM_RECON_SIZES(X) X(64) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(2048)
 
@@ -342,11 +350,12 @@ bool offline_size_supported(int n) {
   }
 }
 
-int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st) {
+int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, bool scale_clip,
+                        cudaStream_t st) {
   switch (n) {
 #define CASE(v) \
   case v:       \
-    return launch_offline<v>(d_jobs, njobs, maxA, maxPair, maxWin, st);
+    return launch_offline<v>(d_jobs, njobs, maxA, maxPair, maxWin, scale_clip, st);
     FSIM_RECON_SIZES(CASE)
 #undef CASE
   }

@@ -12,6 +12,7 @@ struct JobDesc {
   float* out;         // W*W reconstruction
   float* widefield;   // N*N (live path), nullable
   int input_u16, nA, nP, nC, nWin;
+  int clip;  // offline output: 0 CLIPSCALE.NONE, 1 CLIP, 2 BOTH
   float bgr;
   const float* damp;    // N*N border fade, nullable
   const float2* coef;   // [a][c][p] separation coefficients
@@ -21,12 +22,16 @@ struct JobDesc {
   const float* wa;      // Wiener x apodization, quad layout [X/4][Y][X%4]
   const float2* nyq;    // offline: [a][b-1][x, y][N] FFT_N((-1)^n ro_pos[n]) of the pos component's x and y
                         // odd-sample ramps (the Nyquist response, see pass A)
-  float2* I;            // workspace: row-transformed windows [a][band 0, neg of each pair][nWin/4][N][4]
+  float2* I;            // workspace: row-transformed windows [band 0, neg of (a, b)][nWin/4][N][4] (offline);
+                        // live: [a][c] N*N row transforms
   float2* D;            // workspace: [a][b-1][N] Nyquist term d of every row's neg component (pass A)
   float2* G;            // workspace: [a][b-1][nWin] column transform of D with the pos y shift (pass G)
   float2* Tw;           // workspace: column-transformed windows [band 0, neg of (a, b)][nWin/4][nWin][4] (pass B1)
   float2* Dy;           // workspace: [a][b-1][nWin] Nyquist term d' of every neg window column (pass B1)
-  float2* O;            // workspace: W*W after the column pass
+  float2* O;            // workspace: offline: W x N, columns 0..N-1 of the Hermitian half after pass B2
+                        // (row-major, stride N); live: W*W after the column pass
+  float2* On;           // workspace (offline): column N of the Hermitian half, W entries
+  float* clip_max;      // workspace (offline): the image maximum for CLIPSCALE.BOTH
   // widefield side outputs of the offline path (widefield.cu), run after the passes above
   float* fwf;              // W*W filtered widefield, nullable (widefield: W*W offline, N*N live)
   const float* wff;        // N*N filter of the filtered widefield (resident, k_build_wff)
@@ -39,6 +44,7 @@ struct Plan {
   int input_type = FSIM_INPUT_F32;
   int fade_px = 0;
   double bgr = 0;
+  int clip_scale = 0;  // offline output: SimParam.CLIPSCALE ordinal (0 NONE, 1 CLIP, 2 BOTH)
   int nwin = 0;
   void* dev = nullptr;
   size_t dev_bytes = 0;
@@ -80,7 +86,9 @@ int offline_tune_get(int n, int pass);
 bool live_size_supported(int n);
 // maxA, maxPair, maxWin: the largest angle count, band-pair count and OTF-support window
 // of the batch's datasets of size n (they bound the grids; extra blocks exit at once)
-int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st);
+// scale_clip: some job of the class asks for CLIPSCALE.BOTH (one more pass scales its image)
+int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, bool scale_clip,
+                        cudaStream_t st);
 int launch_live_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);
 // widefield and filtered widefield of the offline jobs that ask for them (widefield.cu);
 // launched after launch_offline_size on the same stream (it reuses the job workspaces)

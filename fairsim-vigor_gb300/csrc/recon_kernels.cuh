@@ -27,7 +27,7 @@
 #define FSIM_B1_REGS 64
 #endif
 #ifndef FSIM_B2_REGS
-#define FSIM_B2_REGS 64
+#define FSIM_B2_REGS 80
 #endif
 
 namespace fsim {
@@ -40,10 +40,8 @@ struct Cfg {
   static constexpr int W = 2 * N;
   static constexpr int EN = ENV ? ENV : ((N % 3 == 0) ? 12 : 8);
   static constexpr int T = N / EN;  // threads per line
-  static constexpr int CB = CBV ? CBV : 4;
-  static constexpr int EW = (N % 3 == 0) ? 24 : 16;  // pass C: W-length lines
-  static constexpr int TC = W / EW;
-  static constexpr int GC = (TC >= 128) ? 1 : (128 / TC);  // rows per block in pass C
+  static constexpr int CB = CBV ? CBV : 4;  // passes B1, B2: interleaved columns per block
+  static constexpr int GC = (T >= 128) ? 1 : (128 / T);  // pass C: rows per block
 };
 
 // Copies a job descriptor into shared memory once per block (the passes read its fields
@@ -124,7 +122,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   load_job(&J, jobs + blockIdx.z, t, T);
   __syncthreads();
   if (a > J.nA) return;  // uniform per block
-  const int nA = J.nA, nP = J.nP, nC = J.nC, nPair = (nC - 1) / 2, nS = 1 + nPair;  // I slots per angle
+  const int nA = J.nA, nP = J.nP, nC = J.nC, nPair = (nC - 1) / 2;
   const size_t frame = (size_t)N * N, row = (size_t)y * N;
   if (a == nA) {
     // Band 0 is summed over the angles before the column pass, and its band separation
@@ -158,6 +156,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
       const int m = paste_src<N>(X);
       J.I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = m >= 0 ? bh[sidx(m)] : make_float2(0.f, 0.f);
     }
+    if (y == 0 && t == 0) *J.clip_max = 0.f;  // CLIPSCALE.BOTH: pass C takes the maximum from 0
     return;
   }
   if (nPair == 0) return;  // one band: the band-0 block above is the whole row pass
@@ -229,7 +228,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     __syncthreads();
     // neg window of the shifted spectrum: E[X mod N] + exp(-2 pi i X/W) O[X mod N]
     const int Xs = J.win[2 * (a * nC + cn)];
-    float2* I = J.I + (size_t)(a * nS + b) * J.nWin * N;
+    float2* I = J.I + (size_t)(1 + a * nPair + (b - 1)) * J.nWin * N;  // slot of (a, b)
     for (int xl = t; xl < J.nWin; xl += T) {
       int X = Xs + xl;
       if (X >= W) X -= W;
@@ -315,7 +314,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   const float2* twW = g_tw + tw_offset(W);
   load_job(&J, jobs + blockIdx.z, lt, CB * T);
   __syncthreads();
-  const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2, nS = 1 + nPair;
+  const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2;
   const int comp = blockIdx.y;  // 0: band 0; 1 + a*nPair + (b-1): neg of (a, b)
   if (comp > J.nA * nPair || (int)blockIdx.x * CB >= nWin) return;  // uniform per block
   const int xl = blockIdx.x * CB + lane;  // nWin is a multiple of 4: every lane is inside
@@ -339,7 +338,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
     return;
   }
   const int a = (comp - 1) / nPair, b = 1 + (comp - 1) % nPair, cn = 2 * b - 1;
-  const float2* I = J.I + (size_t)(a * nS + b) * nWin * N + quad;
+  const float2* I = J.I + (size_t)comp * nWin * N + quad;  // slot 1 + a*nPair + (b-1)
 #pragma unroll
   for (int i = 0; i < EN; i++) x[i] = I[(size_t)(t + i * T) * 4];
   line_fft_reg<N, T, CB, false, true>(x, bh, lane, t, twN);  // Z along y
@@ -374,13 +373,21 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   }
 }
 
-// ---- pass B2: masked sum over components, Wiener x apodization, inverse FFT_W along y ------------
+// ---- pass B2: masked Hermitian sum over components, Wiener x apodization, inverse along y ----
+// The image is real: out = Re iFFT2(F) = iFFT2(H) with the Hermitian part
+// H(X, Y) = (F(X, Y) + conj F(-X, -Y)) / 2, so only the columns X = 0..N of H are formed and
+// stored (pass C completes each row by symmetry): half the column-transformed windows,
+// masks and Wiener x apodization reads, inverse transforms and writes of a full-width pass.
 // CB output columns per block; each thread keeps the 2*EN rows Y = t + i*T of its column in
-// registers. The pos component of a pair at (X, Y) comes from the neg transform at (-X, -Y),
-// stored at the mirrored window position (the neg window is the pos window's mirror image):
-//   F_pos[X][Y] = conj(F_neg[-X][-Y]) + exp(-2 pi i Y/W) d'(-X) Qy[Y mod N]
-//                 + exp(-2 pi i X/W) Qx[X mod N] G[Y]
-// (the identity of pass A along y, plus pass G's column for the x term).
+// registers. With the pair identities of pass A (the pos component of a pair at (X, Y) is
+// the conjugate of the neg transform at (-X, -Y) plus two rank-one Nyquist terms n1, and
+// the neg/pos masks are mirror images: mask_neg(-X,-Y) = mask_pos(X,Y)), a pair adds
+//   H += mask_neg(X,Y) (A + conj(n2)/2) + mask_pos(X,Y) (conj(B) + n1/2),
+// A = the neg transform at (X, Y), B = the neg transform at (-X, -Y) (stored at the
+// mirrored position of the neg window, which is the pos window's mirror image), and
+// n1 / n2 the pos component's Nyquist terms at (X, Y) / (-X, -Y):
+//   n1(X,Y) = exp(-2 pi i Y/W) d'(-X) Qy[Y mod N] + exp(-2 pi i X/W) Qx[X mod N] G[Y];
+// band 0 adds mask_0(X,Y) (T0(X,Y) + conj T0(-X,-Y)) / 2.
 template <int N, int ENV, int CBV>
 __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
                                   col_min_blocks<Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T, Cfg<N, ENV, CBV>::EN,
@@ -389,7 +396,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   using P = Cfg<N, ENV, CBV>;
   constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN;
   const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
-  const int X = blockIdx.x * CB + lane;
+  const int X = blockIdx.x * CB + lane;  // X <= N + CB - 1 < W; only X <= N is stored
   __shared__ JobDesc J;
   extern __shared__ float2 sm[];
   float2* bz = sm;                           // N x CB
@@ -400,24 +407,29 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   __syncthreads();
   const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2;
   auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
+  const int Xm = wrap(-X);
   float2 acc[2 * EN];
 #pragma unroll
   for (int i = 0; i < 2 * EN; i++) acc[i] = make_float2(0.f, 0.f);
   // window position (xl, yl) -> offset in a quad-layout nWin x nWin window
   auto qoff = [&](int xl) { return ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3); };
-  {  // band 0
-    const int xl = wrap(X - J.win[0]), Ys = J.win[1];
+  {  // band 0: (T0(X,Y) + conj T0(-X,-Y)) / 2, one symmetric mask
+    const int xl = wrap(X - J.win[0]), xlm = wrap(Xm - J.win[0]), Ys = J.win[1];
     if (xl < nWin) {
       const float* mk = J.masks + qoff(xl);
       const float2* tv = J.Tw + qoff(xl);
+      const float2* tm = J.Tw + qoff(xlm);
+      const bool mirror_in = xlm < nWin;  // (X,Y) in the support puts -X in the window
 #pragma unroll
       for (int i = 0; i < 2 * EN; i++) {
-        const int yl = wrap(t + i * T - Ys);
+        const int Y = t + i * T;
+        const int yl = wrap(Y - Ys), ylm = wrap(wrap(-Y) - Ys);
         if (yl < nWin) {
-          const float f = __ldg(mk + (size_t)yl * 4);
+          const float f = 0.5f * __ldg(mk + (size_t)yl * 4);
           const float2 u = tv[(size_t)yl * 4];
-          acc[i].x += f * u.x;
-          acc[i].y += f * u.y;
+          const float2 um = (mirror_in && ylm < nWin) ? tm[(size_t)ylm * 4] : make_float2(0.f, 0.f);
+          acc[i].x += f * (u.x + um.x);
+          acc[i].y += f * (u.y - um.y);
         }
       }
     }
@@ -426,44 +438,50 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
     for (int b = 1; b <= nPair; b++) {
       const int cn = 2 * b - 1, cp = 2 * b, ab = a * nPair + (b - 1);
       const float2* Tc = J.Tw + (size_t)(1 + ab) * nWin * nWin;
+      const float2* Qx = J.nyq + (size_t)(ab * 2) * N;
+      const float2* Qy = Qx + N;
+      const float2* G = J.G + (size_t)ab * nWin;
       const int xn = wrap(X - J.win[2 * (a * nC + cn)]);
-      if (xn < nWin) {
+      if (xn < nWin) {  // neg at (X, Y), and the pos component's n2 at (-X, -Y)
         const int Yn = J.win[2 * (a * nC + cn) + 1];
         const float* mk = J.masks + (size_t)(a * nC + cn) * nWin * nWin + qoff(xn);
         const float2* tv = Tc + qoff(xn);
+        const float2 dX = J.Dy[(size_t)ab * nWin + xn];
+        const float2 cxm = cmul(twW[Xm], __ldg(Qx + (Xm < N ? Xm : Xm - N)));
 #pragma unroll
         for (int i = 0; i < 2 * EN; i++) {
-          const int yl = wrap(t + i * T - Yn);
+          const int Y = t + i * T;
+          const int yl = wrap(Y - Yn);
           if (yl < nWin) {
+            const int Ym = wrap(-Y);
             const float f = __ldg(mk + (size_t)yl * 4);
-            const float2 u = tv[(size_t)yl * 4];
-            acc[i].x += f * u.x;
-            acc[i].y += f * u.y;
+            const float2 A = tv[(size_t)yl * 4];
+            // n2: its pos-window row is nWin-1-yl (the windows are mirror images)
+            const float2 n2 = cadd(cmul(twW[Ym], cmul(dX, __ldg(Qy + (Ym < N ? Ym : Ym - N)))),
+                                   cmul(cxm, G[nWin - 1 - yl]));
+            acc[i].x += f * (A.x + 0.5f * n2.x);
+            acc[i].y += f * (A.y - 0.5f * n2.y);
           }
         }
       }
       const int xp = wrap(X - J.win[2 * (a * nC + cp)]);
-      if (xp < nWin) {
+      if (xp < nWin) {  // pos at (X, Y) from the neg transform at (-X, -Y)
         const int Yp = J.win[2 * (a * nC + cp) + 1];
         const int xm = nWin - 1 - xp;  // window column of -X in the neg window
         const float* mk = J.masks + (size_t)(a * nC + cp) * nWin * nWin + qoff(xp);
         const float2* tv = Tc + qoff(xm);
-        const float2* Qx = J.nyq + (size_t)(ab * 2) * N;
-        const float2* Qy = Qx + N;
-        const float2 dp = J.Dy[(size_t)ab * nWin + xm];
+        const float2 dM = J.Dy[(size_t)ab * nWin + xm];
         const float2 cx = cmul(twW[X], __ldg(Qx + (X < N ? X : X - N)));
-        const float2* G = J.G + (size_t)ab * nWin;
 #pragma unroll
         for (int i = 0; i < 2 * EN; i++) {
           const int Y = t + i * T;
           const int yl = wrap(Y - Yp);
           if (yl < nWin) {
-            const int m = Y < N ? Y : Y - N;
             const float f = __ldg(mk + (size_t)yl * 4);
-            const float2 e = cconjf(tv[(size_t)(nWin - 1 - yl) * 4]);
-            const float2 u = cadd(cadd(e, cmul(twW[Y], cmul(dp, __ldg(Qy + m)))), cmul(cx, G[yl]));
-            acc[i].x += f * u.x;
-            acc[i].y += f * u.y;
+            const float2 B = tv[(size_t)(nWin - 1 - yl) * 4];
+            const float2 n1 = cadd(cmul(twW[Y], cmul(dM, __ldg(Qy + (Y < N ? Y : Y - N)))), cmul(cx, G[yl]));
+            acc[i].x += f * (B.x + 0.5f * n1.x);
+            acc[i].y += f * (-B.y + 0.5f * n1.y);
           }
         }
       }
@@ -484,36 +502,88 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   }
   line_fft_reg<N, T, CB, true, true>(xe, bz, lane, t, twN);
   line_fft_reg<N, T, CB, true, true>(xo, bh, lane, t, twN);
+  if (X < N) {
 #pragma unroll
-  for (int i = 0; i < EN; i++) {
-    const int k = t + i * T;
-    J.O[(size_t)(2 * k) * W + X] = xe[i];
-    J.O[(size_t)(2 * k + 1) * W + X] = xo[i];
+    for (int i = 0; i < EN; i++) {
+      const int k = t + i * T;
+      J.O[(size_t)(2 * k) * N + X] = xe[i];
+      J.O[(size_t)(2 * k + 1) * N + X] = xo[i];
+    }
+  } else if (X == N) {
+#pragma unroll
+    for (int i = 0; i < EN; i++) {
+      const int k = t + i * T;
+      J.On[2 * k] = xe[i];
+      J.On[2 * k + 1] = xo[i];
+    }
   }
 }
 
-// ---- pass C: rows of the output ---------------------------------------------------------------
+// ---- pass C: rows of the output (complex-to-real) ------------------------------------------------
+// Row y of the image is out[x] = sum_X H[X] exp(+2 pi i x X/W) / W^2 with H[W-X] = conj H[X],
+// H[0..N-1] = O[y][.] and H[N] = On[y]. Both halves of the output come from one N-point
+// inverse FFT: Z[k] = (H[k] + conj H[N-k]) + i exp(+2 pi i k/W) (H[k] - conj H[N-k]) gives
+// iFFT_N(Z)[n] = out[2n] + i out[2n+1] (the two sub-sequences' transforms are real).
+// clip != 0 clips negative values (CLIPSCALE.CLIP); clip == 2 also records the image's
+// maximum (CLIPSCALE.BOTH: k_scale_clip scales afterwards, before clipping).
 template <int N>
-__global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::TC) k_pass_c(const JobDesc* __restrict__ jobs) {
+__global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::T) k_pass_c(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N>;
-  constexpr int W = P::W, T = P::TC, G = P::GC, EW = P::EW;
+  constexpr int W = P::W, T = P::T, G = P::GC, EN = P::EN;
   const JobDesc& J = jobs[blockIdx.y];
   const int g = threadIdx.x / T, t = threadIdx.x % T;
-  const int Y = blockIdx.x * G + g;
-  __shared__ float2 sm[G * smem_line_elems(W, 1)];
-  __shared__ float2 tw[stw_len(W, EW)];
-  stage_stage_twiddles<W, EW>(tw, threadIdx.x, G * T);
-  float2* s = sm + g * smem_line_elems(W, 1);
-  const float2* row = J.O + (size_t)Y * W;
-  float2 x[EW];  // element t + i*T of the row, in registers through the transform
+  const int y = blockIdx.x * G + g;
+  __shared__ float2 sm[G * smem_line_elems(N, 1)];
+  __shared__ float2 tw[stw_len(N, EN)];
+  stage_stage_twiddles<N, EN>(tw, threadIdx.x, G * T);
+  float2* s = sm + g * smem_line_elems(N, 1);
+  const float2* twW = g_tw + tw_offset(W);
+  const float2* row = J.O + (size_t)y * N;
+  const float2 hn = J.On[y];
+  float2 x[EN];  // element t + i*T of Z, in registers through the transform
 #pragma unroll
-  for (int i = 0; i < EW; i++) x[i] = row[t + i * T];
+  for (int i = 0; i < EN; i++) {
+    const int k = t + i * T;
+    const float2 h = row[k];
+    const float2 hm = cconjf(k == 0 ? hn : row[N - k]);
+    const float2 e = cadd(h, hm), d = cmul(csub(h, hm), cconjf(twW[k]));
+    x[i] = make_float2(e.x - d.y, e.y + d.x);  // e + i d
+  }
   __syncthreads();  // the twiddle table is staged
-  line_fft_reg<W, T, 1, true>(x, s, 0, t, tw);
+  line_fft_reg<N, T, 1, true>(x, s, 0, t, tw);
   const float scale = 1.f / ((float)W * (float)W);
-  float* out = J.out + (size_t)Y * W;
+  const int clip = J.clip;
+  float2* out = reinterpret_cast<float2*>(J.out + (size_t)y * W);
+  float mx = 0.f;
 #pragma unroll
-  for (int i = 0; i < EW; i++) out[t + i * T] = x[i].x * scale;
+  for (int i = 0; i < EN; i++) {
+    float2 v = make_float2(x[i].x * scale, x[i].y * scale);
+    if (clip == 2) mx = fmaxf(mx, fmaxf(v.x, v.y));
+    if (clip == 1) {
+      if (v.x < 0) v.x = 0.f;
+      if (v.y < 0) v.y = 0.f;
+    }
+    out[t + i * T] = v;
+  }
+  if (clip == 2) {  // non-negative floats order as their bit patterns
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(reinterpret_cast<unsigned int*>(J.clip_max), __float_as_uint(mx));
+  }
+}
+
+// CLIPSCALE.BOTH (SimUtils.clipAndScale(vec, true, true), S/SimUtils.java:244-264): every pixel
+// times 255/max (max over the image, starting at 0), then negative values set to 0.
+static __global__ void k_scale_clip(const JobDesc* __restrict__ jobs, int W) {
+  const JobDesc& J = jobs[blockIdx.y];
+  if (J.clip != 2) return;
+  const float f = __fdiv_rn(255.f, *J.clip_max);
+  float* out = J.out;
+  const size_t n = (size_t)W * W;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float v = __fmul_rn(out[i], f);
+    if (v < 0) v = 0.f;
+    out[i] = v;
+  }
 }
 
 // ---- launch ----------------------------------------------------------------------------------------
@@ -553,7 +623,8 @@ static int launch_b2(const JobDesc* d_jobs, int njobs, cudaStream_t st) {
     FSIM_CUDA(cudaFuncSetAttribute(k_pass_b2<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  k_pass_b2<N, ENB, CBB><<<dim3(PB::W / PB::CB, njobs), PB::CB * PB::T, smem, st>>>(d_jobs);
+  // the Hermitian half: columns 0..N
+  k_pass_b2<N, ENB, CBB><<<dim3(N / PB::CB + 1, njobs), PB::CB * PB::T, smem, st>>>(d_jobs);
   return FSIM_OK;
 }
 
@@ -578,7 +649,8 @@ __host__ inline int size_slot(int n) {
 // (elements, columns per block) {(E0,4), (E0,2), (E1,4), (E1,2)} with E0 = 8, E1 = 16
 // (3*2^k sizes: 12, 24). The extremes (N <= 128, N >= 2048) have one variant.
 template <int N>
-int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, cudaStream_t st) {
+int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, bool scale_clip,
+                   cudaStream_t st) {
   constexpr bool p3 = (N % 3 == 0);
   constexpr int E0 = p3 ? 12 : 8, E1 = p3 ? 24 : 16;
   constexpr bool single = (N <= 128 || N >= 2048);
@@ -590,8 +662,10 @@ int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int 
   if (va == 0) launch_a<N, E0>(d_jobs, njobs, maxA, maxPair, st);
   else if constexpr (!single) launch_a<N, E1>(d_jobs, njobs, maxA, maxPair, st);
   if (ev) cudaEventRecord(ev[1], st);
-  if (va == 0) launch_g<N, E0>(d_jobs, njobs, maxA, maxPair, st);
-  else if constexpr (!single) launch_g<N, E1>(d_jobs, njobs, maxA, maxPair, st);
+  if (maxPair > 0) {
+    if (va == 0) launch_g<N, E0>(d_jobs, njobs, maxA, maxPair, st);
+    else if constexpr (!single) launch_g<N, E1>(d_jobs, njobs, maxA, maxPair, st);
+  }
   int rc = FSIM_OK;
   if constexpr (single) {
     rc = launch_b1<N, E0, CBX>(d_jobs, njobs, maxA, maxPair, maxWin, st);
@@ -618,7 +692,8 @@ int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int 
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[3], st);
   using PC = Cfg<N>;
-  k_pass_c<N><<<dim3(PC::W / PC::GC, njobs), PC::GC * PC::TC, 0, st>>>(d_jobs);
+  k_pass_c<N><<<dim3(PC::W / PC::GC, njobs), PC::GC * PC::T, 0, st>>>(d_jobs);
+  if (scale_clip) k_scale_clip<<<dim3(2 * N, njobs), 256, 0, st>>>(d_jobs, 2 * N);
   if (ev) {
     cudaEventRecord(ev[4], st);
     profile_mark(4);

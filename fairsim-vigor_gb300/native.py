@@ -244,6 +244,7 @@ _SIGS = {
     "fsim_plan_workspace_bytes": (C.c_size_t, [VP]),
     "fsim_plan_filter_bytes": (C.c_size_t, [VP]),
     "fsim_plan_info": (I32, [VP, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
+    "fsim_plan_set_clip_scale": (I32, [VP, I32]),
     "fsim_recon_batch": (I32, [VP, I32, VP, C.c_size_t, VP]),
     "fsim_recon_batch_host": (I32, [VP, I32, I32]),
     "fsim_batch_graph_create": (I32, [VP, VP, I32, VP, C.c_size_t, VP]),

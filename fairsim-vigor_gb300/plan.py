@@ -48,6 +48,12 @@ class ReconPlan:
         self._c = N.to_c_param(sp)
         N.check(N.lib().fsim_plan_update(self._h, C.byref(self._c)))
 
+    def setClipScale(self, clip_scale: int):
+        """Output scaling of the reconstruction, SimParam.CLIPSCALE ordinal: 0 NONE (default),
+        1 CLIP, 2 BOTH (scaled to 255 at the maximum, then clipped; SimUtils.clipAndScale)."""
+        N.check(N.lib().fsim_plan_set_clip_scale(self._h, int(clip_scale)))
+        return self
+
     def workspace_bytes(self) -> int:
         return int(N.lib().fsim_plan_workspace_bytes(self._h))
 

@@ -200,11 +200,17 @@ int fsim_plan_destroy(fsim_plan* plan);
 size_t fsim_plan_workspace_bytes(const fsim_plan* plan);      /* per dataset */
 size_t fsim_plan_filter_bytes(const fsim_plan* plan);         /* resident filters */
 int fsim_plan_info(const fsim_plan* plan, int* w, int* path, int* input_type);
+/* Output scaling of an offline plan's reconstruction, SimParam.CLIPSCALE
+ * (SimParam.java:61-62, applied by SimUtils.spatial / clipAndScale, SimUtils.java:146-153,
+ * 244-264): 0 NONE (the default here), 1 CLIP (negative values set to 0), 2 BOTH (scaled to
+ * 255 at the image maximum, then clipped; the reference's default). Live plans: NONE only. */
+int fsim_plan_set_clip_scale(fsim_plan* plan, int clip_scale);
 
 typedef struct fsim_job {
   const fsim_plan* plan;
   const void* raw;  /* device: nr_dirs*nr_phases frames, w*w each, f32 or u16 (plan input type) */
-  float* out;       /* device: 2w x 2w float32 reconstruction (real part, CLIPSCALE.NONE) */
+  float* out;       /* device, 8-byte aligned: 2w x 2w float32 reconstruction (real part, scaled
+                       as fsim_plan_set_clip_scale chose; CLIPSCALE.NONE by default) */
   float* widefield; /* device, nullable. Live plans: w x w mean of the damped raw frames
                        (ReconstructionRunner.java:449-496). Offline plans: the 2w x 2w
                        "Widefield" image of runReconstruction (SimAlgorithm.java:533-560) */
@@ -272,15 +278,17 @@ int fsim_estimate_raw(fsim_sim_param* p, const void* raw_device, int input_type,
 int fsim_live_refit(fsim_sim_param* p, const uint16_t* raw_device, double* peaks_out);
 
 /* ---- allocation-free correlation sweep (no counterpart in the reference) ---------------
- * For callers that cannot allocate device memory at this point (a real-time acquisition
- * thread, work being captured into a CUDA graph, or a process whose device memory was
- * partitioned up front): the fit's 10 x 10 correlation grid of Correlation.fitPeak's
- * inner loop, evaluated on caller-provided real-space bands b0, b1 (n x n complex float,
- * device) for shifts kx[nx], ky[ny] (host arrays), scaled by scal; out (host, nx*ny*2
- * doubles, [yi][xi] re/im). Scratch is one static device array per GPU (n <= 2048,
- * nx, ny <= 10; ~0.66 MB kept until exit); the call allocates nothing. Overlapping calls
- * race on that scratch. The first call on a device resolves the array's address; make it
- * before any stream capture. stream: cudaStream_t (NULL = legacy default stream). */
+ * For callers that cannot allocate device memory at this point: a real-time acquisition
+ * thread (no room in its latency budget for the allocator) or a process whose device
+ * memory was partitioned up front (an allocation mid-run could fail or take memory another
+ * component counts on). The fit's 10 x 10 correlation grid of Correlation.fitPeak's inner
+ * loop, evaluated on caller-provided real-space bands b0, b1 (n x n complex float, device)
+ * for shifts kx[nx], ky[ny] (host arrays), scaled by scal; out (host, nx*ny*2 doubles,
+ * [yi][xi] re/im), equal bit for bit to the allocating fit's grid. Scratch is one static
+ * device array per GPU (n <= 2048, nx, ny <= 10; ~0.66 MB kept until exit); the call
+ * allocates nothing and returns once out is written. Overlapping calls race on that
+ * scratch. The first call on a device resolves the array's address; make it before any
+ * stream capture. stream: cudaStream_t (NULL = legacy default stream). */
 int fsim_corr_grid_noalloc(const void* b0, const void* b1, int n, const double* kx, int nx, const double* ky,
                            int ny, double scal, double* out, void* stream);
 

@@ -4,7 +4,8 @@ the 2N grid and multiplying the real-space image by a phase ramp there
 (sim_algorithm/SimUtils.java:43-50 with linalg/BasicVectors.java:259-339):
     F = FFT_W(r * iFFT_W(paste(FFT_N(z)))),  W = 2N.
 The passes evaluate it with N-point transforms only, and transform only the neg component of
-each conjugate band pair (csrc/recon_kernels.cuh, passes A, G, B1, B2)."""
+each conjugate band pair (csrc/recon_kernels.cuh, passes A, G, B); the image is real, so the
+column pass forms only the Hermitian half of the spectrum and the row pass C completes it."""
 import numpy as np
 import pytest
 
@@ -88,7 +89,7 @@ def test_conjugate_pair_in_two_dimensions(N, kx, ky):
                      + exp(-2 pi i X/W) Qx[X mod N] G[Y]
     with d(y) the row Nyquist terms of the neg component (pass A), G their y transform with
     the pos shift (pass G) and d'(X) the Nyquist term of the neg x-transformed column X
-    (pass B1); pass B2 forms the pos component from these and the mirrored neg window."""
+    (pass B); pass B forms the pos component from these and the mirrored neg window."""
     rng = np.random.default_rng(3)
     z = rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))
     W = 2 * N
@@ -139,3 +140,50 @@ def test_real_output_row_from_hermitian_halves(N):
     y = np.fft.ifft(herm(a) + 1j * herm(b)) / 2
     assert np.allclose(full[0::2], y.real, atol=1e-13)
     assert np.allclose(full[1::2], y.imag, atol=1e-13)
+
+
+@pytest.mark.parametrize("N,kx,ky", [(16, 3.25, -2.5), (32, -7.6, 5.1)])
+def test_hermitian_half_of_a_band_pair(N, kx, ky):
+    """Pass B stores H = (F(k) + conj F(-k))/2 (the image Re iFFT2(F) = iFFT2(H)) for the
+    columns 0..N only. For a pair with mirror-image masks (mask_neg(-k) = mask_pos(k)) and
+    F = mask_neg F_neg + mask_pos F_pos, with F_pos(k) = conj(F_neg(-k)) + n1(k):
+        H(k) = mask_neg(k) (A + conj(n2)/2) + mask_pos(k) (conj(B) + n1/2),
+    A = F_neg(k), B = F_neg(-k), n2(k) = n1(-k). Band 0 (a symmetric mask) adds
+    mask_0(k) (T0(k) + conj T0(-k)) / 2."""
+    rng = np.random.default_rng(6)
+    W = 2 * N
+    z = rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))
+    F_neg = shifted_spectrum_2d(z, kx, ky)
+    F_pos = shifted_spectrum_2d(np.conj(z), -kx, -ky)
+    Yi, Xi = np.meshgrid(np.arange(W), np.arange(W), indexing="ij")
+    mir = lambda a: a[(-Yi) % W, (-Xi) % W]  # noqa: E731  a(-k)
+    n1 = F_pos - np.conj(mir(F_neg))
+    m_pos = rng.uniform(size=(W, W))  # any real mask; the neg mask is its mirror image
+    m_neg = mir(m_pos)
+    m0 = rng.uniform(size=(W, W))
+    m0 = (m0 + mir(m0)) / 2  # band 0: symmetric
+    T0 = np.fft.fft2(rng.normal(size=(W, W)) + 1j * rng.normal(size=(W, W)))
+    F = m_neg * F_neg + m_pos * F_pos + m0 * T0
+    H_direct = (F + np.conj(mir(F))) / 2
+    A, B, n2 = F_neg, mir(F_neg), mir(n1)
+    H_pass_b = m_neg * (A + np.conj(n2) / 2) + m_pos * (np.conj(B) + n1 / 2) + m0 * (T0 + np.conj(mir(T0))) / 2
+    assert np.allclose(H_pass_b, H_direct, atol=1e-10)
+    assert np.allclose(np.real(np.fft.ifft2(F)), np.fft.ifft2(H_direct), atol=1e-12)
+
+
+@pytest.mark.parametrize("N", [8, 24, 64])
+def test_complex_to_real_row_from_half_spectrum(N):
+    """Pass C: a real row out[x] = sum_X H[X] exp(+2 pi i x X/W) of a Hermitian H
+    (H[W-X] = conj H[X]) from its half H[0..N] by one N-point inverse transform of
+    Z[k] = (H[k] + conj H[N-k]) + i exp(+2 pi i k/W) (H[k] - conj H[N-k]):
+    iFFT_N(Z)[n] N = out[2n] + i out[2n+1]."""
+    rng = np.random.default_rng(7)
+    W = 2 * N
+    h = np.fft.fft(rng.normal(size=W))  # Hermitian
+    out = np.fft.ifft(h).real * W        # unnormalised inverse
+    k = np.arange(N)
+    hk, hm = h[k], np.conj(h[N - k])
+    Z = (hk + hm) + 1j * np.exp(2j * np.pi * k / W) * (hk - hm)
+    z = np.fft.ifft(Z) * N
+    assert np.allclose(z.real, out[0::2], atol=1e-10)
+    assert np.allclose(z.imag, out[1::2], atol=1e-10)

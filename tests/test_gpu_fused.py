@@ -35,16 +35,46 @@ def make(fs, n, seed, **kw):
     return raw, truth, sp
 
 
-@pytest.mark.parametrize("n", [64, 128, 256, 384, 512, 1024])
+@pytest.mark.parametrize("n", [64, 128, 192, 256, 384, 512, 768, 1024])
 def test_offline_fused_vs_oracle(fs, oracle, n):
+    """Every offline size up to 1024^2 (the 3*2^k sizes run radix-3 line plans) within 1e-4
+    of the float oracle and 1e-5 of the FP64 oracle (the float oracle itself is 4e-6 from
+    it at 768^2 and 8e-6 at 1024^2: the reference rounds the shift phase to float)."""
     raw, truth, sp = make(fs, n, seed=20 + n)
     plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
     got = plan.reconstruct_host(raw)
     exp32 = oracle.recon_raw(sp, raw, fade=10)
     assert rel_l2(got, exp32) < 1e-4
-    if n <= 512:
-        exp64 = oracle.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
-        assert rel_l2(got, exp64) < 1e-5
+    exp64 = oracle.recon_raw(sp, raw.astype(np.float64), fade=10, dtype=np.float64)
+    assert rel_l2(got, exp64) < 1e-5
+
+
+@pytest.mark.parametrize("clip", [1, 2])
+def test_offline_fused_clip_scale_vs_oracle(fs, oracle, torch_cuda, clip):
+    """CLIPSCALE.CLIP and .BOTH (the reference's default; SimUtils.clipAndScale,
+    S/SimUtils.java:244-264) on the fused plans, alone and in a batch with NONE jobs."""
+    torch = torch_cuda
+    n = 256
+    raw, truth, sp = make(fs, n, seed=27)
+    plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    plan.setClipScale(clip)
+    got = plan.reconstruct_host(raw)
+    exp = oracle.recon_raw(sp, raw, fade=10, clip_scale=clip)
+    assert got.min() >= 0
+    assert rel_l2(got, exp) < 1e-4
+    if clip == 2:
+        assert abs(got.max() - 255.0) < 1e-3
+    # in one batch with an unscaled job of the same size: each keeps its own scaling
+    plain = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    d_raw = torch.from_numpy(raw).cuda()
+    d_out = [torch.empty((2 * n, 2 * n), dtype=torch.float32, device="cuda") for _ in range(2)]
+    ws = torch.empty(fs.plan.batch_workspace_bytes([plan, plain]), dtype=torch.uint8, device="cuda")
+    fs.plan.recon_batch([(plan, d_raw.data_ptr(), d_out[0].data_ptr()), (plain, d_raw.data_ptr(), d_out[1].data_ptr())],
+                        ws.data_ptr(), ws.numel())
+    torch.cuda.synchronize()
+    assert np.array_equal(d_out[0].cpu().numpy(), got)
+    assert np.array_equal(d_out[1].cpu().numpy(), plain.reconstruct_host(raw))
+    assert rel_l2(d_out[1].cpu().numpy(), oracle.recon_raw(sp, raw, fade=10)) < 1e-4
 
 
 @pytest.mark.parametrize("variant", ["bgr_att", "five_phases", "three_bands"])
@@ -74,6 +104,45 @@ def test_live_fused_vs_oracle(fs, oracle, n):
     got = plan.reconstruct_host(raw)
     exp, _ = oracle.live_recon(sp, raw)
     assert rel_l2(got, exp[0]) < 1e-4
+
+
+@pytest.mark.parametrize("n", [256, 512])
+def test_live_fused_fifteen_frames_vs_oracle(fs, oracle, n):
+    """Live path on 3 angles x 5 phases (15-frame stacks, pseudo-inverse separation)."""
+    raw, truth, sp = make(fs, n, seed=45 + n, as_u16=True, n_phases=5)
+    plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE, input_type=fs.native.INPUT_U16, fade_px=10)
+    got = plan.reconstruct_host(raw)
+    exp, _ = oracle.live_recon(sp, raw)
+    assert rel_l2(got, exp[0]) < 1e-4
+
+
+def test_mixed_batch_datasets_vs_oracle(fs, oracle, torch_cuda):
+    """The ragged batch of the mixed workload (sizes 256^2-1024^2, emission 488/525/600 nm,
+    per-dataset k0 and modulation 0.5-0.9, 1-3 channels) in one call: one dataset per (size,
+    wavelength) against the oracle, not only against its own single run."""
+    torch = torch_cuda
+    rng = np.random.default_rng(5)
+    plans, raws, sps = [], [], []
+    for i, n in enumerate((256, 384, 512, 768, 1024)):
+        for j, lam in enumerate((488.0, 525.0, 600.0)):
+            mod = float(rng.uniform(0.5, 0.9))
+            raw, truth = fs.synth.make_dataset(n=n, seed=300 + 3 * i + j, em_wavelength=lam, modulation=mod,
+                                               k0_frac=float(rng.uniform(0.75, 0.9)))
+            sp = fs.synth.sim_param_for(truth, n)
+            plans.append(fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32,
+                                           fade_px=10))
+            raws.append(raw)
+            sps.append(sp)
+    d_raw = [torch.from_numpy(r).cuda() for r in raws]
+    d_out = [torch.empty((2 * p.w, 2 * p.w), dtype=torch.float32, device="cuda") for p in plans]
+    ws = torch.empty(fs.plan.batch_workspace_bytes(plans), dtype=torch.uint8, device="cuda")
+    order = rng.permutation(len(plans))  # sizes interleaved in the job table
+    fs.plan.recon_batch([(plans[k], d_raw[k].data_ptr(), d_out[k].data_ptr()) for k in order],
+                        ws.data_ptr(), ws.numel())
+    torch.cuda.synchronize()
+    for k in range(len(plans)):
+        exp = oracle.recon_raw(sps[k], raws[k], fade=10)
+        assert rel_l2(d_out[k].cpu().numpy(), exp) < 1e-4, (plans[k].w, k)
 
 
 def test_live_widefield_and_attenuation(fs, oracle, torch_cuda):

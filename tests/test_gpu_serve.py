@@ -13,9 +13,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def channel(fs, n, seed, lam=525.0):
-    raw, truth = fs.synth.make_dataset(n=n, seed=seed, em_wavelength=lam, as_u16=True)
-    return raw, fs.synth.sim_param_for(truth, n)
+def channel(fs, n, seed, lam=525.0, n_phases=3):
+    raw, truth = fs.synth.make_dataset(n=n, seed=seed, em_wavelength=lam, as_u16=True, n_phases=n_phases)
+    return raw, fs.synth.sim_param_for(truth, n, n_phases=n_phases)
 
 
 def test_results_identical_alone_and_in_mix(fs):
@@ -36,6 +36,31 @@ def test_results_identical_alone_and_in_mix(fs):
         assert np.array_equal(out, alone[c])
     st = srv.stats()
     assert st["completed"] == len(order) and st["rejected"] == 0
+    srv.close()
+
+
+def test_fifteen_frame_stacks_identical_alone_and_in_mix(fs, oracle):
+    """15-frame (3 x 5) and 9-frame channels served together: each result equals its plan's
+    result alone, and the 15-frame results match the oracle's live reconstruction."""
+    specs = [(256, 21, 488.0, 5), (512, 22, 525.0, 5), (256, 23, 600.0, 3)]
+    chans = [channel(fs, n, s, lam, nph) for n, s, lam, nph in specs]
+    alone = []
+    for raw, sp in chans:
+        plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE, input_type=fs.native.INPUT_U16, fade_px=10)
+        alone.append(plan.reconstruct_host(raw))
+    for (raw, sp), a, (_, _, _, nph) in zip(chans, alone, specs):
+        if nph == 5:
+            exp, _ = oracle.live_recon(sp, raw)
+            assert np.linalg.norm(a - exp[0]) / np.linalg.norm(exp[0]) < 1e-4
+    srv = fs.plan.Server([sp for _, sp in chans], max_batch=8, max_inflight=32, streams=3, refit_every=0)
+    order = [0, 1, 2, 1, 0, 2, 2, 1, 0, 0, 1]
+    tickets = [(srv.submit(c, chans[c][0]), c) for c in order]
+    for tk, c in tickets:
+        n = chans[c][1].w
+        out = np.empty((2 * n, 2 * n), np.float32)
+        srv.wait(tk, out)
+        assert np.array_equal(out, alone[c])
+    assert srv.stats()["completed"] == len(order)
     srv.close()
 
 
