@@ -16,6 +16,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "fft_layouts.h"
 
 namespace fsim {
 
@@ -113,20 +114,31 @@ static int upload_stage_twiddles_this_tu() {
 }
 static int g_stw_registered = register_twiddle_uploader(&upload_stage_twiddles_this_tu);
 
-// ---- shared-memory addressing: one pad slot every 16 entries -------------------
-// Shared-memory layouts of the line buffers: one padding element per 16 (SW false), or a
-// permutation inside each 16-element group (SW true; the padding elements stay unused),
-// which avoids the 2-way bank conflicts of the stride-8 stage of 512-point lines on 64
-// threads but costs integer work per access. Measured per pass on GB300 (512^2 3x3, batch
-// 64): the column passes B1 and B2 gain with the permutation (B2 0.563 -> 0.508 ms), the
-// row passes A and C lose (A 0.613 -> 0.661 ms, spilling).
+// ---- shared-memory addressing -----------------------------------------------------
+// Layouts of the line buffers as the callers address them around a transform: one padding
+// element per 16 (SW false), or a permutation inside each 16-element group (SW true).
 template <bool SW>
 __device__ __forceinline__ int sidx_t(int a) {
   if constexpr (SW) return a ^ ((a >> 4) & 7) ^ (((a >> 6) & 1) << 3);
   else return a + (a >> 4);
 }
 __device__ __forceinline__ int sidx(int a) { return sidx_t<false>(a); }
-__host__ __device__ constexpr int smem_line_elems(int L, int C) { return L * C + (L * C) / 16 + 1; }
+// Layouts of the register-chained transform's inter-stage exchanges; fft_layouts.h picks
+// one per exchange with a bank model (gen_fft_layouts.py): 0 a + a/16, 1 a + a/16 + 2(a/32),
+// 2 a + a/16 + 4(a/64), 3 a + a/16 + 8(a/128), 4 the permutation of sidx_t<true>. Every
+// layout stays below a + a/8 + 1 entries, the size of a line buffer. On 512-point lines of
+// 8 elements per thread the second exchange pads by layout 1 (96 -> 64 modelled wavefronts
+// per warp pair and transform), and the first exchange of four interleaved lines too
+// (384 -> 256).
+template <int LAY>
+__device__ __forceinline__ int sidx_x(int a) {
+  if constexpr (LAY == 1) return a + (a >> 4) + ((a >> 5) << 1);
+  else if constexpr (LAY == 2) return a + (a >> 4) + ((a >> 6) << 2);
+  else if constexpr (LAY == 3) return a + (a >> 4) + ((a >> 7) << 3);
+  else if constexpr (LAY == 4) return sidx_t<true>(a);
+  else return a + (a >> 4);
+}
+__host__ __device__ constexpr int smem_line_elems(int L, int C) { return L * C + (L * C) / 8 + 1; }
 
 // ---- radix-R butterflies --------------------------------------------------------
 template <bool INV>
@@ -323,7 +335,7 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2*
 // 2(S-1) shared-memory passes for S stages instead of 2(S+1), and 2(S-1) barriers.
 // The caller must not be using `s` when the transform starts (the first stage writes it);
 // `s` is free again when it returns.
-template <int L, int T, int C, int R, int NS, bool INV, bool FIRST, bool LAST, bool SW>
+template <int L, int T, int C, int R, int NS, bool INV, bool FIRST, bool LAST>
 __device__ __forceinline__ void fft_stage_reg(float2 (&x)[L / T], float2* s, int c, int t, const float2* tw) {
   constexpr int E = L / T, NB = E / R, LR = L / R;
   constexpr int NT = NS > 1 ? (R == 16 ? 3 : (R >= 8 || R == 3 ? 2 : 1)) : 1;
@@ -338,13 +350,15 @@ __device__ __forceinline__ void fft_stage_reg(float2 (&x)[L / T], float2* s, int
       if constexpr (R == 16) tl[b][2] = tw[7 * NS + k];
     }
   }
+  // the exchange that feeds this stage, and the one this stage feeds (bank-model layouts)
+  constexpr int LIN = fft_xlay(L, E, C, NS), LOUT = fft_xlay(L, E, C, NS * R);
   float2 v[NB][R];
 #pragma unroll
   for (int b = 0; b < NB; b++)
 #pragma unroll
     for (int r = 0; r < R; r++) {
       if constexpr (FIRST) v[b][r] = x[b + NB * r];
-      else v[b][r] = s[sidx_t<SW>((t + b * T + r * LR) * C + c)];
+      else v[b][r] = s[sidx_x<LIN>((t + b * T + r * LR) * C + c)];
     }
   if constexpr (!FIRST) __syncthreads();
 #pragma unroll
@@ -385,24 +399,24 @@ __device__ __forceinline__ void fft_stage_reg(float2 (&x)[L / T], float2* s, int
     } else {
       const int base = (j / NS) * NS * R + k;
 #pragma unroll
-      for (int r = 0; r < R; r++) s[sidx_t<SW>((base + r * NS) * C + c)] = v[b][r];
+      for (int r = 0; r < R; r++) s[sidx_x<LOUT>((base + r * NS) * C + c)] = v[b][r];
     }
   }
   if constexpr (!LAST) __syncthreads();
 }
-template <int L, int T, int C, bool INV, int NS, bool SW>
+template <int L, int T, int C, bool INV, int NS>
 __device__ __forceinline__ void fft_stages_reg(float2 (&x)[L / T], float2* s, int c, int t, const float2* tw) {
   constexpr int R = pick_radix(L / NS, L / T);
   static_assert((L / NS) % R == 0 && (L / T) % R == 0, "bad radix plan");
-  fft_stage_reg<L, T, C, R, NS, INV, NS == 1, NS * R == L, SW>(x, s, c, t, tw);
-  if constexpr (NS * R < L) fft_stages_reg<L, T, C, INV, NS * R, SW>(x, s, c, t, tw + (R - 1) * NS);
+  fft_stage_reg<L, T, C, R, NS, INV, NS == 1, NS * R == L>(x, s, c, t, tw);
+  if constexpr (NS * R < L) fft_stages_reg<L, T, C, INV, NS * R>(x, s, c, t, tw + (R - 1) * NS);
 }
 // Transform line c of C interleaved lines held in registers (x[i] = element t + i*T),
 // with `s` (C interleaved lines, shared memory) as scratch; stage tables (g_stw layout).
-template <int L, int T, int C, bool INV, bool SW = false>
+template <int L, int T, int C, bool INV>
 __device__ __forceinline__ void line_fft_reg(float2 (&x)[L / T], float2* s, int c, int t, const float2* stw) {
   static_assert(supported_len(L) && plan_ok(L, T) && stw_ok(L, L / T), "no stage table for this plan");
-  fft_stages_reg<L, T, C, INV, 1, SW>(x, s, c, t, stw);
+  fft_stages_reg<L, T, C, INV, 1>(x, s, c, t, stw);
 }
 
 template <int L, int T, int C, bool INV, int NS, int TS, int M = 1>

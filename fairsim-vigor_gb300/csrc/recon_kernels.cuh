@@ -187,8 +187,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   // registers from one transform to the next (x[i] = element t + i*T), bz and bh serve as
   // scratch.
   // the band pairs of this block's angle (band 0 of every angle is the blockIdx.y == nA block's)
-  float2 x[EN], zk[EN];  // zk: the first pair's neg component, kept for the even-sample product
-  mix(1, zk);
+  float2 x[EN];
   // pair (neg, pos): only the neg component is transformed and stored. With
   // z_pos = conj(z_neg) and opposite shifts (ro_pos = conj(ro_neg), re_pos = conj(re_neg)):
   //   E_pos[m] = conj(E_neg[-m]),
@@ -199,10 +198,12 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   // forms it from the neg windows (mirror images of the pos windows) and d, kept here.
   for (int b = 1; b <= nPair; b++) {
     const int cn = 2 * b - 1;
-    if (b > 1) mix(cn, zk);
-#pragma unroll
-    for (int i = 0; i < EN; i++) x[i] = zk[i];
+    mix(cn, x);
     __syncthreads();  // the previous window reads of bh and bz are done
+    // the mixed row waits in bz (each thread its own elements) for the even-sample product
+    // below, instead of in 16 registers across the three transforms of the odd samples
+#pragma unroll
+    for (int i = 0; i < EN; i++) bz[sidx(t + i * T)] = x[i];
     line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);  // Z = FFT_N(z)
     if (t == (N / 2) % T) {
       const float2 zn = x[(N / 2) / T];
@@ -221,10 +222,11 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
     // even samples times the even-sample ramp, FFT: E
 #pragma unroll
-    for (int i = 0; i < EN; i++) zk[i] = cmul(zk[i], __ldg(re + t + i * T));
-    line_fft_reg<N, T, 1, false>(zk, bz, 0, t, twN);
+    for (int i = 0; i < EN; i++) x[i] = cmul(bz[sidx(t + i * T)], __ldg(re + t + i * T));
+    __syncthreads();  // every thread has its elements back before the transform reuses bz
+    line_fft_reg<N, T, 1, false>(x, bz, 0, t, twN);
 #pragma unroll
-    for (int i = 0; i < EN; i++) bz[sidx(t + i * T)] = zk[i];
+    for (int i = 0; i < EN; i++) bz[sidx(t + i * T)] = x[i];
     __syncthreads();
     // neg window of the shifted spectrum: E[X mod N] + exp(-2 pi i X/W) O[X mod N]
     const int Xs = J.win[2 * (a * nC + cn)];
@@ -324,7 +326,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   if (comp == 0) {  // band 0: summed over the angles and row-transformed in pass A (slot 0)
 #pragma unroll
     for (int i = 0; i < EN; i++) x[i] = J.I[quad + (size_t)(t + i * T) * 4];
-    line_fft_reg<N, T, CB, false, true>(x, bh, lane, t, twN);
+    line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);
 #pragma unroll
     for (int i = 0; i < EN; i++) bh[sidx_t<true>((t + i * T) * CB + lane)] = x[i];
     __syncthreads();
@@ -341,7 +343,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   const float2* I = J.I + (size_t)comp * nWin * N + quad;  // slot 1 + a*nPair + (b-1)
 #pragma unroll
   for (int i = 0; i < EN; i++) x[i] = I[(size_t)(t + i * T) * 4];
-  line_fft_reg<N, T, CB, false, true>(x, bh, lane, t, twN);  // Z along y
+  line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);  // Z along y
   if (t == (N / 2) % T) {
     const float2 z = x[(N / 2) / T];
     J.Dy[(size_t)(comp - 1) * nWin + xl] = make_float2(-2.f * z.y, -2.f * z.x);
@@ -351,16 +353,16 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   // odd samples, iFFT_N(Z * s), times the odd-sample ramp, FFT: O
 #pragma unroll
   for (int i = 0; i < EN; i++) x[i] = cmul(x[i], half_shift<N>(twW, t + i * T));
-  line_fft_reg<N, T, CB, true, true>(x, bh, lane, t, twN);
+  line_fft_reg<N, T, CB, true>(x, bh, lane, t, twN);
 #pragma unroll
   for (int i = 0; i < EN; i++) x[i] = cmul(x[i], __ldg(ro + t + i * T));
-  line_fft_reg<N, T, CB, false, true>(x, bh, lane, t, twN);
+  line_fft_reg<N, T, CB, false>(x, bh, lane, t, twN);
 #pragma unroll
   for (int i = 0; i < EN; i++) bh[sidx_t<true>((t + i * T) * CB + lane)] = x[i];
   // even samples (the column again, from L2) times the even-sample ramp, FFT: E
 #pragma unroll
   for (int i = 0; i < EN; i++) x[i] = cmul(I[(size_t)(t + i * T) * 4], __ldg(re + t + i * T));
-  line_fft_reg<N, T, CB, false, true>(x, bz, lane, t, twN);
+  line_fft_reg<N, T, CB, false>(x, bz, lane, t, twN);
 #pragma unroll
   for (int i = 0; i < EN; i++) bz[sidx_t<true>((t + i * T) * CB + lane)] = x[i];
   __syncthreads();
@@ -500,8 +502,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
     xe[i] = cadd(u0, u1);
     xo[i] = cmul(csub(u0, u1), cconjf(twW[k]));
   }
-  line_fft_reg<N, T, CB, true, true>(xe, bz, lane, t, twN);
-  line_fft_reg<N, T, CB, true, true>(xo, bh, lane, t, twN);
+  line_fft_reg<N, T, CB, true>(xe, bz, lane, t, twN);
+  line_fft_reg<N, T, CB, true>(xo, bh, lane, t, twN);
   if (X < N) {
 #pragma unroll
     for (int i = 0; i < EN; i++) {
