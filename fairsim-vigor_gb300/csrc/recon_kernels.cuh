@@ -27,7 +27,7 @@
 #define FSIM_B1_REGS 64
 #endif
 #ifndef FSIM_B2_REGS
-#define FSIM_B2_REGS 80
+#define FSIM_B2_REGS 64
 #endif
 
 namespace fsim {
@@ -83,7 +83,7 @@ __host__ __device__ constexpr int col_min_blocks() {
 }
 // Raw pixels fo + row + t + i*T (frame offset fo, row start row) with the background clip
 // and the border damping applied: all EN loads of the row are issued before any is used.
-template <int EN, int T>
+template <int EN, int T, bool DAMP = true>
 __device__ __forceinline__ void raw_row(const JobDesc& J, size_t fo, size_t row, int t, float (&v)[EN]) {
   if (J.input_u16) {
     const uint16_t* r = (const uint16_t*)J.raw + fo + row + t;
@@ -101,10 +101,24 @@ __device__ __forceinline__ void raw_row(const JobDesc& J, size_t fo, size_t row,
       if (v[i] < 0) v[i] = 0;
     }
   }
-  if (J.damp) {
+  if (DAMP && J.damp) {
     const float* d = J.damp + row + t;
 #pragma unroll
     for (int i = 0; i < EN; i++) v[i] = v[i] * __ldg(d + i * T);
+  }
+}
+// The border damping of a mixed row: the mix of damped rows is the damped mix (the damping
+// is one real factor per pixel), so the factors are read once per row, not once per frame.
+template <int EN, int T>
+__device__ __forceinline__ void damp_row(const JobDesc& J, size_t row, int t, float2 (&z)[EN]) {
+  if (J.damp) {
+    const float* d = J.damp + row + t;
+#pragma unroll
+    for (int i = 0; i < EN; i++) {
+      const float f = __ldg(d + i * T);
+      z[i].x *= f;
+      z[i].y *= f;
+    }
   }
 }
 
@@ -137,7 +151,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
 #pragma unroll 3
     for (int f = 0; f < nF; f++) {
       float v[EN];
-      raw_row<EN, T>(J, f * frame, row, t, v);
+      raw_row<EN, T, false>(J, f * frame, row, t, v);
       const float2 c = coef[f];
 #pragma unroll
       for (int i = 0; i < EN; i++) {
@@ -145,6 +159,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
         x[i].y += c.y * v[i];
       }
     }
+    damp_row<EN, T>(J, row, t, x);
     line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
 #pragma unroll
     for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
@@ -172,7 +187,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
 #pragma unroll 1
     for (int p = 0; p < nP; p++) {
       float v[EN];
-      raw_row<EN, T>(J, (size_t)(a * nP + p) * frame, row, t, v);
+      raw_row<EN, T, false>(J, (size_t)(a * nP + p) * frame, row, t, v);
       const float2 m = coef[cm * nP + p];
 #pragma unroll
       for (int i = 0; i < EN; i++) {
@@ -180,6 +195,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
         z[i].y += m.y * v[i];
       }
     }
+    damp_row<EN, T>(J, row, t, z);
   };
   // Components: band 0, then per band b the pair neg = 2b-1, pos = 2b. The separation
   // coefficients of a pair are complex conjugates, so z_pos = conj(z_neg): the pos
@@ -380,8 +396,9 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
 // H(X, Y) = (F(X, Y) + conj F(-X, -Y)) / 2, so only the columns X = 0..N of H are formed and
 // stored (pass C completes each row by symmetry): half the column-transformed windows,
 // masks and Wiener x apodization reads, inverse transforms and writes of a full-width pass.
-// CB output columns per block; each thread keeps the 2*EN rows Y = t + i*T of its column in
-// registers. With the pair identities of pass A (the pos component of a pair at (X, Y) is
+// CB output columns per block, 2T threads per column: each thread keeps the EN rows
+// Y = t + i*2T of its column in registers (twice the threads of a transform, so that twice
+// the loads are in flight for the same registers). With the pair identities of pass A (the pos component of a pair at (X, Y) is
 // the conjugate of the neg transform at (-X, -Y) plus two rank-one Nyquist terms n1, and
 // the neg/pos masks are mirror images: mask_neg(-X,-Y) = mask_pos(X,Y)), a pair adds
 //   H += mask_neg(X,Y) (A + conj(n2)/2) + mask_pos(X,Y) (conj(B) + n1/2),
@@ -391,13 +408,14 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
 //   n1(X,Y) = exp(-2 pi i Y/W) d'(-X) Qy[Y mod N] + exp(-2 pi i X/W) Qx[X mod N] G[Y];
 // band 0 adds mask_0(X,Y) (T0(X,Y) + conj T0(-X,-Y)) / 2.
 template <int N, int ENV, int CBV>
-__global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
-                                  col_min_blocks<Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T, Cfg<N, ENV, CBV>::EN,
-                                                 FSIM_B2_REGS>())
+__global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
+                                  col_min_blocks<2 * Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T,
+                                                 Cfg<N, ENV, CBV>::EN, FSIM_B2_REGS>())
     k_pass_b2(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N, ENV, CBV>;
-  constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN;
-  const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
+  constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN, T2 = 2 * T;
+  static_assert(EN % 2 == 0, "rows k and k + N must share a thread");
+  const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;  // t in [0, 2T)
   const int X = blockIdx.x * CB + lane;  // X <= N + CB - 1 < W; only X <= N is stored
   __shared__ JobDesc J;
   extern __shared__ float2 sm[];
@@ -405,14 +423,14 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   float2* bh = bz + smem_line_elems(N, CB);  // N x CB
   const float2* twN = g_stw + stw_offset(N, EN);
   const float2* twW = g_tw + tw_offset(W);
-  load_job(&J, jobs + blockIdx.y, lt, CB * T);
+  load_job(&J, jobs + blockIdx.y, lt, CB * T2);
   __syncthreads();
   const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2;
   auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
   const int Xm = wrap(-X);
-  float2 acc[2 * EN];
+  float2 acc[EN];
 #pragma unroll
-  for (int i = 0; i < 2 * EN; i++) acc[i] = make_float2(0.f, 0.f);
+  for (int i = 0; i < EN; i++) acc[i] = make_float2(0.f, 0.f);
   // window position (xl, yl) -> offset in a quad-layout nWin x nWin window
   auto qoff = [&](int xl) { return ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3); };
   {  // band 0: (T0(X,Y) + conj T0(-X,-Y)) / 2, one symmetric mask
@@ -423,8 +441,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
       const float2* tm = J.Tw + qoff(xlm);
       const bool mirror_in = xlm < nWin;  // (X,Y) in the support puts -X in the window
 #pragma unroll
-      for (int i = 0; i < 2 * EN; i++) {
-        const int Y = t + i * T;
+      for (int i = 0; i < EN; i++) {
+        const int Y = t + i * T2;
         const int yl = wrap(Y - Ys), ylm = wrap(wrap(-Y) - Ys);
         if (yl < nWin) {
           const float f = 0.5f * __ldg(mk + (size_t)yl * 4);
@@ -451,8 +469,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
         const float2 dX = J.Dy[(size_t)ab * nWin + xn];
         const float2 cxm = cmul(twW[Xm], __ldg(Qx + (Xm < N ? Xm : Xm - N)));
 #pragma unroll
-        for (int i = 0; i < 2 * EN; i++) {
-          const int Y = t + i * T;
+        for (int i = 0; i < EN; i++) {
+          const int Y = t + i * T2;
           const int yl = wrap(Y - Yn);
           if (yl < nWin) {
             const int Ym = wrap(-Y);
@@ -475,8 +493,8 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
         const float2 dM = J.Dy[(size_t)ab * nWin + xm];
         const float2 cx = cmul(twW[X], __ldg(Qx + (X < N ? X : X - N)));
 #pragma unroll
-        for (int i = 0; i < 2 * EN; i++) {
-          const int Y = t + i * T;
+        for (int i = 0; i < EN; i++) {
+          const int Y = t + i * T2;
           const int yl = wrap(Y - Yp);
           if (yl < nWin) {
             const float f = __ldg(mk + (size_t)yl * 4);
@@ -490,34 +508,37 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
     }
   }
   // Wiener denominator x apodization, then iFFT_W along y as two N-point inverse FFTs:
-  //   out[2n] = iFFT_N(A[k] + A[k+N]),  out[2n+1] = iFFT_N((A[k] - A[k+N]) exp(i pi k/N))
-  const float* wa = J.wa + (size_t)(X >> 2) * W * 4 + (X & 3);
-  float2 xe[EN], xo[EN];  // even and odd output rows, in registers through the transforms
+  //   out[2n] = iFFT_N(A[k] + A[k+N]),  out[2n+1] = iFFT_N((A[k] - A[k+N]) exp(i pi k/N));
+  // rows k and k + N are acc[i] and acc[i + EN/2] of one thread. The even sequences of the CB
+  // columns go to bz, the odd ones to bh; threads of the first half then transform the even
+  // lines and those of the second half the odd ones.
+  {
+    const float* wa = J.wa + (size_t)(X >> 2) * W * 4 + (X & 3);
 #pragma unroll
-  for (int i = 0; i < EN; i++) {
-    const int k = t + i * T;
-    const float f0 = __ldg(wa + (size_t)k * 4), f1 = __ldg(wa + (size_t)(k + N) * 4);
-    const float2 u0 = make_float2(acc[i].x * f0, acc[i].y * f0);
-    const float2 u1 = make_float2(acc[i + EN].x * f1, acc[i + EN].y * f1);
-    xe[i] = cadd(u0, u1);
-    xo[i] = cmul(csub(u0, u1), cconjf(twW[k]));
+    for (int i = 0; i < EN / 2; i++) {
+      const int k = t + i * T2;
+      const float f0 = __ldg(wa + (size_t)k * 4), f1 = __ldg(wa + (size_t)(k + N) * 4);
+      const float2 u0 = make_float2(acc[i].x * f0, acc[i].y * f0);
+      const float2 u1 = make_float2(acc[i + EN / 2].x * f1, acc[i + EN / 2].y * f1);
+      bz[sidx_t<true>(k * CB + lane)] = cadd(u0, u1);
+      bh[sidx_t<true>(k * CB + lane)] = cmul(csub(u0, u1), cconjf(twW[k]));
+    }
   }
-  line_fft_reg<N, T, CB, true>(xe, bz, lane, t, twN);
-  line_fft_reg<N, T, CB, true>(xo, bh, lane, t, twN);
-  if (X < N) {
+  __syncthreads();
+  const int g = lt / (CB * T), il = lt % CB, it = (lt / CB) % T;
+  float2* buf = g ? bh : bz;
+  float2 x[EN];  // element it + i*T of line il (even rows for g = 0, odd rows for g = 1)
 #pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int k = t + i * T;
-      J.O[(size_t)(2 * k) * N + X] = xe[i];
-      J.O[(size_t)(2 * k + 1) * N + X] = xo[i];
-    }
-  } else if (X == N) {
+  for (int i = 0; i < EN; i++) x[i] = buf[sidx_t<true>((it + i * T) * CB + il)];
+  __syncthreads();  // every thread holds its elements before the transforms reuse the buffers
+  line_fft_reg<N, T, CB, true>(x, buf, il, it, twN);
+  const int Xo = blockIdx.x * CB + il;
+  if (Xo < N) {
 #pragma unroll
-    for (int i = 0; i < EN; i++) {
-      const int k = t + i * T;
-      J.On[2 * k] = xe[i];
-      J.On[2 * k + 1] = xo[i];
-    }
+    for (int i = 0; i < EN; i++) J.O[(size_t)(2 * (it + i * T) + g) * N + Xo] = x[i];
+  } else if (Xo == N) {
+#pragma unroll
+    for (int i = 0; i < EN; i++) J.On[2 * (it + i * T) + g] = x[i];
   }
 }
 
@@ -625,8 +646,8 @@ static int launch_b2(const JobDesc* d_jobs, int njobs, cudaStream_t st) {
     FSIM_CUDA(cudaFuncSetAttribute(k_pass_b2<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  // the Hermitian half: columns 0..N
-  k_pass_b2<N, ENB, CBB><<<dim3(N / PB::CB + 1, njobs), PB::CB * PB::T, smem, st>>>(d_jobs);
+  // the Hermitian half: columns 0..N, 2T threads per column
+  k_pass_b2<N, ENB, CBB><<<dim3(N / PB::CB + 1, njobs), 2 * PB::CB * PB::T, smem, st>>>(d_jobs);
   return FSIM_OK;
 }
 
