@@ -393,6 +393,7 @@ void Plan::fill_job_live(JobDesc& j, const void* raw, float* out, float* wf, cha
   j.On = nullptr;
   j.clip_max = nullptr;
   j.clip = 0;
+  j.cmask = 0;
   j.fwf = nullptr;
   j.wff = nullptr;
   j.Wf = nullptr;

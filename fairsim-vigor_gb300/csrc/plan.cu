@@ -84,6 +84,8 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
     FSIM_REQUIRE(((uintptr_t)jobs[i].widefield & 7) == 0 && ((uintptr_t)jobs[i].filtered_widefield & 7) == 0,
                  FSIM_EINVAL, "job %d: widefield outputs must be 8-byte aligned", i);
     FSIM_REQUIRE(((uintptr_t)jobs[i].out & 7) == 0, FSIM_EINVAL, "job %d: the output must be 8-byte aligned", i);
+    FSIM_REQUIRE(!jobs[i].filtered_widefield || !otf_measured(&static_cast<const Plan*>(jobs[i].plan)->prm), FSIM_EINVAL,
+                 "job %d: the filtered widefield needs an estimated OTF (its filter is real)", i);
     order[i] = i;
   }
   auto key = [&](int i) {
@@ -145,10 +147,15 @@ int recon_batch(const fsim_job* jobs, int n, void* ws, size_t ws_bytes, cudaStre
     // largest classes sort last; the first class stays on st, the rest spread over aux
     cudaStream_t s = (nfork > 0 && g > 0) ? aux[(g - 1) % nfork] : st;
     bool scale_clip = false;
-    for (int i = k; i < e; i++) scale_clip = scale_clip || static_cast<const Plan*>(jobs[order[i]].plan)->clip_scale == 2;
+    int masks = 0;
+    for (int i = k; i < e; i++) {
+      const Plan* pi = static_cast<const Plan*>(jobs[order[i]].plan);
+      scale_clip = scale_clip || pi->clip_scale == 2;
+      masks |= otf_measured(&pi->prm) ? 2 : 1;
+    }
     rc = (p0->path == FSIM_PATH_LIVE)
              ? launch_live_size(p0->prm.w, d_table + k, e - k, maxA, s)
-             : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxPair, maxWin, scale_clip, s);
+             : launch_offline_size(p0->prm.w, d_table + k, e - k, maxA, maxPair, maxWin, scale_clip, masks, s);
     if (rc == FSIM_OK && p0->path == FSIM_PATH_OFFLINE) {
       bool wf = false;
       for (int i = k; i < e; i++) wf = wf || jobs[order[i]].widefield || jobs[order[i]].filtered_widefield;
@@ -219,8 +226,8 @@ int fsim_plan_create(fsim_plan** out, const fsim_sim_param* p, int path, int inp
   FSIM_REQUIRE(p->nr_phases <= FSIM_MAX_PHASES && 2 * p->nr_bands - 1 <= 7, FSIM_EINVAL, "too many phases/bands");
   FSIM_REQUIRE(p->filter_style == FSIM_FILTER_WIENER, FSIM_EINVAL,
                "fused plans apply the Wiener filter; RL filter styles run through fsim_run_reconstruction");
-  FSIM_REQUIRE(!otf_measured(p), FSIM_EINVAL,
-               "fused plans take estimated OTFs; measured OTFs run through fsim_run_reconstruction");
+  FSIM_REQUIRE(path == FSIM_PATH_OFFLINE || !otf_measured(p), FSIM_EINVAL,
+               "live plans take estimated OTFs; measured OTFs run through offline plans or fsim_run_reconstruction");
   NEED_INIT();
   fsim_plan* pl = new fsim_plan();
   pl->prm = *p;
@@ -246,8 +253,10 @@ int fsim_plan_update(fsim_plan* plan, const fsim_sim_param* p) {
   FSIM_REQUIRE(p->w == plan->prm.w && p->nr_dirs == plan->prm.nr_dirs && p->nr_bands == plan->prm.nr_bands &&
                    p->nr_phases == plan->prm.nr_phases,
                FSIM_EINVAL, "plan_update: geometry (size, dirs, bands, phases) must not change");
-  FSIM_REQUIRE(p->filter_style == FSIM_FILTER_WIENER && !otf_measured(p), FSIM_EINVAL,
-               "fused plans apply the Wiener filter with an estimated OTF");
+  FSIM_REQUIRE(p->filter_style == FSIM_FILTER_WIENER && (plan->path == FSIM_PATH_OFFLINE || !otf_measured(p)),
+               FSIM_EINVAL, "fused plans apply the Wiener filter; live plans take estimated OTFs");
+  FSIM_REQUIRE(otf_measured(p) == otf_measured(&plan->prm), FSIM_EINVAL,
+               "plan_update: an estimated OTF cannot become a measured one (or back) in place");
   // callers may have work in flight that reads the old tables
   FSIM_CUDA(cudaDeviceSynchronize());
   plan->prm = *p;

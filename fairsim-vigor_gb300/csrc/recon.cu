@@ -40,15 +40,24 @@ namespace fsim {
 std::vector<float> fade_vector(int w, int h, int px);
 
 // ---- plan build kernels -------------------------------------------------------------------------
-// conj(OTF(r - k)) mask of one component over its window, quad layout [xl/4][yl][xl%4]
+// conj(OTF(r - k)) mask of one component over its window, quad layout [xl/4][yl][xl%4]:
+// real values for estimated OTFs; complex values (float2) of OTF band `band` for measured
+// ones (OtfProvider.applyOtf(vec, band, kx, ky), S/SimAlgorithm.java:397-403)
 __global__ void k_build_mask(float* __restrict__ mask, int W, int nWin, int Xs, int Ys, double kx, double ky,
-                             const OtfTable* __restrict__ t, int att) {
+                             const OtfTable* __restrict__ t, int att, int band) {
   const int xl = blockIdx.x * blockDim.x + threadIdx.x, yl = blockIdx.y;
   if (xl >= nWin) return;
   int X = (Xs + xl) % W, Y = (Ys + yl) % W;
+  const size_t i = ((size_t)(xl >> 2) * nWin + yl) * 4 + (xl & 3);
+  if (t->measured) {
+    float2 c = make_float2(0.f, 0.f);
+    if (!otf_at_c(*t, band, (double)freq_x(X, W), (double)freq_y(Y, W), kx, ky, att != 0, &c)) c = make_float2(0.f, 0.f);
+    reinterpret_cast<float2*>(mask)[i] = make_float2(c.x, -c.y);
+    return;
+  }
   float v = 0.f;
   if (!otf_at(*t, (double)freq_x(X, W), (double)freq_y(Y, W), kx, ky, att != 0, &v)) v = 0.f;
-  mask[((size_t)(xl >> 2) * nWin + yl) * 4 + (xl & 3)] = v;
+  mask[i] = v;
 }
 
 // 1/(sum |OTF|^2 + w^2) * apo, quad layout [X/4][Y][X%4]
@@ -64,11 +73,22 @@ __global__ void k_build_wa(float* __restrict__ wa, int W, const OtfTable* __rest
       const double kx = shifts.px[d] * b, ky = shifts.py[d] * b;
       double r1 = __dmul_rn(d_hypot_java(__dsub_rn(xh, kx), __dsub_rn(yh, ky)), cpm);
       double r2 = __dmul_rn(d_hypot_java(__dadd_rn(xh, kx), __dadd_rn(yh, ky)), cpm);
-      float o1 = otf_val(*t, r1, false), o2 = otf_val(*t, r2, false);
-      float v1 = __fmul_rn(o1, o1), v2 = __fmul_rn(o2, o2);
-      if (use_att) {
-        v1 = __fmul_rn(v1, att_val(*t, r1));
-        v2 = __fmul_rn(v2, att_val(*t, r2));
+      float v1, v2;
+      if (t->measured) {  // band b's complex values, |OTF|^2 as Cplx.Float.absSq (WienerFilter.java)
+        v1 = abs_sq(otf_val_c(*t, b, r1, false));
+        v2 = abs_sq(otf_val_c(*t, b, r2, false));
+        if (use_att) {
+          v1 = __fmul_rn(v1, att_val_b(*t, b, r1));
+          v2 = __fmul_rn(v2, att_val_b(*t, b, r2));
+        }
+      } else {
+        const float o1 = otf_val(*t, r1, false), o2 = otf_val(*t, r2, false);
+        v1 = __fmul_rn(o1, o1);
+        v2 = __fmul_rn(o2, o2);
+        if (use_att) {
+          v1 = __fmul_rn(v1, att_val(*t, r1));
+          v2 = __fmul_rn(v2, att_val(*t, r2));
+        }
       }
       acc = __fadd_rn(__fadd_rn(acc, v1), v2);
     }
@@ -195,7 +215,8 @@ int Plan::build(cudaStream_t st) {
   size_t off_otf = off_win + al(win.size() * sizeof(int));
   size_t off_damp = off_otf + al(sizeof(OtfTable));
   size_t off_mask = off_damp + al((size_t)N * N * sizeof(float));
-  size_t off_wa = off_mask + al((size_t)nA * nC * nwin * nwin * sizeof(float));
+  const size_t mask_elem = otf_measured(&prm) ? sizeof(float2) : sizeof(float);
+  size_t off_wa = off_mask + al((size_t)nA * nC * nwin * nwin * mask_elem);
   size_t off_nyq = off_wa + al((size_t)W * W * sizeof(float));
   size_t off_wff = off_nyq + al(nyq.size() * sizeof(float2));
   size_t total = off_wff + al((size_t)N * N * sizeof(float));
@@ -233,8 +254,9 @@ int Plan::build(cudaStream_t st) {
       double kx, ky;
       comp_shift(&prm, a, c, &kx, &ky);
       dim3 g(div_up(nwin, 128), nwin);
-      k_build_mask<<<g, 128, 0, st>>>(d_masks + (size_t)(a * nC + c) * nwin * nwin, W, nwin, win[2 * (a * nC + c)],
-                                      win[2 * (a * nC + c) + 1], kx, ky, d_otf, prm.use_attenuation);
+      k_build_mask<<<g, 128, 0, st>>>(d_masks + (size_t)(a * nC + c) * nwin * nwin * (mask_elem / sizeof(float)), W,
+                                      nwin, win[2 * (a * nC + c)], win[2 * (a * nC + c) + 1], kx, ky, d_otf,
+                                      prm.use_attenuation, (c + 1) / 2);
     }
   {
     dim3 g(div_up(W, 128), W);
@@ -287,6 +309,7 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, float* f
   j.nP = prm.nr_phases;
   j.nC = nC;
   j.nWin = nwin;
+  j.cmask = otf_measured(&prm) ? 1 : 0;
   j.clip = clip_scale;
   j.bgr = (float)bgr;
   j.damp = d_damp;
@@ -327,15 +350,15 @@ int offline_tune_get(int n, int pass) {
   return (k < 0 || pass < 0 || pass > 2) ? -1 : var_table(pass)[k];
 }
 
-extern template int launch_offline<64>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
-extern template int launch_offline<128>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
-extern template int launch_offline<192>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
-extern template int launch_offline<256>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
-extern template int launch_offline<384>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
-extern template int launch_offline<512>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
-extern template int launch_offline<768>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
-extern template int launch_offline<1024>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
-extern template int launch_offline<2048>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+extern template int launch_offline<64>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
+extern template int launch_offline<128>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
+extern template int launch_offline<192>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
+extern template int launch_offline<256>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
+extern template int launch_offline<384>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
+extern template int launch_offline<512>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
+extern template int launch_offline<768>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
+extern template int launch_offline<1024>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
+extern template int launch_offline<2048>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
 
 #define FSIM_RECON_SIZES(X) X(64) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(2048)
 
@@ -351,11 +374,11 @@ bool offline_size_supported(int n) {
 }
 
 int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, bool scale_clip,
-                        cudaStream_t st) {
+                        int masks, cudaStream_t st) {
   switch (n) {
 #define CASE(v) \
   case v:       \
-    return launch_offline<v>(d_jobs, njobs, maxA, maxPair, maxWin, scale_clip, st);
+    return launch_offline<v>(d_jobs, njobs, maxA, maxPair, maxWin, scale_clip, masks, st);
     FSIM_RECON_SIZES(CASE)
 #undef CASE
   }

@@ -12,13 +12,14 @@ struct JobDesc {
   float* out;         // W*W reconstruction
   float* widefield;   // N*N (live path), nullable
   int input_u16, nA, nP, nC, nWin;
-  int clip;  // offline output: 0 CLIPSCALE.NONE, 1 CLIP, 2 BOTH
+  int clip;   // offline output: 0 CLIPSCALE.NONE, 1 CLIP, 2 BOTH
+  int cmask;  // offline: masks are complex (float2; measured OTFs), else real
   float bgr;
   const float* damp;    // N*N border fade, nullable
   const float2* coef;   // [a][c][p] separation coefficients
   const float2* ramps;  // [a][c] {x ramp[W], y ramp[W]}  (offline) / {x ramp[N], y ramp[N]} (live)
   const int* win;       // [a][c] {Xs, Ys} window origins (offline) / {xInt, yInt} paste offsets (live)
-  const float* masks;   // [a][c] OTF masks (offline) / N*N conj-OTF vector (live)
+  const float* masks;   // [a][c] OTF masks (offline; float2 when cmask) / N*N conj-OTF vector (live)
   const float* wa;      // Wiener x apodization, quad layout [X/4][Y][X%4]
   const float2* nyq;    // offline: [a][b-1][x, y][N] FFT_N((-1)^n ro_pos[n]) of the pos component's x and y
                         // odd-sample ramps (the Nyquist response, see pass A)
@@ -87,8 +88,9 @@ bool live_size_supported(int n);
 // maxA, maxPair, maxWin: the largest angle count, band-pair count and OTF-support window
 // of the batch's datasets of size n (they bound the grids; extra blocks exit at once)
 // scale_clip: some job of the class asks for CLIPSCALE.BOTH (one more pass scales its image)
+// masks: bit 0 some job of the class has real OTF masks, bit 1 some has complex ones
 int launch_offline_size(int n, const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, bool scale_clip,
-                        cudaStream_t st);
+                        int masks, cudaStream_t st);
 int launch_live_size(int n, const JobDesc* d_jobs, int njobs, int maxA, cudaStream_t st);
 // widefield and filtered widefield of the offline jobs that ask for them (widefield.cu);
 // launched after launch_offline_size on the same stream (it reuses the job workspaces)

@@ -3,6 +3,6 @@
 #include "recon_kernels.cuh"
 
 namespace fsim {
-template int launch_offline<768>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
-template int launch_offline<1024>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+template int launch_offline<768>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
+template int launch_offline<1024>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
 }  // namespace fsim

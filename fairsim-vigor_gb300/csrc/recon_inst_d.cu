@@ -3,5 +3,5 @@
 #include "recon_kernels.cuh"
 
 namespace fsim {
-template int launch_offline<2048>(const JobDesc*, int, int, int, int, bool, cudaStream_t);
+template int launch_offline<2048>(const JobDesc*, int, int, int, int, bool, int, cudaStream_t);
 }  // namespace fsim

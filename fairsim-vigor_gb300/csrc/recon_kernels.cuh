@@ -407,7 +407,11 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
 // n1 / n2 the pos component's Nyquist terms at (X, Y) / (-X, -Y):
 //   n1(X,Y) = exp(-2 pi i Y/W) d'(-X) Qy[Y mod N] + exp(-2 pi i X/W) Qx[X mod N] G[Y];
 // band 0 adds mask_0(X,Y) (T0(X,Y) + conj T0(-X,-Y)) / 2.
-template <int N, int ENV, int CBV>
+// Measured OTFs give complex masks (CM): the masks still depend on |k - shift| only, so the
+// mirror relations hold, and a pair adds Re(mask_neg) A + Re(mask_pos) conj(B) +
+// (mask_pos n1 + conj(mask_neg n2)) / 2, band 0 (mask_0 T0(X,Y) + conj(mask_0 T0(-X,-Y))) / 2.
+// A launch of one kind skips the jobs of the other (uniform per block).
+template <int N, int ENV, int CBV, bool CM>
 __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
                                   col_min_blocks<2 * Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T,
                                                  Cfg<N, ENV, CBV>::EN, FSIM_B2_REGS>())
@@ -425,9 +429,11 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   const float2* twW = g_tw + tw_offset(W);
   load_job(&J, jobs + blockIdx.y, lt, CB * T2);
   __syncthreads();
+  if ((J.cmask != 0) != CM) return;  // the other launch's job (uniform per block)
   const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2;
   auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
   const int Xm = wrap(-X);
+  const float2* cmasks = reinterpret_cast<const float2*>(J.masks);  // complex masks (CM)
   float2 acc[EN];
 #pragma unroll
   for (int i = 0; i < EN; i++) acc[i] = make_float2(0.f, 0.f);
@@ -437,6 +443,7 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
     const int xl = wrap(X - J.win[0]), xlm = wrap(Xm - J.win[0]), Ys = J.win[1];
     if (xl < nWin) {
       const float* mk = J.masks + qoff(xl);
+      const float2* mkc = cmasks + qoff(xl);
       const float2* tv = J.Tw + qoff(xl);
       const float2* tm = J.Tw + qoff(xlm);
       const bool mirror_in = xlm < nWin;  // (X,Y) in the support puts -X in the window
@@ -445,11 +452,18 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
         const int Y = t + i * T2;
         const int yl = wrap(Y - Ys), ylm = wrap(wrap(-Y) - Ys);
         if (yl < nWin) {
-          const float f = 0.5f * __ldg(mk + (size_t)yl * 4);
           const float2 u = tv[(size_t)yl * 4];
           const float2 um = (mirror_in && ylm < nWin) ? tm[(size_t)ylm * 4] : make_float2(0.f, 0.f);
-          acc[i].x += f * (u.x + um.x);
-          acc[i].y += f * (u.y - um.y);
+          if constexpr (CM) {
+            const float2 m = __ldg(mkc + (size_t)yl * 4);
+            const float2 p = cmul(m, u), q = cmul(m, um);
+            acc[i].x += 0.5f * (p.x + q.x);
+            acc[i].y += 0.5f * (p.y - q.y);
+          } else {
+            const float f = 0.5f * __ldg(mk + (size_t)yl * 4);
+            acc[i].x += f * (u.x + um.x);
+            acc[i].y += f * (u.y - um.y);
+          }
         }
       }
     }
@@ -465,6 +479,7 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
       if (xn < nWin) {  // neg at (X, Y), and the pos component's n2 at (-X, -Y)
         const int Yn = J.win[2 * (a * nC + cn) + 1];
         const float* mk = J.masks + (size_t)(a * nC + cn) * nWin * nWin + qoff(xn);
+        const float2* mkc = cmasks + (size_t)(a * nC + cn) * nWin * nWin + qoff(xn);
         const float2* tv = Tc + qoff(xn);
         const float2 dX = J.Dy[(size_t)ab * nWin + xn];
         const float2 cxm = cmul(twW[Xm], __ldg(Qx + (Xm < N ? Xm : Xm - N)));
@@ -474,13 +489,19 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
           const int yl = wrap(Y - Yn);
           if (yl < nWin) {
             const int Ym = wrap(-Y);
-            const float f = __ldg(mk + (size_t)yl * 4);
             const float2 A = tv[(size_t)yl * 4];
             // n2: its pos-window row is nWin-1-yl (the windows are mirror images)
             const float2 n2 = cadd(cmul(twW[Ym], cmul(dX, __ldg(Qy + (Ym < N ? Ym : Ym - N)))),
                                    cmul(cxm, G[nWin - 1 - yl]));
-            acc[i].x += f * (A.x + 0.5f * n2.x);
-            acc[i].y += f * (A.y - 0.5f * n2.y);
+            if constexpr (CM) {
+              const float2 m = __ldg(mkc + (size_t)yl * 4), q = cmul(m, n2);
+              acc[i].x += m.x * A.x + 0.5f * q.x;
+              acc[i].y += m.x * A.y - 0.5f * q.y;
+            } else {
+              const float f = __ldg(mk + (size_t)yl * 4);
+              acc[i].x += f * (A.x + 0.5f * n2.x);
+              acc[i].y += f * (A.y - 0.5f * n2.y);
+            }
           }
         }
       }
@@ -489,6 +510,7 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
         const int Yp = J.win[2 * (a * nC + cp) + 1];
         const int xm = nWin - 1 - xp;  // window column of -X in the neg window
         const float* mk = J.masks + (size_t)(a * nC + cp) * nWin * nWin + qoff(xp);
+        const float2* mkc = cmasks + (size_t)(a * nC + cp) * nWin * nWin + qoff(xp);
         const float2* tv = Tc + qoff(xm);
         const float2 dM = J.Dy[(size_t)ab * nWin + xm];
         const float2 cx = cmul(twW[X], __ldg(Qx + (X < N ? X : X - N)));
@@ -497,11 +519,17 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
           const int Y = t + i * T2;
           const int yl = wrap(Y - Yp);
           if (yl < nWin) {
-            const float f = __ldg(mk + (size_t)yl * 4);
             const float2 B = tv[(size_t)(nWin - 1 - yl) * 4];
             const float2 n1 = cadd(cmul(twW[Y], cmul(dM, __ldg(Qy + (Y < N ? Y : Y - N)))), cmul(cx, G[yl]));
-            acc[i].x += f * (B.x + 0.5f * n1.x);
-            acc[i].y += f * (-B.y + 0.5f * n1.y);
+            if constexpr (CM) {
+              const float2 m = __ldg(mkc + (size_t)yl * 4), q = cmul(m, n1);
+              acc[i].x += m.x * B.x + 0.5f * q.x;
+              acc[i].y += -m.x * B.y + 0.5f * q.y;
+            } else {
+              const float f = __ldg(mk + (size_t)yl * 4);
+              acc[i].x += f * (B.x + 0.5f * n1.x);
+              acc[i].y += f * (-B.y + 0.5f * n1.y);
+            }
           }
         }
       }
@@ -637,18 +665,27 @@ static int launch_b1(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, in
                            st>>>(d_jobs);
   return FSIM_OK;
 }
-template <int N, int ENB, int CBB>
-static int launch_b2(const JobDesc* d_jobs, int njobs, cudaStream_t st) {
+template <int N, int ENB, int CBB, bool CM>
+static int launch_b2_kind(const JobDesc* d_jobs, int njobs, cudaStream_t st) {
   using PB = Cfg<N, ENB, CBB>;
   const size_t smem = sizeof(float2) * 2 * smem_line_elems(N, PB::CB);
   static bool attr = false;
   if (!attr) {
-    FSIM_CUDA(cudaFuncSetAttribute(k_pass_b2<N, ENB, CBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FSIM_CUDA(
+        cudaFuncSetAttribute(k_pass_b2<N, ENB, CBB, CM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
   // the Hermitian half: columns 0..N, 2T threads per column
-  k_pass_b2<N, ENB, CBB><<<dim3(N / PB::CB + 1, njobs), 2 * PB::CB * PB::T, smem, st>>>(d_jobs);
+  k_pass_b2<N, ENB, CBB, CM><<<dim3(N / PB::CB + 1, njobs), 2 * PB::CB * PB::T, smem, st>>>(d_jobs);
   return FSIM_OK;
+}
+// masks: bit 0 launches the real-mask kind, bit 1 the complex-mask kind (measured OTFs)
+template <int N, int ENB, int CBB>
+static int launch_b2(const JobDesc* d_jobs, int njobs, int masks, cudaStream_t st) {
+  int rc = FSIM_OK;
+  if (masks & 1) rc = launch_b2_kind<N, ENB, CBB, false>(d_jobs, njobs, st);
+  if (!rc && (masks & 2)) rc = launch_b2_kind<N, ENB, CBB, true>(d_jobs, njobs, st);
+  return rc;
 }
 
 // tuned variants per size: index into the variant lists of launch_offline
@@ -672,7 +709,7 @@ __host__ inline int size_slot(int n) {
 // (elements, columns per block) {(E0,4), (E0,2), (E1,4), (E1,2)} with E0 = 8, E1 = 16
 // (3*2^k sizes: 12, 24). The extremes (N <= 128, N >= 2048) have one variant.
 template <int N>
-int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, bool scale_clip,
+int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int maxWin, bool scale_clip, int masks,
                    cudaStream_t st) {
   constexpr bool p3 = (N % 3 == 0);
   constexpr int E0 = p3 ? 12 : 8, E1 = p3 ? 24 : 16;
@@ -703,13 +740,13 @@ int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int 
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[2], st);
   if constexpr (single) {
-    rc = launch_b2<N, E0, CBX>(d_jobs, njobs, st);
+    rc = launch_b2<N, E0, CBX>(d_jobs, njobs, masks, st);
   } else {
     switch (vb2) {
-      case 0: rc = launch_b2<N, E0, 4>(d_jobs, njobs, st); break;
-      case 1: rc = launch_b2<N, E0, 2>(d_jobs, njobs, st); break;
-      case 2: rc = launch_b2<N, E1, 4>(d_jobs, njobs, st); break;
-      default: rc = launch_b2<N, E1, 2>(d_jobs, njobs, st); break;
+      case 0: rc = launch_b2<N, E0, 4>(d_jobs, njobs, masks, st); break;
+      case 1: rc = launch_b2<N, E0, 2>(d_jobs, njobs, masks, st); break;
+      case 2: rc = launch_b2<N, E1, 4>(d_jobs, njobs, masks, st); break;
+      default: rc = launch_b2<N, E1, 2>(d_jobs, njobs, masks, st); break;
     }
   }
   if (rc) return rc;

@@ -1,10 +1,15 @@
 // Served form: the GB300 counterpart of ReconstructionRunner
 // (LM/ReconstructionRunner.java:140-593, 599-748, 753-829).
 //
-// * Admission: a stack is admitted into one of a fixed set of slots (pinned host staging
-//   + device raw/output buffers). The slot count is bounded by max_inflight and by the
-//   HBM budget; a full server returns FSIM_EBUSY instead of dropping frames silently
-//   (the reference counts misses when its queue is full, :140-150).
+// * Admission: a stack is admitted into a slot (pinned host staging + device raw/output
+//   buffers) of its channel's size class, so that a 512^2 stack does not hold a 1024^2
+//   slot. At open the slots are sized from the free HBM (cudaMemGetInfo, less a headroom
+//   for other users of the device) and hbm_budget_bytes, at most max_inflight per class;
+//   the classes take the memory in equal shares of bytes (a class of small stacks gets
+//   more slots than one of large stacks). After every refit the free HBM is read again and
+//   classes below max_inflight grow. A class without a free slot returns FSIM_EBUSY
+//   instead of dropping frames silently (the reference counts misses when its queue is
+//   full, :140-150), while other classes still admit.
 // * Continuous batching: a worker thread takes every pending stack (up to max_batch) and
 //   launches one fused batch (H2D, reconstruction, D2H) on the next of `streams` CUDA
 //   streams; stacks arriving while batches run are taken by the next launch, so batches
@@ -125,6 +130,13 @@ struct fsim_server {
     bool refit_busy = false;
     void* d_refit_raw = nullptr;
     size_t raw_bytes = 0;
+    int cls = 0;  // slot class (stack and image size)
+  };
+  struct SlotClass {
+    size_t raw_bytes = 0, out_bytes = 0;
+    int n_channels = 0;
+    int total = 0;  // slots allocated (at most max_inflight)
+    std::vector<int> free;
   };
   enum { FREE = 0, FILLING, PENDING, RUNNING, DONE, COLLECTING };
   struct Slot {
@@ -136,6 +148,7 @@ struct fsim_server {
     bool cancelled = false;  // the client gave the ticket up; the slot frees itself when done
     uint64_t ticket = 0;
     int channel = 0;
+    int cls = 0;
     double t_submit = 0, t_done = 0;
   };
   struct Done {
@@ -145,8 +158,8 @@ struct fsim_server {
 
   fsim_serve_config cfg{};
   std::vector<Channel> ch;
-  std::vector<Slot> slots;
-  std::vector<int> free_list;
+  std::vector<Slot> slots;  // capacity max_inflight, reserved at open: slots never move
+  std::vector<SlotClass> cls;
   std::deque<int> pending;
   std::map<uint64_t, int> by_ticket;
   uint64_t next_ticket = 1;
@@ -185,7 +198,7 @@ static void CUDART_CB on_batch_done(void* arg) {
         sl.cancelled = false;
         s->by_ticket.erase(sl.ticket);
         sl.ticket = 0;
-        s->free_list.push_back(i);
+        s->cls[sl.cls].free.push_back(i);
       }
     }
   }
@@ -267,6 +280,8 @@ static void worker_loop(fsim_server* s) {
   }
 }
 
+static void grow_slots(fsim_server* s);
+
 static void refit_loop(fsim_server* s) {
   cudaSetDevice(ctx().device);
   for (;;) {
@@ -310,8 +325,11 @@ static void refit_loop(fsim_server* s) {
         s->refits++;
       }
     }
-    std::lock_guard<std::mutex> g(s->mu);
-    chn.refit_busy = false;
+    {
+      std::lock_guard<std::mutex> g(s->mu);
+      chn.refit_busy = false;
+    }
+    grow_slots(s);  // the free HBM may have changed since open
   }
 }
 
@@ -372,12 +390,87 @@ int fsim_serve_open(fsim_server** out, const fsim_serve_config* cfg, const fsim_
   return FSIM_OK;
 }
 
+}  // extern "C"
+
+// Device memory left to other users of the GPU when slots are sized from its free HBM.
+static size_t hbm_headroom(size_t total) { return std::max(total / 16, (size_t)1 << 30); }
+
+// One slot of class c: pinned host staging and device buffers; false when an allocation fails
+// (whatever was allocated is released).
+static bool alloc_slot(const fsim_server::SlotClass& c, fsim_server::Slot* sl) {
+  if (cudaMallocHost(&sl->h_raw, c.raw_bytes) != cudaSuccess) sl->h_raw = nullptr;
+  if (sl->h_raw && cudaMallocHost(&sl->h_out, c.out_bytes) != cudaSuccess) sl->h_out = nullptr;
+  if (sl->h_out && fsim::dev_alloc(&sl->d_raw, c.raw_bytes) != cudaSuccess) sl->d_raw = nullptr;
+  if (sl->d_raw && fsim::dev_alloc(&sl->d_out, c.out_bytes) != cudaSuccess) sl->d_out = nullptr;
+  if (sl->d_out) return true;
+  if (sl->d_raw) cudaFree(sl->d_raw);
+  if (sl->h_out) cudaFreeHost(sl->h_out);
+  if (sl->h_raw) cudaFreeHost(sl->h_raw);
+  sl->h_raw = sl->d_raw = nullptr;
+  sl->h_out = sl->d_out = nullptr;
+  cudaGetLastError();  // a failed allocation is not a sticky error
+  return false;
+}
+
+// Bytes of device memory slots may still take: the free HBM less the headroom, and within
+// hbm_budget_bytes (which also covers the batch workspaces) when that is set.
+static size_t slot_room(fsim_server* s, size_t slot_bytes_now) {
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 0;
+  const size_t head = hbm_headroom(total_b);
+  size_t room = free_b > head ? free_b - head : 0;
+  if (s->cfg.hbm_budget_bytes > 0) {
+    const size_t used = s->ws_bytes * s->streams.size() + slot_bytes_now;
+    room = std::min(room, s->cfg.hbm_budget_bytes > used ? s->cfg.hbm_budget_bytes - used : (size_t)0);
+  }
+  return room;
+}
+
+// Adds slots, one at a time to the class with the fewest bytes of slots among those below
+// max_inflight, while the room allows.
+// Called at open (no other thread yet) and after refits (slots only grow up to the reserved
+// capacity, so the indices and references of existing slots stay valid).
+static void grow_slots(fsim_server* s) {
+  for (;;) {
+    int c = -1;
+    size_t slot_bytes_now = 0;
+    {
+      std::lock_guard<std::mutex> g(s->mu);
+      if (s->slots.size() >= s->slots.capacity()) return;
+      int best = -1;
+      size_t best_bytes = 0;
+      for (size_t k = 0; k < s->cls.size(); k++) {
+        const auto& sc = s->cls[k];
+        const size_t bytes = (sc.raw_bytes + sc.out_bytes) * sc.total;
+        slot_bytes_now += bytes;
+        if (sc.total < s->cfg.max_inflight && (best < 0 || bytes < best_bytes)) {
+          best = (int)k;
+          best_bytes = bytes;
+        }
+      }
+      c = best;
+    }
+    if (c < 0) return;
+    const auto& sc = s->cls[c];  // the class list is fixed after open
+    if (slot_room(s, slot_bytes_now) < sc.raw_bytes + sc.out_bytes) return;
+    fsim_server::Slot sl;
+    if (!alloc_slot(sc, &sl)) return;
+    sl.cls = c;
+    std::lock_guard<std::mutex> g(s->mu);
+    s->slots.push_back(sl);
+    s->cls[c].total++;
+    s->cls[c].free.push_back((int)s->slots.size() - 1);
+  }
+}
+
+extern "C" {
+
 static int serve_setup(fsim_server* s, const fsim_serve_config* cfg, const fsim_sim_param* channels,
                        int n_channels) {
   int rc = FSIM_OK;
   s->cfg = *cfg;
   s->ch.resize(n_channels);
-  size_t max_raw = 0, max_out = 0, max_ws = 0;
+  size_t max_ws = 0;
   const int in_sz = cfg->input_type == FSIM_INPUT_U16 ? 2 : 4;
   for (int c = 0; c < n_channels; c++) {
     auto& chn = s->ch[c];
@@ -392,30 +485,24 @@ static int serve_setup(fsim_server* s, const fsim_serve_config* cfg, const fsim_
     const size_t N = channels[c].w;
     chn.raw_bytes = N * N * channels[c].nr_dirs * channels[c].nr_phases * in_sz;
     FSIM_CUDA(fsim::dev_alloc(&chn.d_refit_raw, chn.raw_bytes));
-    max_raw = std::max(max_raw, chn.raw_bytes);
-    max_out = std::max(max_out, 4 * N * N * sizeof(float));
+    const size_t out_bytes = 4 * N * N * sizeof(float);
+    // size classes: channels with the same stack and image size share slots
+    int k = 0;
+    while (k < (int)s->cls.size() && !(s->cls[k].raw_bytes == chn.raw_bytes && s->cls[k].out_bytes == out_bytes)) k++;
+    if (k == (int)s->cls.size()) {
+      s->cls.emplace_back();
+      s->cls[k].raw_bytes = chn.raw_bytes;
+      s->cls[k].out_bytes = out_bytes;
+    }
+    s->cls[k].n_channels++;
+    chn.cls = k;
     max_ws = std::max(max_ws, (plan_ws(chn.plans[0]) + 255) & ~(size_t)255);
   }
   s->ws_bytes = ((sizeof(JobDesc) * cfg->max_batch + 255) & ~(size_t)255) + max_ws * cfg->max_batch;
-  // admission bound: slots fit the HBM budget after the per-stream workspaces
-  size_t per_slot = max_raw + max_out;
-  size_t ws_total = s->ws_bytes * cfg->streams;
-  int nslots = cfg->max_inflight;
-  if (cfg->hbm_budget_bytes > 0) {
-    FSIM_REQUIRE(cfg->hbm_budget_bytes > ws_total + per_slot, FSIM_EOOM,
-                 "serve_open: HBM budget %zu below workspace %zu + one slot %zu", cfg->hbm_budget_bytes, ws_total,
-                 per_slot);
-    nslots = std::min<size_t>(nslots, (cfg->hbm_budget_bytes - ws_total) / per_slot);
-  }
-  s->slots.resize(nslots);
-  for (int i = 0; i < nslots; i++) {
-    auto& sl = s->slots[i];
-    FSIM_CUDA(cudaMallocHost(&sl.h_raw, max_raw));
-    FSIM_CUDA(cudaMallocHost(&sl.h_out, max_out));
-    FSIM_CUDA(fsim::dev_alloc(&sl.d_raw, max_raw));
-    FSIM_CUDA(fsim::dev_alloc(&sl.d_out, max_out));
-    s->free_list.push_back(nslots - 1 - i);
-  }
+  if (cfg->hbm_budget_bytes > 0)
+    FSIM_REQUIRE(cfg->hbm_budget_bytes > s->ws_bytes * cfg->streams, FSIM_EOOM,
+                 "serve_open: HBM budget %zu below the batch workspaces %zu", cfg->hbm_budget_bytes,
+                 s->ws_bytes * cfg->streams);
   s->streams.resize(cfg->streams);
   s->ws.resize(cfg->streams);
   for (int k = 0; k < cfg->streams; k++) {
@@ -423,6 +510,12 @@ static int serve_setup(fsim_server* s, const fsim_serve_config* cfg, const fsim_
     FSIM_CUDA(fsim::dev_alloc(&s->ws[k], s->ws_bytes));
   }
   FSIM_CUDA(cudaStreamCreateWithFlags(&s->refit_stream, cudaStreamNonBlocking));
+  s->slots.reserve((size_t)cfg->max_inflight * s->cls.size());
+  grow_slots(s);
+  for (size_t k = 0; k < s->cls.size(); k++)
+    FSIM_REQUIRE(s->cls[k].total > 0, FSIM_EOOM,
+                 "serve_open: no device memory for a slot of %zu + %zu bytes (class %zu) within the free HBM "
+                 "and the budget", s->cls[k].raw_bytes, s->cls[k].out_bytes, k);
   FSIM_CUDA(cudaDeviceSynchronize());
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
   s->copier.reset(new CopyPool((int)std::min(7u, std::max(1u, hw / 4))));
@@ -439,13 +532,15 @@ int fsim_serve_submit(fsim_server* s, int channel, const void* raw_host, size_t 
   int i;
   {
     std::lock_guard<std::mutex> g(s->mu);
-    if (s->free_list.empty()) {
+    auto& fl = s->cls[s->ch[channel].cls].free;
+    if (fl.empty()) {
       s->rejected++;
-      set_error("serve_submit: no free slot (%zu in flight)", s->slots.size());
+      set_error("serve_submit: no free slot for channel %d (all %d slots of its %d x %d class in flight)", channel,
+                s->cls[s->ch[channel].cls].total, s->ch[channel].prm.w, s->ch[channel].prm.w);
       return FSIM_EBUSY;
     }
-    i = s->free_list.back();
-    s->free_list.pop_back();
+    i = fl.back();
+    fl.pop_back();
     auto& sl = s->slots[i];
     sl.state = fsim_server::FILLING;
     sl.channel = channel;
@@ -494,7 +589,7 @@ int fsim_serve_wait(fsim_server* s, uint64_t ticket, float* out_host, int timeou
   lk.lock();
   sl.state = fsim_server::FREE;
   sl.ticket = 0;
-  s->free_list.push_back(i);
+  s->cls[sl.cls].free.push_back(i);
   return FSIM_OK;
 }
 
@@ -514,12 +609,12 @@ int fsim_serve_cancel(fsim_server* s, uint64_t ticket) {
     sl.state = fsim_server::FREE;
     sl.ticket = 0;
     s->by_ticket.erase(it);
-    s->free_list.push_back(i);
+    s->cls[sl.cls].free.push_back(i);
   } else if (sl.state == fsim_server::DONE) {
     sl.state = fsim_server::FREE;
     sl.ticket = 0;
     s->by_ticket.erase(it);
-    s->free_list.push_back(i);
+    s->cls[sl.cls].free.push_back(i);
   } else {
     sl.cancelled = true;  // on the GPU: the completion callback frees the slot
   }
@@ -549,6 +644,15 @@ int fsim_serve_stats_get(fsim_server* s, fsim_serve_stats* out) {
   }
   out->wall_s = (s->t_last - s->t_first) / 1000.0;
   out->recon_per_s = out->wall_s > 0 ? s->completed / out->wall_s : 0;
+  return FSIM_OK;
+}
+
+int fsim_serve_capacity(fsim_server* s, int channel, int* slots, int* free_slots) {
+  FSIM_REQUIRE(s && channel >= 0 && channel < (int)s->ch.size(), FSIM_EINVAL, "serve_capacity: bad arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  const auto& sc = s->cls[s->ch[channel].cls];
+  if (slots) *slots = sc.total;
+  if (free_slots) *free_slots = (int)sc.free.size();
   return FSIM_OK;
 }
 

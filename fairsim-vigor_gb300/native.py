@@ -266,6 +266,7 @@ _SIGS = {
     "fsim_serve_wait": (I32, [VP, C.c_uint64, VP, I32, C.POINTER(F64)]),
     "fsim_serve_stats_get": (I32, [VP, VP]),
     "fsim_serve_params": (I32, [VP, I32, VP]),
+    "fsim_serve_capacity": (I32, [VP, I32, C.POINTER(I32), C.POINTER(I32)]),
     "fsim_serve_close": (I32, [VP]),
     "fsim_rl_deconvolve": (I32, [VP, VP, I32, I32]),
     "fsim_auto_correlation": (I32, [VP, F64, F64, C.POINTER(F64), C.POINTER(F64)]),

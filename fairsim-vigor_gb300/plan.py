@@ -223,6 +223,12 @@ class Server:
         N.check(N.lib().fsim_serve_stats_get(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in N.ServeStats._fields_}
 
+    def capacity(self, ch: int) -> dict:
+        """Slots of the channel's size class: allocated, and free now."""
+        tot, free = C.c_int(), C.c_int()
+        N.check(N.lib().fsim_serve_capacity(self._h, int(ch), C.byref(tot), C.byref(free)))
+        return {"slots": tot.value, "free": free.value}
+
     def channel_params(self, ch: int) -> dict:
         c = N.SimParamC()
         N.check(N.lib().fsim_serve_params(self._h, int(ch), C.byref(c)))

@@ -301,12 +301,13 @@ int fsim_debug_fail_alloc(int nth);
 typedef struct fsim_server fsim_server;
 typedef struct fsim_serve_config {
   int32_t max_batch;        /* stacks per launch */
-  int32_t max_inflight;     /* admitted stacks not yet returned (slots) */
+  int32_t max_inflight;     /* admitted stacks not yet returned, per size class (slots) */
   int32_t streams;          /* concurrent batch streams */
   int32_t refit_every;      /* re-fit a channel's parameters every N stacks (0 = never) */
   int32_t input_type;       /* FSIM_INPUT_U16 or FSIM_INPUT_F32 */
   int32_t fade_px;
-  size_t hbm_budget_bytes;  /* admission bound on device memory for in-flight stacks */
+  size_t hbm_budget_bytes;  /* 0, or a bound on the device memory of the batch workspaces and
+                               the slots together */
 } fsim_serve_config;
 typedef struct fsim_serve_stats {
   uint64_t submitted, completed, rejected, refits;
@@ -315,12 +316,19 @@ typedef struct fsim_serve_stats {
   double wall_s;
   uint64_t cancelled;
 } fsim_serve_stats;
+/* Admission by free HBM: channels of one stack and image size share a class of slots
+ * (pinned staging + device buffers of that size). At open, slots are allocated, one at a
+ * time to the class with the fewest bytes of slots, up to max_inflight per class, while the
+ * free device memory (cudaMemGetInfo, less a headroom of max(1/16 of the device, 1 GiB) for
+ * other users) and hbm_budget_bytes allow; after every refit the free memory is read again
+ * and classes below max_inflight grow. FSIM_EOOM when some class gets no slot at all. */
 int fsim_serve_open(fsim_server** out, const fsim_serve_config* cfg, const fsim_sim_param* channels,
                     int n_channels);
-/* Copies the raw stack (host, raw_bytes long) into a staging slot. FSIM_EBUSY when no slot
- * is free (the reference's live queue drops and counts the frame instead,
- * ReconstructionRunner.java:140-150); FSIM_EINVAL when raw_bytes is not the channel's
- * nr_dirs*nr_phases*w*w*sample size (the reference throws from Vec.failSize). */
+/* Copies the raw stack (host, raw_bytes long) into a staging slot of the channel's class.
+ * FSIM_EBUSY when that class has no free slot (the reference's live queue drops and counts
+ * the frame instead, ReconstructionRunner.java:140-150); other classes keep admitting.
+ * FSIM_EINVAL when raw_bytes is not the channel's nr_dirs*nr_phases*w*w*sample size (the
+ * reference throws from Vec.failSize). */
 int fsim_serve_submit(fsim_server* s, int channel, const void* raw_host, size_t raw_bytes, uint64_t* ticket);
 /* Gives a ticket up: a queued stack is dropped, a finished one released, and one on the GPU
  * releases its slot when its batch completes. Waiting on it afterwards gives
@@ -330,6 +338,9 @@ int fsim_serve_cancel(fsim_server* s, uint64_t ticket);
 int fsim_serve_wait(fsim_server* s, uint64_t ticket, float* out_host, int timeout_ms, double* latency_ms);
 int fsim_serve_stats_get(fsim_server* s, fsim_serve_stats* out);
 int fsim_serve_params(fsim_server* s, int channel, fsim_sim_param* out);
+/* Slots of the channel's size class: allocated so far, and free now (no reference
+ * counterpart). */
+int fsim_serve_capacity(fsim_server* s, int channel, int* slots, int* free_slots);
 int fsim_serve_close(fsim_server* s);
 
 /* ---- live stream ingest (host only, no device work) -------------------------------------

@@ -97,8 +97,8 @@ def test_measured_otf_roundtrip_and_fused_refusal(fs, tmp_path):
     sp = fs.SimParam.create(2, 3, 3, 256, 0.08, otf)
     c = fs.native.to_c_param(sp)  # the record carries the bands to the library
     assert (c.otf_bands, c.otf_samples, c.otf_cycles) == (2, 4, 0.0125)
-    with pytest.raises(ValueError):  # the fused plans take estimated OTFs only
-        fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    with pytest.raises(ValueError):  # live plans take estimated OTFs only (checked before any device work)
+        fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE, input_type=fs.native.INPUT_U16, fade_px=10)
 
 
 @pytest.mark.skipif(not REF or not os.path.isdir(REF), reason="FSIM_REFERENCE_ROOT unset or not a directory")

@@ -77,6 +77,37 @@ def test_offline_fused_clip_scale_vs_oracle(fs, oracle, torch_cuda, clip):
     assert rel_l2(d_out[1].cpu().numpy(), oracle.recon_raw(sp, raw, fade=10)) < 1e-4
 
 
+# (with attenuation on, the table must reach the cutoff: the reference indexes beyond its
+# arrays otherwise, and the oracle stops there)
+@pytest.mark.parametrize("n,samples,att", [(256, 300, False), (512, 300, True), (384, 200, False)])
+def test_offline_fused_measured_otf_vs_oracle(fs, oracle, torch_cuda, n, samples, att):
+    """Measured two-band complex OTFs (OtfProvider.loadFromConfig with band data) on the fused
+    offline plans: complex masks of each component's band and the band-aware Wiener
+    denominator, within 1e-4 of the oracle; in one batch with an estimated-OTF plan of the
+    same size, each keeps its own result."""
+    from test_gpu_vector_api import measured_otf
+    torch = torch_cuda
+    raw, truth, sp = make(fs, n, seed=23 + n)
+    sp.setOtf(measured_otf(fs, samples=samples))
+    if att:
+        sp.otf().setAttenuation(0.97, 1.1)
+        sp.otf().switchAttenuation(True)
+    plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    got = plan.reconstruct_host(raw)
+    exp = oracle.recon_raw(sp, raw, fade=10)
+    assert rel_l2(got, exp) < 1e-4
+    raw2, truth2, sp2 = make(fs, n, seed=24 + n)
+    est = fs.plan.ReconPlan(sp2, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    d_raw = [torch.from_numpy(r).cuda() for r in (raw, raw2)]
+    d_out = [torch.empty((2 * n, 2 * n), dtype=torch.float32, device="cuda") for _ in range(2)]
+    ws = torch.empty(fs.plan.batch_workspace_bytes([plan, est]), dtype=torch.uint8, device="cuda")
+    fs.plan.recon_batch([(plan, d_raw[0].data_ptr(), d_out[0].data_ptr()), (est, d_raw[1].data_ptr(), d_out[1].data_ptr())],
+                        ws.data_ptr(), ws.numel())
+    torch.cuda.synchronize()
+    assert np.array_equal(d_out[0].cpu().numpy(), got)
+    assert np.array_equal(d_out[1].cpu().numpy(), est.reconstruct_host(raw2))
+
+
 @pytest.mark.parametrize("variant", ["bgr_att", "five_phases", "three_bands"])
 def test_offline_fused_variants(fs, oracle, variant):
     n = 256

@@ -77,6 +77,47 @@ def test_admission_refuses_when_slots_are_full(fs):
     srv.close()
 
 
+def test_admission_by_size_class(fs):
+    """Slots are sized per channel size, max_inflight of them per class: a full 1024^2 class
+    refuses with FSIM_EBUSY while 512^2 stacks are still admitted, and every admitted stack
+    reconstructs as it does alone."""
+    raw5, sp5 = channel(fs, 512, 31)
+    raw10, sp10 = channel(fs, 1024, 32)
+    srv = fs.plan.Server([sp5, sp10], max_batch=2, max_inflight=2, streams=2, refit_every=0)
+    assert srv.capacity(0) == {"slots": 2, "free": 2} and srv.capacity(1) == {"slots": 2, "free": 2}
+    t10 = [srv.try_submit(1, raw10) for _ in range(2)]
+    assert all(t is not None for t in t10)
+    assert srv.try_submit(1, raw10) is None  # every 1024^2 slot is taken until a result is collected
+    t5 = [srv.try_submit(0, raw5) for _ in range(2)]
+    assert all(t is not None for t in t5)  # the 512^2 class still admits
+    assert srv.try_submit(0, raw5) is None
+    alone = {}
+    for c, (raw, sp) in enumerate(((raw5, sp5), (raw10, sp10))):
+        plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE, input_type=fs.native.INPUT_U16, fade_px=10)
+        alone[c] = plan.reconstruct_host(raw)
+    for c, tickets in ((1, t10), (0, t5)):
+        n = (sp5, sp10)[c].w
+        for tk in tickets:
+            out = np.empty((2 * n, 2 * n), np.float32)
+            srv.wait(tk, out)
+            assert np.array_equal(out, alone[c])
+    assert srv.capacity(0)["free"] == 2 and srv.capacity(1)["free"] == 2
+    assert srv.stats()["rejected"] == 2
+    srv.close()
+
+
+def test_slots_follow_the_hbm_budget(fs):
+    """Within a device-memory budget the classes take equal shares of bytes: the class of
+    small stacks gets more slots than the class of large ones."""
+    raw5, sp5 = channel(fs, 256, 33)
+    raw10, sp10 = channel(fs, 1024, 34)
+    srv = fs.plan.Server([sp5, sp10], max_batch=1, max_inflight=64, streams=1, refit_every=0,
+                         hbm_budget_bytes=1 << 30)
+    small, large = srv.capacity(0)["slots"], srv.capacity(1)["slots"]
+    assert 1 <= large < small <= 64
+    srv.close()
+
+
 def test_refit_on_device_matches_oracle(fs, oracle):
     raw, sp = channel(fs, 512, 11)
     # start from deliberately wrong parameters; the refit must recover them from the stack

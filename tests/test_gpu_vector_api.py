@@ -324,8 +324,8 @@ def test_run_reconstruction_rl_styles_vs_oracle(fs, oracle, V, style):
     out = fs.algorithm.SimAlgorithm.runReconstruction(sp, inFFT, False, 0).vectorData()
     assert rel_l2(out, exp32) < 1e-4
     assert rel_l2(out, exp64) < 1e-4
-    with pytest.raises(ValueError):  # the fused plans apply the Wiener filter only
-        fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    with pytest.raises(ValueError):  # live plans take estimated OTFs only
+        fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE, input_type=fs.native.INPUT_U16, fade_px=10)
 
 
 def measured_otf(fs, samples=300, bands=2, spacing=256, na=1.4, lam=525.0, a=0.3):
