@@ -75,7 +75,7 @@ __global__ void k_common_region(float2* __restrict__ b0, float2* __restrict__ b1
       v1 = make_float2(__fmul_rn(v1.x, r), __fmul_rn(v1.y, r));
     }
   }
-  const double mx = sqrt(kx * kx + ky * ky);
+  const double mx = __dsqrt_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)));  // unfused, as Java
   auto cut = [&](int xx, int yy) {
     long long a = (xx < w / 2) ? (long long)xx * xx : (long long)(xx - w) * (xx - w);
     long long b = (yy < h / 2) ? (long long)yy * yy : (long long)(yy - h) * (yy - h);

@@ -13,16 +13,22 @@
 
 namespace fsim {
 
+// Lines up to 512: 8 elements per thread in 64 registers (32 resident warps per SM; 0.115 ->
+// 0.111 ms for 64 x 512^2 on GB300); longer lines keep 16 (8 measured slower at 1024: 0.126
+// -> 0.133 ms for 16 x 1024^2); 3*2^k lengths 12.
 template <int L>
 struct LinePlan {
-  static constexpr int E = (L % 3 == 0) ? 12 : 16;
+  static constexpr int E = (L % 3 == 0) ? 12 : (L <= 512 ? (L >= 64 ? 8 : 4) : 16);
   static constexpr int T = L / E;
   static constexpr int G = T >= 256 ? 1 : 256 / T;  // rows per block in the row pass
-  static constexpr int C = L <= 1024 ? 8 : (L <= 3072 ? 4 : 2);  // columns per block, column pass
+  static constexpr int C = (E <= 8) ? (T >= 128 ? 4 : 8) : (L <= 1024 ? 8 : (L <= 3072 ? 4 : 2));  // column pass
+  static constexpr int MINB_R = (E <= 8) ? 4 : 1;  // blocks per SM the register budgets allow
+  static constexpr int MINB_C = (E <= 8) ? 65536 / (C * T * 64) : 1;
 };
 
 template <int L, bool INV>
-__global__ void __launch_bounds__(256) k_fft_rows(float2* __restrict__ data, int nrows, size_t item_stride, float scale) {
+__global__ void __launch_bounds__(LinePlan<L>::G* LinePlan<L>::T, LinePlan<L>::MINB_R)
+    k_fft_rows(float2* __restrict__ data, int nrows, size_t item_stride, float scale) {
   using P = LinePlan<L>;
   constexpr int T = P::T, E = P::E, G = P::G, SL = smem_line_elems(L, 1);
   extern __shared__ float2 sm[];
@@ -41,7 +47,8 @@ __global__ void __launch_bounds__(256) k_fft_rows(float2* __restrict__ data, int
 }
 
 template <int L, bool INV>
-__global__ void k_fft_cols(float2* __restrict__ data, int ncols, size_t item_stride, float scale) {
+__global__ void __launch_bounds__(LinePlan<L>::C* LinePlan<L>::T, LinePlan<L>::MINB_C)
+    k_fft_cols(float2* __restrict__ data, int ncols, size_t item_stride, float scale) {
   using P = LinePlan<L>;
   constexpr int T = P::T, E = P::E, C = P::C;
   extern __shared__ float2 s[];

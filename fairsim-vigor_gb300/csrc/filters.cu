@@ -57,6 +57,13 @@ void build_otf_table(const fsim_sim_param* p, OtfTable* t) {
     t->only_att[v] = (float)(1 - p->att_strength * std::exp(-(std::pow(dist, 2)) / (2 * std::pow(p->att_fwhm / 2.355, 2))));
     t->vals_att[v] = t->vals[v] * t->only_att[v];
   }
+  auto split = [](double v, float* o) {
+    o[0] = (float)v;
+    o[1] = (float)(v - (double)o[0]);
+  };
+  split(t->vec_cpm, t->ff_cpm);
+  split(t->vec_cpm / t->cycles_per_sample, t->ff_pos);
+  split(t->cutoff, t->ff_cut);
 }
 
 // ---- kernels ------------------------------------------------------------------------
@@ -111,8 +118,9 @@ __global__ void k_att_vector(float* __restrict__ v, int w, int h, double vec_cpm
   if (x >= w) return;
   double rad = d_hypot_java(__dsub_rn((double)freq_x(x, w), kx), __dsub_rn((double)freq_y(y, h), ky));
   double dist = __dmul_rn(rad, vec_cpm);
-  double s = fwhm / 2.355;
-  v[(size_t)y * w + x] = (float)(1 - str * exp(-(dist * dist) / (2 * (s * s))));
+  const double s = fwhm / 2.355;  // Java's separate roundings (no FMA contraction)
+  const double g = exp(-__dmul_rn(dist, dist) / __dmul_rn(2.0, __dmul_rn(s, s)));
+  v[(size_t)y * w + x] = (float)__dsub_rn(1.0, __dmul_rn(str, g));
 }
 
 __global__ void k_mask_otf(float2* __restrict__ v, int w, int h, double vec_cpm, double cutoff, double kx, double ky) {
@@ -206,6 +214,27 @@ int upload_otf_table(const fsim_sim_param* p, OtfTable** dev, cudaStream_t st) {
     for (int i = 0; i < 7; i++) key[i] = measured ? std::nan("") : k[i];
   }
   *dev = buf;
+  return FSIM_OK;
+}
+
+FShiftSet fshift_set(const ShiftSet& s) {
+  FShiftSet f{};
+  for (int d = 0; d < s.n_dirs && d < FSIM_MAX_DIRS; d++)
+    for (int b = 0; b < s.n_bands && b < FSIM_MAX_BANDS; b++) f.k[d][b] = fshift_host(s.px[d] * b, s.py[d] * b);
+  return f;
+}
+
+__global__ void k_apo_octant(float* __restrict__ q, int n, double vec_cpm, double cutoff_abs, double bend) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (j > i) return;
+  const double frac = __dmul_rn(d_hypot_java((double)i, (double)j), vec_cpm) / cutoff_abs;
+  const double io = ideal_otf_dev(frac);
+  q[(size_t)i * (n + 1) + j] = (float)(bend == 1.0 ? io : pow(io, bend));  // Math.pow(x, 1.0) is x
+}
+
+int apo_octant_device(float* q, int n, double vec_cpm, double cutoff_abs, double bend, cudaStream_t st) {
+  k_apo_octant<<<dim3(div_up(n + 1, 128), n + 1), 128, 0, st>>>(q, n, vec_cpm, cutoff_abs, bend);
+  FSIM_CHECK_LAUNCH();
   return FSIM_OK;
 }
 

@@ -13,6 +13,16 @@ struct ShiftSet {  // per-direction band-1 shifts
   double px[FSIM_MAX_DIRS], py[FSIM_MAX_DIRS];
 };
 ShiftSet shift_set(const fsim_sim_param* p);
+// the band shifts (px[d] * b, py[d] * b) of a ShiftSet as float hi + lo (otf_pos_ff)
+struct FShiftSet {
+  FShift k[FSIM_MAX_DIRS][FSIM_MAX_BANDS];
+};
+FShiftSet fshift_set(const ShiftSet& s);
+// The apodization (float)pow(valIdealOTF(hypot(x, y) * vec_cpm / cutoff_abs), bend) of
+// OtfProvider.writeApoVector depends on |x| and |y| only, and symmetrically: it is
+// evaluated in double once per point 0 <= j <= i <= n of one octant into q[i * (n + 1) + j]
+// (bit-equal to the per-pixel evaluation; callers read q[max * (n + 1) + min]).
+int apo_octant_device(float* q, int n, double vec_cpm, double cutoff_abs, double bend, cudaStream_t st);
 
 constexpr int SEP_MAX_OUT = 2 * FSIM_MAX_BANDS - 1;
 struct SepArgs {

@@ -257,34 +257,28 @@ __global__ void __launch_bounds__(LCfg<N>::CD* LCfg<N>::TW) k_live_d(const JobDe
 __global__ void k_live_otf(float* __restrict__ v, int N, const OtfTable* __restrict__ t, int att) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   if (x >= N) return;
-  float o = 0.f;
-  if (!otf_at(*t, (double)freq_x(x, N), (double)freq_y(y, N), 0, 0, att != 0, &o)) o = 0.f;
-  v[(size_t)y * N + x] = o;
+  float2 o = make_float2(0.f, 0.f);
+  if (!otf_at_fast(*t, 0, freq_x(x, N), freq_y(y, N), FShift{0.f, 0.f, 0.f, 0.f}, 0, 0, att != 0, &o)) o.x = 0.f;
+  v[(size_t)y * N + x] = o.x;
 }
-__global__ void k_live_wa(float* __restrict__ wa, int W, const OtfTable* __restrict__ t, ShiftSet shifts, int use_att,
-                          float wp, double apo_cut_abs, double bend) {
+// getDenominator x writeApoVector (the apodization from its octant table, W/2 + 1 per row)
+__global__ void k_live_wa(float* __restrict__ wa, int W, const OtfTable* __restrict__ t, ShiftSet shifts, FShiftSet fsh,
+                          int use_att, float wp, const float* __restrict__ apo) {
   const int X = blockIdx.x * blockDim.x + threadIdx.x, Y = blockIdx.y;
   if (X >= W) return;
-  const double xh = freq_x(X, W), yh = freq_y(Y, W);
-  const double cpm = t->vec_cpm;
+  const int xh = freq_x(X, W), yh = freq_y(Y, W);
   float acc = 0.f;
   for (int d = 0; d < shifts.n_dirs; d++)
     for (int b = 0; b < shifts.n_bands; b++) {
       const double kx = shifts.px[d] * b, ky = shifts.py[d] * b;
-      double r1 = __dmul_rn(d_hypot_java(__dsub_rn(xh, kx), __dsub_rn(yh, ky)), cpm);
-      double r2 = __dmul_rn(d_hypot_java(__dadd_rn(xh, kx), __dadd_rn(yh, ky)), cpm);
-      float o1 = otf_val(*t, r1, false), o2 = otf_val(*t, r2, false);
-      float v1 = __fmul_rn(o1, o1), v2 = __fmul_rn(o2, o2);
-      if (use_att) {
-        v1 = __fmul_rn(v1, att_val(*t, r1));
-        v2 = __fmul_rn(v2, att_val(*t, r2));
-      }
+      const FShift k = fsh.k[d][b];
+      const float v1 = wiener_term(*t, 0, xh, yh, k, kx, ky, use_att != 0);
+      const float v2 = wiener_term(*t, 0, xh, yh, fshift_neg(k), -kx, -ky, use_att != 0);
       acc = __fadd_rn(__fadd_rn(acc, v1), v2);
     }
   const float den = __fdiv_rn(1.f, __fadd_rn(acc, wp));
-  double frac = __dmul_rn(d_hypot_java(xh, yh), cpm) / apo_cut_abs;
-  const float apo = (float)pow(ideal_otf_dev(frac), bend);
-  wa[(size_t)Y * W + X] = __fmul_rn(den, apo);
+  const int ax = abs(xh), ay = abs(yh);
+  wa[(size_t)Y * W + X] = __fmul_rn(den, __ldg(apo + (size_t)max(ax, ay) * (W / 2 + 1) + min(ax, ay)));
 }
 
 int Plan::build_live(cudaStream_t st) {
@@ -326,7 +320,8 @@ int Plan::build_live(cudaStream_t st) {
   size_t o_damp = o_otf + al(sizeof(OtfTable));
   size_t o_mask = o_damp + al((size_t)N * N * sizeof(float));
   size_t o_wa = o_mask + al((size_t)N * N * sizeof(float));
-  size_t total = o_wa + al((size_t)W * W * sizeof(float));
+  size_t o_apo = o_wa + al((size_t)W * W * sizeof(float));
+  size_t total = o_apo + al((size_t)(N + 1) * (N + 1) * sizeof(float));
   if (total > dev_bytes) {
     if (dev) cudaFree(dev);
     dev = nullptr;
@@ -353,8 +348,14 @@ int Plan::build_live(cudaStream_t st) {
   FSIM_CUDA(cudaStreamSynchronize(st));
   k_live_otf<<<dim3(div_up(N, 128), N), 128, 0, st>>>(d_masks, N, d_otf, prm.use_attenuation);
   // setupFilters: getDenominator(wienParam) and writeApoVector(apo, 1, 2)
-  k_live_wa<<<dim3(div_up(W, 128), W), 128, 0, st>>>(d_wa, W, d_otf, shift_set(&prm), prm.use_attenuation,
-                                                     (float)(prm.wiener * prm.wiener), ht.cutoff * 2.0, 1.0);
+  {
+    float* d_apo = (float*)(b + o_apo);
+    int rc = apo_octant_device(d_apo, N, ht.vec_cpm, ht.cutoff * 2.0, 1.0, st);
+    if (rc) return rc;
+    const ShiftSet sh = shift_set(&prm);
+    k_live_wa<<<dim3(div_up(W, 128), W), 128, 0, st>>>(d_wa, W, d_otf, sh, fshift_set(sh), prm.use_attenuation,
+                                                       (float)(prm.wiener * prm.wiener), d_apo);
+  }
   FSIM_CHECK_LAUNCH();
   FSIM_CUDA(cudaStreamSynchronize(st));
   filter_bytes = total;
@@ -377,6 +378,7 @@ void Plan::fill_job_live(JobDesc& j, const void* raw, float* out, float* wf, cha
   j.nA = prm.nr_dirs;
   j.nP = prm.nr_phases;
   j.nC = nC;
+  j.status = ctx().status;
   j.nWin = 0;
   j.bgr = 0.f;
   j.damp = d_damp;

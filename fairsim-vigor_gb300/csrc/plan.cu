@@ -288,6 +288,26 @@ int fsim_plan_set_clip_scale(fsim_plan* plan, int clip_scale) {
   return FSIM_OK;
 }
 
+int fsim_plan_filter_table(const fsim_plan* plan, float* host_out, size_t n_floats, int* ncols) {
+  FSIM_REQUIRE(plan && host_out, FSIM_EINVAL, "filter_table: null plan or output");
+  const int N = plan->prm.w, W = 2 * N, nc = plan->path == FSIM_PATH_LIVE ? W : N + 1;
+  FSIM_REQUIRE(n_floats >= (size_t)W * nc, FSIM_EINVAL, "filter_table: %zu floats given, %zu needed", n_floats,
+               (size_t)W * nc);
+  NEED_INIT();
+  FSIM_CUDA(cudaDeviceSynchronize());
+  if (plan->path == FSIM_PATH_LIVE) {
+    FSIM_CUDA(cudaMemcpy(host_out, plan->d_wa, (size_t)W * W * sizeof(float), cudaMemcpyDeviceToHost));
+  } else {
+    // quad layout [X/4][Y][X%4] over the columns X < N + 4
+    std::vector<float> q((size_t)(N + 4) * W);
+    FSIM_CUDA(cudaMemcpy(q.data(), plan->d_wa, q.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int Y = 0; Y < W; Y++)
+      for (int X = 0; X < nc; X++) host_out[(size_t)Y * nc + X] = q[((size_t)(X >> 2) * W + Y) * 4 + (X & 3)];
+  }
+  if (ncols) *ncols = nc;
+  return FSIM_OK;
+}
+
 int fsim_plan_info(const fsim_plan* plan, int* w, int* path, int* input_type) {
   FSIM_REQUIRE(plan, FSIM_EINVAL, "null plan");
   if (w) *w = plan->prm.w;

@@ -17,8 +17,9 @@
 //      iFFT_W along y;
 //   C  (rows,    per output row): iFFT_W along x, real part, 1/W^2.
 // Shift phases use exact per-axis ramp tables; OTF masks and the Wiener*apo filter are
-// resident per plan, built with the reference's double-precision radius and floor-indexed
-// OTF lookup.
+// resident per plan, built with the reference's floor-indexed OTF lookup (table positions in
+// float-float arithmetic, the reference's double-precision radius at their boundaries) and
+// its double-precision apodization (one evaluation per octant point).
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -42,61 +43,40 @@ std::vector<float> fade_vector(int w, int h, int px);
 // ---- plan build kernels -------------------------------------------------------------------------
 // conj(OTF(r - k)) mask of one component over its window, quad layout [xl/4][yl][xl%4]:
 // real values for estimated OTFs; complex values (float2) of OTF band `band` for measured
-// ones (OtfProvider.applyOtf(vec, band, kx, ky), S/SimAlgorithm.java:397-403)
-__global__ void k_build_mask(float* __restrict__ mask, int W, int nWin, int Xs, int Ys, double kx, double ky,
+// ones (OtfProvider.applyOtf(vec, band, kx, ky), S/SimAlgorithm.java:397-403). Table
+// positions in float-float, the reference's double-precision lookup at their boundaries.
+__global__ void k_build_mask(float* __restrict__ mask, int W, int nWin, int Xs, int Ys, double kx, double ky, FShift kf,
                              const OtfTable* __restrict__ t, int att, int band) {
   const int xl = blockIdx.x * blockDim.x + threadIdx.x, yl = blockIdx.y;
   if (xl >= nWin) return;
   int X = (Xs + xl) % W, Y = (Ys + yl) % W;
   const size_t i = ((size_t)(xl >> 2) * nWin + yl) * 4 + (xl & 3);
-  if (t->measured) {
-    float2 c = make_float2(0.f, 0.f);
-    if (!otf_at_c(*t, band, (double)freq_x(X, W), (double)freq_y(Y, W), kx, ky, att != 0, &c)) c = make_float2(0.f, 0.f);
-    reinterpret_cast<float2*>(mask)[i] = make_float2(c.x, -c.y);
-    return;
-  }
-  float v = 0.f;
-  if (!otf_at(*t, (double)freq_x(X, W), (double)freq_y(Y, W), kx, ky, att != 0, &v)) v = 0.f;
-  mask[i] = v;
+  float2 c = make_float2(0.f, 0.f);
+  if (!otf_at_fast(*t, band, freq_x(X, W), freq_y(Y, W), kf, kx, ky, att != 0, &c)) c = make_float2(0.f, 0.f);
+  if (t->measured) reinterpret_cast<float2*>(mask)[i] = make_float2(c.x, -c.y);
+  else mask[i] = c.x;
 }
 
-// 1/(sum |OTF|^2 + w^2) * apo, quad layout [X/4][Y][X%4]
-__global__ void k_build_wa(float* __restrict__ wa, int W, const OtfTable* __restrict__ t, ShiftSet shifts, int use_att,
-                           float wp, double apo_cut_abs, double bend) {
+// 1/(sum |OTF|^2 + w^2) * apo, quad layout [X/4][Y][X%4], for the columns X < ncols; the
+// apodization from its octant table apo (W/2 + 1 entries per row)
+__global__ void k_build_wa(float* __restrict__ wa, int ncols, int W, const OtfTable* __restrict__ t, ShiftSet shifts,
+                           FShiftSet fsh, int use_att, float wp, const float* __restrict__ apo) {
   const int X = blockIdx.x * blockDim.x + threadIdx.x, Y = blockIdx.y;
-  if (X >= W) return;
-  const double xh = freq_x(X, W), yh = freq_y(Y, W);
-  const double cpm = t->vec_cpm;
+  if (X >= ncols) return;
+  const int xh = freq_x(X, W), yh = freq_y(Y, W);
   float acc = 0.f;
   for (int d = 0; d < shifts.n_dirs; d++)
     for (int b = 0; b < shifts.n_bands; b++) {
       const double kx = shifts.px[d] * b, ky = shifts.py[d] * b;
-      double r1 = __dmul_rn(d_hypot_java(__dsub_rn(xh, kx), __dsub_rn(yh, ky)), cpm);
-      double r2 = __dmul_rn(d_hypot_java(__dadd_rn(xh, kx), __dadd_rn(yh, ky)), cpm);
-      float v1, v2;
-      if (t->measured) {  // band b's complex values, |OTF|^2 as Cplx.Float.absSq (WienerFilter.java)
-        v1 = abs_sq(otf_val_c(*t, b, r1, false));
-        v2 = abs_sq(otf_val_c(*t, b, r2, false));
-        if (use_att) {
-          v1 = __fmul_rn(v1, att_val_b(*t, b, r1));
-          v2 = __fmul_rn(v2, att_val_b(*t, b, r2));
-        }
-      } else {
-        const float o1 = otf_val(*t, r1, false), o2 = otf_val(*t, r2, false);
-        v1 = __fmul_rn(o1, o1);
-        v2 = __fmul_rn(o2, o2);
-        if (use_att) {
-          v1 = __fmul_rn(v1, att_val(*t, r1));
-          v2 = __fmul_rn(v2, att_val(*t, r2));
-        }
-      }
+      const FShift k = fsh.k[d][b];
+      const float v1 = wiener_term(*t, b, xh, yh, k, kx, ky, use_att != 0);
+      const float v2 = wiener_term(*t, b, xh, yh, fshift_neg(k), -kx, -ky, use_att != 0);
       acc = __fadd_rn(__fadd_rn(acc, v1), v2);
     }
   const float den = __fdiv_rn(1.f, __fadd_rn(acc, wp));
-  double rad = d_hypot_java(xh, yh);
-  double frac = __dmul_rn(rad, cpm) / apo_cut_abs;
-  const float apo = (float)pow(ideal_otf_dev(frac), bend);
-  wa[((size_t)(X >> 2) * W + Y) * 4 + (X & 3)] = __fmul_rn(den, apo);
+  const int ax = abs(xh), ay = abs(yh);
+  const float ap = __ldg(apo + (size_t)max(ax, ay) * (W / 2 + 1) + min(ax, ay));
+  wa[((size_t)(X >> 2) * W + Y) * 4 + (X & 3)] = __fmul_rn(den, ap);
 }
 
 // ---- plan --------------------------------------------------------------------------------------
@@ -217,7 +197,10 @@ int Plan::build(cudaStream_t st) {
   size_t off_mask = off_damp + al((size_t)N * N * sizeof(float));
   const size_t mask_elem = otf_measured(&prm) ? sizeof(float2) : sizeof(float);
   size_t off_wa = off_mask + al((size_t)nA * nC * nwin * nwin * mask_elem);
-  size_t off_nyq = off_wa + al((size_t)W * W * sizeof(float));
+  // Wiener x apo over the Hermitian half read by pass B2 (columns X <= N in whole quads),
+  // then the apodization's octant table ((N + 1)^2 floats, plan build only)
+  const size_t wa_elems = (size_t)(N + 4) * W, apo_elems = (size_t)(N + 1) * (N + 1);
+  size_t off_nyq = off_wa + al((wa_elems + apo_elems) * sizeof(float));
   size_t off_wff = off_nyq + al(nyq.size() * sizeof(float2));
   size_t total = off_wff + al((size_t)N * N * sizeof(float));
   if (total > dev_bytes) {
@@ -255,13 +238,17 @@ int Plan::build(cudaStream_t st) {
       comp_shift(&prm, a, c, &kx, &ky);
       dim3 g(div_up(nwin, 128), nwin);
       k_build_mask<<<g, 128, 0, st>>>(d_masks + (size_t)(a * nC + c) * nwin * nwin * (mask_elem / sizeof(float)), W,
-                                      nwin, win[2 * (a * nC + c)], win[2 * (a * nC + c) + 1], kx, ky, d_otf,
-                                      prm.use_attenuation, (c + 1) / 2);
+                                      nwin, win[2 * (a * nC + c)], win[2 * (a * nC + c) + 1], kx, ky,
+                                      fshift_host(kx, ky), d_otf, prm.use_attenuation, (c + 1) / 2);
     }
   {
-    dim3 g(div_up(W, 128), W);
-    k_build_wa<<<g, 128, 0, st>>>(d_wa, W, d_otf, shift_set(&prm), prm.use_attenuation, (float)(prm.wiener * prm.wiener),
-                                  ht.cutoff * prm.apo_cutoff, prm.apo_bend);
+    float* d_apo = d_wa + wa_elems;
+    int rc = apo_octant_device(d_apo, N, ht.vec_cpm, ht.cutoff * prm.apo_cutoff, prm.apo_bend, st);
+    if (rc) return rc;
+    const ShiftSet sh = shift_set(&prm);
+    dim3 g(div_up(N + 4, 128), W);
+    k_build_wa<<<g, 128, 0, st>>>(d_wa, N + 4, W, d_otf, sh, fshift_set(sh), prm.use_attenuation,
+                                  (float)(prm.wiener * prm.wiener), d_apo);
   }
   FSIM_CHECK_LAUNCH();
   {
@@ -309,6 +296,7 @@ void Plan::fill_job(JobDesc& j, const void* raw, float* out, float* wf, float* f
   j.nP = prm.nr_phases;
   j.nC = nC;
   j.nWin = nwin;
+  j.status = ctx().status;
   j.cmask = otf_measured(&prm) ? 1 : 0;
   j.clip = clip_scale;
   j.bgr = (float)bgr;

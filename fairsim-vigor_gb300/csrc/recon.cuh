@@ -37,6 +37,7 @@ struct JobDesc {
   float* fwf;              // W*W filtered widefield, nullable (widefield: W*W offline, N*N live)
   const float* wff;        // N*N filter of the filtered widefield (resident, k_build_wff)
   float2* Wf;              // workspace (reused after pass C): N*N band-0 rows, then 2 x [W][N] columns
+  int* status;             // the context's device status word (bounded waits that expired)
 };
 
 struct Plan {

@@ -13,6 +13,7 @@
 // FFT_W along y is folded the same way into two N-point inverse FFTs (even/odd rows).
 #pragma once
 
+#include "bulk.cuh"
 #include "common.cuh"
 #include "fft_line.cuh"
 #include "filters.cuh"
@@ -411,135 +412,111 @@ __global__ void __launch_bounds__(Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
 // mirror relations hold, and a pair adds Re(mask_neg) A + Re(mask_pos) conj(B) +
 // (mask_pos n1 + conj(mask_neg n2)) / 2, band 0 (mask_0 T0(X,Y) + conj(mask_0 T0(-X,-Y))) / 2.
 // A launch of one kind skips the jobs of the other (uniform per block).
-template <int N, int ENV, int CBV, bool CM>
-__global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
-                                  col_min_blocks<2 * Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T,
-                                                 Cfg<N, ENV, CBV>::EN, FSIM_B2_REGS>())
-    k_pass_b2(const JobDesc* __restrict__ jobs) {
-  using P = Cfg<N, ENV, CBV>;
-  constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN, T2 = 2 * T;
-  static_assert(EN % 2 == 0, "rows k and k + N must share a thread");
-  const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;  // t in [0, 2T)
-  const int X = blockIdx.x * CB + lane;  // X <= N + CB - 1 < W; only X <= N is stored
-  __shared__ JobDesc J;
-  extern __shared__ float2 sm[];
-  float2* bz = sm;                           // N x CB
-  float2* bh = bz + smem_line_elems(N, CB);  // N x CB
+// Loads of pass B2's pair terms: through the read-only path from global memory, or plain
+// loads from the shared-memory stage of the bulk-copy variant.
+template <bool SM, class V>
+__device__ __forceinline__ V b2_ld(const V* p) {
+  if constexpr (SM) return *p;
+  else return __ldg(p);
+}
+// Pass B2's accumulation in explicitly rounded operations (fixed FMA forms): the bits do not
+// depend on how the compiler contracts the expressions in each kernel that inlines them, so
+// the staged and the plain-load variants (chosen per launch) give the same result.
+__device__ __forceinline__ float2 b2_cmul(float2 a, float2 b) {
+  return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)), __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float2 b2_cadd(float2 a, float2 b) {
+  return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+}
+// Band 0: (T0(X,Y) + conj T0(-X,-Y)) / 2 with one symmetric mask (global loads).
+template <int N, int T2, int EN, bool CM>
+__device__ __forceinline__ void b2_band0(const JobDesc& J, float2 (&acc)[EN], int t, int X, int Xm) {
+  constexpr int W = 2 * N;
+  const int nWin = J.nWin;
+  auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
+  auto qoff = [&](int xl) { return ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3); };
+  const int xl = wrap(X - J.win[0]), xlm = wrap(Xm - J.win[0]), Ys = J.win[1];
+  if (xl >= nWin) return;
+  const float* mk = J.masks + qoff(xl);
+  const float2* mkc = reinterpret_cast<const float2*>(J.masks) + qoff(xl);
+  const float2* tv = J.Tw + qoff(xl);
+  const float2* tm = J.Tw + qoff(xlm);
+  const bool mirror_in = xlm < nWin;  // (X,Y) in the support puts -X in the window
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int Y = t + i * T2;
+    const int yl = wrap(Y - Ys), ylm = wrap(wrap(-Y) - Ys);
+    if (yl < nWin) {
+      const float2 u = tv[(size_t)yl * 4];
+      const float2 um = (mirror_in && ylm < nWin) ? tm[(size_t)ylm * 4] : make_float2(0.f, 0.f);
+      if constexpr (CM) {
+        const float2 m = __ldg(mkc + (size_t)yl * 4);
+        const float2 p = b2_cmul(m, u), q = b2_cmul(m, um);
+        acc[i].x = __fmaf_rn(0.5f, __fadd_rn(p.x, q.x), acc[i].x);
+        acc[i].y = __fmaf_rn(0.5f, __fsub_rn(p.y, q.y), acc[i].y);
+      } else {
+        const float f = __fmul_rn(0.5f, __ldg(mk + (size_t)yl * 4));
+        acc[i].x = __fmaf_rn(f, __fadd_rn(u.x, um.x), acc[i].x);
+        acc[i].y = __fmaf_rn(f, __fsub_rn(u.y, um.y), acc[i].y);
+      }
+    }
+  }
+}
+// One component of a band pair. neg (POS false): mask_neg(X,Y) (A + conj(n2)/2), A = the neg
+// transform at (X, Y) = tv[yl*4], n2 from G[nWin-1-yl]; pos (POS true): mask_pos(X,Y)
+// (conj(B) + n1/2), B = the neg transform at (-X, -Y) = tv[(nWin-1-yl)*4] (the mirrored
+// column), n1 from G[yl]. tv / mk / mkc point at the thread's column of a window column quad
+// (row stride 4), G at the pair's pos-shift column transform, Qy at its y Nyquist response;
+// dd = d' of the neg window column (pos: the mirrored one), cxx = exp(-2 pi i X~/W) Qx[X~ mod N]
+// at X~ = -X (neg) or X (pos).
+template <int N, int T2, int EN, bool CM, bool POS, bool SM>
+__device__ __forceinline__ void b2_pair(float2 (&acc)[EN], int t, int Ys, int nWin, const float2* tv, const float* mk,
+                                        const float2* mkc, const float2* G, const float2* Qy, float2 dd, float2 cxx,
+                                        const float2* twW) {
+  constexpr int W = 2 * N;
+  auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int Y = t + i * T2;
+    const int yl = wrap(Y - Ys);
+    if (yl < nWin) {
+      float2 v, n;
+      if constexpr (!POS) {
+        const int Ym = wrap(-Y);
+        v = b2_ld<SM>(tv + (size_t)yl * 4);
+        // n2: its pos-window row is nWin-1-yl (the windows are mirror images)
+        n = b2_cadd(b2_cmul(twW[Ym], b2_cmul(dd, b2_ld<SM>(Qy + (Ym < N ? Ym : Ym - N)))),
+                    b2_cmul(cxx, b2_ld<SM>(G + (nWin - 1 - yl))));
+      } else {
+        v = b2_ld<SM>(tv + (size_t)(nWin - 1 - yl) * 4);
+        n = b2_cadd(b2_cmul(twW[Y], b2_cmul(dd, b2_ld<SM>(Qy + (Y < N ? Y : Y - N)))),
+                    b2_cmul(cxx, b2_ld<SM>(G + yl)));
+      }
+      // neg: A + conj(n2)/2 (times the mask); pos: conj(B) + n1/2
+      const float vy = POS ? -v.y : v.y, hy = POS ? 0.5f : -0.5f;
+      if constexpr (CM) {
+        const float2 m = b2_ld<SM>(mkc + (size_t)yl * 4), q = b2_cmul(m, n);
+        acc[i].x = __fadd_rn(acc[i].x, __fmaf_rn(m.x, v.x, __fmul_rn(0.5f, q.x)));
+        acc[i].y = __fadd_rn(acc[i].y, __fmaf_rn(m.x, vy, __fmul_rn(hy, q.y)));
+      } else {
+        const float f = b2_ld<SM>(mk + (size_t)yl * 4);
+        acc[i].x = __fmaf_rn(f, __fmaf_rn(0.5f, n.x, v.x), acc[i].x);
+        acc[i].y = __fmaf_rn(f, __fmaf_rn(hy, n.y, vy), acc[i].y);
+      }
+    }
+  }
+}
+// Wiener denominator x apodization, then iFFT_W along y as two N-point inverse FFTs:
+//   out[2n] = iFFT_N(A[k] + A[k+N]),  out[2n+1] = iFFT_N((A[k] - A[k+N]) exp(i pi k/N));
+// rows k and k + N are acc[i] and acc[i + EN/2] of one thread. The even sequences of the CB
+// columns go to bz, the odd ones to bh; threads of the first half then transform the even
+// lines and those of the second half the odd ones.
+template <int N, int T, int CB, int EN>
+__device__ __forceinline__ void b2_finish(const JobDesc& J, float2 (&acc)[EN], float2* bz, float2* bh, int lt, int lane,
+                                          int t, int X) {
+  constexpr int W = 2 * N, T2 = 2 * T;
   const float2* twN = g_stw + stw_offset(N, EN);
   const float2* twW = g_tw + tw_offset(W);
-  load_job(&J, jobs + blockIdx.y, lt, CB * T2);
-  __syncthreads();
-  if ((J.cmask != 0) != CM) return;  // the other launch's job (uniform per block)
-  const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2;
-  auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
-  const int Xm = wrap(-X);
-  const float2* cmasks = reinterpret_cast<const float2*>(J.masks);  // complex masks (CM)
-  float2 acc[EN];
-#pragma unroll
-  for (int i = 0; i < EN; i++) acc[i] = make_float2(0.f, 0.f);
-  // window position (xl, yl) -> offset in a quad-layout nWin x nWin window
-  auto qoff = [&](int xl) { return ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3); };
-  {  // band 0: (T0(X,Y) + conj T0(-X,-Y)) / 2, one symmetric mask
-    const int xl = wrap(X - J.win[0]), xlm = wrap(Xm - J.win[0]), Ys = J.win[1];
-    if (xl < nWin) {
-      const float* mk = J.masks + qoff(xl);
-      const float2* mkc = cmasks + qoff(xl);
-      const float2* tv = J.Tw + qoff(xl);
-      const float2* tm = J.Tw + qoff(xlm);
-      const bool mirror_in = xlm < nWin;  // (X,Y) in the support puts -X in the window
-#pragma unroll
-      for (int i = 0; i < EN; i++) {
-        const int Y = t + i * T2;
-        const int yl = wrap(Y - Ys), ylm = wrap(wrap(-Y) - Ys);
-        if (yl < nWin) {
-          const float2 u = tv[(size_t)yl * 4];
-          const float2 um = (mirror_in && ylm < nWin) ? tm[(size_t)ylm * 4] : make_float2(0.f, 0.f);
-          if constexpr (CM) {
-            const float2 m = __ldg(mkc + (size_t)yl * 4);
-            const float2 p = cmul(m, u), q = cmul(m, um);
-            acc[i].x += 0.5f * (p.x + q.x);
-            acc[i].y += 0.5f * (p.y - q.y);
-          } else {
-            const float f = 0.5f * __ldg(mk + (size_t)yl * 4);
-            acc[i].x += f * (u.x + um.x);
-            acc[i].y += f * (u.y - um.y);
-          }
-        }
-      }
-    }
-  }
-  for (int a = 0; a < J.nA; a++) {
-    for (int b = 1; b <= nPair; b++) {
-      const int cn = 2 * b - 1, cp = 2 * b, ab = a * nPair + (b - 1);
-      const float2* Tc = J.Tw + (size_t)(1 + ab) * nWin * nWin;
-      const float2* Qx = J.nyq + (size_t)(ab * 2) * N;
-      const float2* Qy = Qx + N;
-      const float2* G = J.G + (size_t)ab * nWin;
-      const int xn = wrap(X - J.win[2 * (a * nC + cn)]);
-      if (xn < nWin) {  // neg at (X, Y), and the pos component's n2 at (-X, -Y)
-        const int Yn = J.win[2 * (a * nC + cn) + 1];
-        const float* mk = J.masks + (size_t)(a * nC + cn) * nWin * nWin + qoff(xn);
-        const float2* mkc = cmasks + (size_t)(a * nC + cn) * nWin * nWin + qoff(xn);
-        const float2* tv = Tc + qoff(xn);
-        const float2 dX = J.Dy[(size_t)ab * nWin + xn];
-        const float2 cxm = cmul(twW[Xm], __ldg(Qx + (Xm < N ? Xm : Xm - N)));
-#pragma unroll
-        for (int i = 0; i < EN; i++) {
-          const int Y = t + i * T2;
-          const int yl = wrap(Y - Yn);
-          if (yl < nWin) {
-            const int Ym = wrap(-Y);
-            const float2 A = tv[(size_t)yl * 4];
-            // n2: its pos-window row is nWin-1-yl (the windows are mirror images)
-            const float2 n2 = cadd(cmul(twW[Ym], cmul(dX, __ldg(Qy + (Ym < N ? Ym : Ym - N)))),
-                                   cmul(cxm, G[nWin - 1 - yl]));
-            if constexpr (CM) {
-              const float2 m = __ldg(mkc + (size_t)yl * 4), q = cmul(m, n2);
-              acc[i].x += m.x * A.x + 0.5f * q.x;
-              acc[i].y += m.x * A.y - 0.5f * q.y;
-            } else {
-              const float f = __ldg(mk + (size_t)yl * 4);
-              acc[i].x += f * (A.x + 0.5f * n2.x);
-              acc[i].y += f * (A.y - 0.5f * n2.y);
-            }
-          }
-        }
-      }
-      const int xp = wrap(X - J.win[2 * (a * nC + cp)]);
-      if (xp < nWin) {  // pos at (X, Y) from the neg transform at (-X, -Y)
-        const int Yp = J.win[2 * (a * nC + cp) + 1];
-        const int xm = nWin - 1 - xp;  // window column of -X in the neg window
-        const float* mk = J.masks + (size_t)(a * nC + cp) * nWin * nWin + qoff(xp);
-        const float2* mkc = cmasks + (size_t)(a * nC + cp) * nWin * nWin + qoff(xp);
-        const float2* tv = Tc + qoff(xm);
-        const float2 dM = J.Dy[(size_t)ab * nWin + xm];
-        const float2 cx = cmul(twW[X], __ldg(Qx + (X < N ? X : X - N)));
-#pragma unroll
-        for (int i = 0; i < EN; i++) {
-          const int Y = t + i * T2;
-          const int yl = wrap(Y - Yp);
-          if (yl < nWin) {
-            const float2 B = tv[(size_t)(nWin - 1 - yl) * 4];
-            const float2 n1 = cadd(cmul(twW[Y], cmul(dM, __ldg(Qy + (Y < N ? Y : Y - N)))), cmul(cx, G[yl]));
-            if constexpr (CM) {
-              const float2 m = __ldg(mkc + (size_t)yl * 4), q = cmul(m, n1);
-              acc[i].x += m.x * B.x + 0.5f * q.x;
-              acc[i].y += -m.x * B.y + 0.5f * q.y;
-            } else {
-              const float f = __ldg(mk + (size_t)yl * 4);
-              acc[i].x += f * (B.x + 0.5f * n1.x);
-              acc[i].y += f * (-B.y + 0.5f * n1.y);
-            }
-          }
-        }
-      }
-    }
-  }
-  // Wiener denominator x apodization, then iFFT_W along y as two N-point inverse FFTs:
-  //   out[2n] = iFFT_N(A[k] + A[k+N]),  out[2n+1] = iFFT_N((A[k] - A[k+N]) exp(i pi k/N));
-  // rows k and k + N are acc[i] and acc[i + EN/2] of one thread. The even sequences of the CB
-  // columns go to bz, the odd ones to bh; threads of the first half then transform the even
-  // lines and those of the second half the odd ones.
   {
     const float* wa = J.wa + (size_t)(X >> 2) * W * 4 + (X & 3);
 #pragma unroll
@@ -568,6 +545,217 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
 #pragma unroll
     for (int i = 0; i < EN; i++) J.On[2 * (it + i * T) + g] = x[i];
   }
+}
+
+template <int N, int ENV, int CBV, bool CM>
+__global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
+                                  col_min_blocks<2 * Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T,
+                                                 Cfg<N, ENV, CBV>::EN, FSIM_B2_REGS>())
+    k_pass_b2(const JobDesc* __restrict__ jobs) {
+  using P = Cfg<N, ENV, CBV>;
+  constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN, T2 = 2 * T;
+  static_assert(EN % 2 == 0, "rows k and k + N must share a thread");
+  const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;  // t in [0, 2T)
+  const int X = blockIdx.x * CB + lane;  // X <= N + CB - 1 < W; only X <= N is stored
+  __shared__ JobDesc J;
+  extern __shared__ float2 sm[];
+  float2* bz = sm;                           // N x CB
+  float2* bh = bz + smem_line_elems(N, CB);  // N x CB
+  const float2* twW = g_tw + tw_offset(W);
+  load_job(&J, jobs + blockIdx.y, lt, CB * T2);
+  __syncthreads();
+  if ((J.cmask != 0) != CM) return;  // the other launch's job (uniform per block)
+  const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2;
+  auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
+  const int Xm = wrap(-X);
+  const size_t ME = CM ? 2 : 1;  // floats per mask element
+  float2 acc[EN];
+#pragma unroll
+  for (int i = 0; i < EN; i++) acc[i] = make_float2(0.f, 0.f);
+  auto qoff = [&](int xl) { return ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3); };
+  b2_band0<N, T2, EN, CM>(J, acc, t, X, Xm);
+  for (int a = 0; a < J.nA; a++) {
+    for (int b = 1; b <= nPair; b++) {
+      const int cn = 2 * b - 1, cp = 2 * b, ab = a * nPair + (b - 1);
+      const float2* Tc = J.Tw + (size_t)(1 + ab) * nWin * nWin;
+      const float2* Qx = J.nyq + (size_t)(ab * 2) * N;
+      const float2* Qy = Qx + N;
+      const float2* G = J.G + (size_t)ab * nWin;
+      const int xn = wrap(X - J.win[2 * (a * nC + cn)]);
+      if (xn < nWin) {  // neg at (X, Y), and the pos component's n2 at (-X, -Y)
+        const float* mk = J.masks + ((size_t)(a * nC + cn) * nWin * nWin + qoff(xn)) * ME;
+        const float2 cxm = cmul(twW[Xm], __ldg(Qx + (Xm < N ? Xm : Xm - N)));
+        b2_pair<N, T2, EN, CM, false, false>(acc, t, J.win[2 * (a * nC + cn) + 1], nWin, Tc + qoff(xn), mk,
+                                             reinterpret_cast<const float2*>(mk), G, Qy,
+                                             J.Dy[(size_t)ab * nWin + xn], cxm, twW);
+      }
+      const int xp = wrap(X - J.win[2 * (a * nC + cp)]);
+      if (xp < nWin) {  // pos at (X, Y) from the neg transform at (-X, -Y)
+        const int xm = nWin - 1 - xp;  // window column of -X in the neg window
+        const float* mk = J.masks + ((size_t)(a * nC + cp) * nWin * nWin + qoff(xp)) * ME;
+        const float2 cx = cmul(twW[X], __ldg(Qx + (X < N ? X : X - N)));
+        b2_pair<N, T2, EN, CM, true, false>(acc, t, J.win[2 * (a * nC + cp) + 1], nWin, Tc + qoff(xm), mk,
+                                            reinterpret_cast<const float2*>(mk), G, Qy,
+                                            J.Dy[(size_t)ab * nWin + xm], cx, twW);
+      }
+    }
+  }
+  b2_finish<N, T, CB, EN>(J, acc, bz, bh, lt, lane, t, X);
+}
+
+// Pass B2 with bulk-copy staging. The pair components whose window covers a column of this
+// block's quad are processed as stages: one thread copies a stage's window column quads of
+// the neg transforms, the component's mask quads, the pair's G column and Qy response into a
+// ring of `depth` shared-memory slots with cp.async.bulk, `depth` stages ahead, each slot
+// tracked by an mbarrier; the block reads the stage from shared memory. A pos component reads
+// the mirrored neg column quad, which is aligned with the window's quads; the neg window is
+// the mirror image of the aligned pos window, so the block's four columns fall into one or
+// two of its quads, adjacent in the quad layout and copied together. Band 0 is read from
+// global memory while the first stages are in flight. The FFT buffers of the epilogue alias
+// the ring. Slot layout (bytes, lw = the launch's largest window): quads [0, 64 lw), masks
+// [64 lw, (64 + 32 ME) lw), G [.., + 8 lw), Qy [.., + 8 N).
+constexpr int B2S_MAX_DEPTH = 4;
+constexpr int B2S_MAX_STAGES = 2 * FSIM_MAX_DIRS * (FSIM_MAX_BANDS - 1);
+constexpr int B2S_WAIT_LIMIT = 1 << 20;  // polls of about 100 ns: a copy seen incomplete for ~0.1 s
+__host__ __device__ constexpr size_t b2s_slot_bytes(int lw, int n, bool cm) {
+  return ((size_t)(64 + 32 * (cm ? 2 : 1) + 8) * lw + (size_t)8 * n + 127) / 128 * 128;
+}
+template <int N, int ENV, int CBV, bool CM>
+__global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
+                                  col_min_blocks<2 * Cfg<N, ENV, CBV>::CB * Cfg<N, ENV, CBV>::T,
+                                                 Cfg<N, ENV, CBV>::EN, FSIM_B2_REGS>())
+    k_pass_b2s(const JobDesc* __restrict__ jobs, int lw, int slot_bytes, int depth) {
+  using P = Cfg<N, ENV, CBV>;
+  constexpr int W = P::W, T = P::T, CB = P::CB, EN = P::EN, T2 = 2 * T;
+  constexpr int ME = CM ? 2 : 1;
+  static_assert(EN % 2 == 0, "rows k and k + N must share a thread");
+  static_assert(CB == 4, "one block per column quad");
+  const int lt = threadIdx.x, lane = lt % CB, t = lt / CB;
+  const int X = blockIdx.x * CB + lane;
+  __shared__ JobDesc J;
+  __shared__ alignas(8) uint64_t full[B2S_MAX_DEPTH];
+  // per stage: (a * nPair + b - 1, pos | quads << 1, first Tw quad, first mask quad)
+  __shared__ int4 stg[B2S_MAX_STAGES];
+  __shared__ int nstg, expired;
+  extern __shared__ __align__(128) unsigned char b2s_ring[];
+  const float2* twW = g_tw + tw_offset(W);
+  load_job(&J, jobs + blockIdx.y, lt, CB * T2);
+  __syncthreads();
+  if ((J.cmask != 0) != CM) return;
+  const int nC = J.nC, nWin = J.nWin, nPair = (nC - 1) / 2;
+  auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
+  const int Xm = wrap(-X);
+  if (lt == 0) {
+    const int X0 = blockIdx.x * CB;
+    int n = 0;
+    for (int a = 0; a < J.nA; a++)
+      for (int b = 1; b <= nPair; b++) {
+        const int ab = a * nPair + (b - 1);
+        int qlo = 1 << 30, qhi = -1;
+        for (int l = 0; l < CB; l++) {
+          const int xn = wrap(X0 + l - J.win[2 * (a * nC + 2 * b - 1)]);
+          if (xn < nWin) {
+            qlo = min(qlo, xn >> 2);
+            qhi = max(qhi, xn >> 2);
+          }
+        }
+        // the columns are consecutive inside the window (it is narrower than the grid), so
+        // their quads are one or two adjacent ones
+        if (qhi >= 0 && qhi - qlo <= 1) stg[n++] = make_int4(ab, (qhi - qlo + 1) << 1, qlo, qlo);
+        else if (qhi >= 0 && J.status) atomicOr(J.status, FSIM_STATUS_STAGE_LAYOUT);
+        const int xp0 = wrap(X0 - J.win[2 * (a * nC + 2 * b)]);  // the pos window is quad-aligned
+        if (xp0 < nWin) stg[n++] = make_int4(ab, 1 | (1 << 1), (nWin - 1 - xp0) >> 2, xp0 >> 2);
+      }
+    nstg = n;
+    expired = 0;
+    for (int d = 0; d < depth; d++) mbar_init(&full[d], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  const int ns = nstg;
+  const size_t oq = 0, om = (size_t)64 * lw, og = om + (size_t)32 * ME * lw, oy = og + (size_t)8 * lw;
+  auto issue = [&](int s) {  // thread 0: stage s into slot s % depth
+    const int4 e = stg[s];
+    unsigned char* slot = b2s_ring + (size_t)(s % depth) * slot_bytes;
+    const int ab = e.x, a = ab / nPair, b = ab % nPair + 1, pos = e.y & 1, nq = e.y >> 1;
+    const int comp = pos ? 2 * b : 2 * b - 1;
+    const float2* src_q = J.Tw + ((size_t)(1 + ab) * nWin * nWin + (size_t)e.z * nWin * 4);
+    const float* src_m = J.masks + ((size_t)(a * nC + comp) * nWin * nWin + (size_t)e.w * nWin * 4) * ME;
+    const float2* src_g = J.G + (size_t)ab * nWin;
+    const float2* src_y = J.nyq + (size_t)(ab * 2 + 1) * N;
+    const uint32_t bq = 32u * nq * nWin, bm = 16u * ME * nq * nWin, bg = 8u * nWin, by = 8u * N;
+    uint64_t* bar = &full[s % depth];
+    mbar_arrive_expect(bar, bq + bm + bg + by);
+    bulk_copy_g2s(slot + oq, src_q, bq, bar);
+    bulk_copy_g2s(slot + om, src_m, bm, bar);
+    bulk_copy_g2s(slot + og, src_g, bg, bar);
+    bulk_copy_g2s(slot + oy, src_y, by, bar);
+  };
+  if (lt == 0) {
+    fence_proxy_async();
+    for (int s = 0; s < ns && s < depth; s++) issue(s);
+  }
+  float2 acc[EN];
+#pragma unroll
+  for (int i = 0; i < EN; i++) acc[i] = make_float2(0.f, 0.f);
+  b2_band0<N, T2, EN, CM>(J, acc, t, X, Xm);
+  for (int s = 0; s < ns; s++) {
+    uint64_t* bar = &full[s % depth];
+    const uint32_t par = (uint32_t)(s / depth) & 1u;
+    if (!bulk_wait(bar, par, B2S_WAIT_LIMIT)) {
+      expired = 1;
+      if (J.status && atomicOr(J.status, FSIM_STATUS_BULK_WAIT) == 0) {
+        const unsigned long long w = *reinterpret_cast<volatile unsigned long long*>(bar);
+        J.status[1] = (int)blockIdx.x | (s << 12) | (ns << 18) | (depth << 24);
+        J.status[2] = (int)(w & 0xffffffffu);
+        J.status[3] = (int)(w >> 32);
+      }
+    }
+    const int4 e = stg[s];
+    const unsigned char* slot = b2s_ring + (size_t)(s % depth) * slot_bytes;
+    const int ab = e.x, a = ab / nPair, b = ab % nPair + 1;
+    const float2* Qx = J.nyq + (size_t)(ab * 2) * N;
+    const float2* sq = reinterpret_cast<const float2*>(slot + oq);
+    const float* smk = reinterpret_cast<const float*>(slot + om);
+    const float2* sg = reinterpret_cast<const float2*>(slot + og);
+    const float2* sy = reinterpret_cast<const float2*>(slot + oy);
+    if (!(e.y & 1)) {
+      const int xn = wrap(X - J.win[2 * (a * nC + 2 * b - 1)]);
+      if (xn < nWin) {
+        const size_t qo = (size_t)((xn >> 2) - e.z) * nWin * 4 + (xn & 3);
+        const float* mk = smk + qo * ME;
+        const float2 cxm = cmul(twW[Xm], __ldg(Qx + (Xm < N ? Xm : Xm - N)));
+        b2_pair<N, T2, EN, CM, false, true>(acc, t, J.win[2 * (a * nC + 2 * b - 1) + 1], nWin, sq + qo, mk,
+                                            reinterpret_cast<const float2*>(mk), sg, sy,
+                                            J.Dy[(size_t)ab * nWin + xn], cxm, twW);
+      }
+    } else {
+      const int xp = wrap(X - J.win[2 * (a * nC + 2 * b)]), xm = nWin - 1 - xp;
+      const float* mk = smk + ((size_t)((xp >> 2) - e.w) * nWin * 4 + (xp & 3)) * ME;
+      const float2 cx = cmul(twW[X], __ldg(Qx + (X < N ? X : X - N)));
+      b2_pair<N, T2, EN, CM, true, true>(acc, t, J.win[2 * (a * nC + 2 * b) + 1], nWin,
+                                         sq + (size_t)((xm >> 2) - e.z) * nWin * 4 + (xm & 3), mk,
+                                         reinterpret_cast<const float2*>(mk), sg, sy,
+                                         J.Dy[(size_t)ab * nWin + xm], cx, twW);
+    }
+    __syncthreads();  // every thread is done with the slot
+    if (lt == 0 && s + depth < ns) {
+      fence_proxy_async();
+      issue(s + depth);
+    }
+  }
+  // the ring is free (every issued stage was waited for and read): the FFT buffers alias it.
+  // After an expired wait, the copies of each slot's last stage are waited for once more
+  // (bounded) before the buffers are reused and the block exits.
+  if (expired) {
+    if (lt == 0)
+      for (int s = ns - depth < 0 ? 0 : ns - depth; s < ns; s++)
+        bulk_wait(&full[s % depth], (uint32_t)(s / depth) & 1u, B2S_WAIT_LIMIT);
+    __syncthreads();
+  }
+  float2* bz = reinterpret_cast<float2*>(b2s_ring);
+  float2* bh = bz + smem_line_elems(N, CB);
+  b2_finish<N, T, CB, EN>(J, acc, bz, bh, lt, lane, t, X);
 }
 
 // ---- pass C: rows of the output (complex-to-real) ------------------------------------------------
@@ -679,12 +867,37 @@ static int launch_b2_kind(const JobDesc* d_jobs, int njobs, cudaStream_t st) {
   k_pass_b2<N, ENB, CBB, CM><<<dim3(N / PB::CB + 1, njobs), 2 * PB::CB * PB::T, smem, st>>>(d_jobs);
   return FSIM_OK;
 }
+// The bulk-copy variant where `depth` >= 2 stages of the launch's largest window fit in
+// B2S_RING_BYTES (two blocks of 512 threads per SM) and every window is narrower than the grid;
+// otherwise (and when b2_staging_enabled() is off) the variant with plain loads.
+constexpr size_t B2S_RING_BYTES = 108 * 1024;
+bool b2_staging_enabled();
+template <int N, int ENB, int CBB, bool CM>
+static int launch_b2s_kind(const JobDesc* d_jobs, int njobs, int maxWin, cudaStream_t st) {
+  using PB = Cfg<N, ENB, CBB>;
+  const size_t slot = b2s_slot_bytes(maxWin, N, CM);
+  const int depth = (int)std::min<size_t>(B2S_MAX_DEPTH, B2S_RING_BYTES / slot);
+  if (CBB != 4 || depth < 2 || maxWin >= 2 * N || !b2_staging_enabled())
+    return launch_b2_kind<N, ENB, CBB, CM>(d_jobs, njobs, st);
+  if constexpr (CBB == 4) {
+    const size_t smem = std::max(depth * slot, sizeof(float2) * 2 * smem_line_elems(N, PB::CB));
+    static size_t attr = 0;
+    if (smem > attr) {
+      FSIM_CUDA(cudaFuncSetAttribute(k_pass_b2s<N, ENB, CBB, CM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+      attr = smem;
+    }
+    k_pass_b2s<N, ENB, CBB, CM><<<dim3(N / PB::CB + 1, njobs), 2 * PB::CB * PB::T, smem, st>>>(
+        d_jobs, maxWin, (int)slot, depth);
+  }
+  return FSIM_OK;
+}
 // masks: bit 0 launches the real-mask kind, bit 1 the complex-mask kind (measured OTFs)
 template <int N, int ENB, int CBB>
-static int launch_b2(const JobDesc* d_jobs, int njobs, int masks, cudaStream_t st) {
+static int launch_b2(const JobDesc* d_jobs, int njobs, int masks, int maxWin, cudaStream_t st) {
   int rc = FSIM_OK;
-  if (masks & 1) rc = launch_b2_kind<N, ENB, CBB, false>(d_jobs, njobs, st);
-  if (!rc && (masks & 2)) rc = launch_b2_kind<N, ENB, CBB, true>(d_jobs, njobs, st);
+  if (masks & 1) rc = launch_b2s_kind<N, ENB, CBB, false>(d_jobs, njobs, maxWin, st);
+  if (!rc && (masks & 2)) rc = launch_b2s_kind<N, ENB, CBB, true>(d_jobs, njobs, maxWin, st);
   return rc;
 }
 
@@ -740,13 +953,13 @@ int launch_offline(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, int 
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[2], st);
   if constexpr (single) {
-    rc = launch_b2<N, E0, CBX>(d_jobs, njobs, masks, st);
+    rc = launch_b2<N, E0, CBX>(d_jobs, njobs, masks, maxWin, st);
   } else {
     switch (vb2) {
-      case 0: rc = launch_b2<N, E0, 4>(d_jobs, njobs, masks, st); break;
-      case 1: rc = launch_b2<N, E0, 2>(d_jobs, njobs, masks, st); break;
-      case 2: rc = launch_b2<N, E1, 4>(d_jobs, njobs, masks, st); break;
-      default: rc = launch_b2<N, E1, 2>(d_jobs, njobs, masks, st); break;
+      case 0: rc = launch_b2<N, E0, 4>(d_jobs, njobs, masks, maxWin, st); break;
+      case 1: rc = launch_b2<N, E0, 2>(d_jobs, njobs, masks, maxWin, st); break;
+      case 2: rc = launch_b2<N, E1, 4>(d_jobs, njobs, masks, maxWin, st); break;
+      default: rc = launch_b2<N, E1, 2>(d_jobs, njobs, masks, maxWin, st); break;
     }
   }
   if (rc) return rc;

@@ -27,6 +27,9 @@ const char* last_error() { return g_errbuf; }
 
 // Test hook: the n-th next device allocation of the library fails (fsim_debug_fail_alloc).
 static std::atomic<int> g_fail_alloc{0};
+// Pass B2's bulk-copy staging on (fsim_debug_b2_staging)
+static std::atomic<int> g_b2_staging{1};
+bool b2_staging_enabled() { return g_b2_staging.load(std::memory_order_relaxed) != 0; }
 
 cudaError_t dev_alloc(void** p, size_t bytes) {
   int n = g_fail_alloc.load();
@@ -132,6 +135,8 @@ int ensure_init() {
   }
   FSIM_CUDA(fsim::dev_alloc(&g_ctx.red, sizeof(double) * RED_SLOTS));
   FSIM_CUDA(cudaMallocHost(&g_ctx.red_host, sizeof(double) * RED_SLOTS));
+  FSIM_CUDA(fsim::dev_alloc((void**)&g_ctx.status, 4 * sizeof(int)));
+  FSIM_CUDA(cudaMemset(g_ctx.status, 0, 4 * sizeof(int)));
   cudaDeviceProp prop;
   FSIM_CUDA(cudaGetDeviceProperties(&prop, g_ctx.device));
   g_ctx.num_sms = prop.multiProcessorCount;
@@ -165,6 +170,20 @@ int fsim_sync(void) {
   int rc = fsim::ensure_init();
   if (rc) return rc;
   FSIM_CUDA(cudaDeviceSynchronize());
+  return FSIM_OK;
+}
+
+int fsim_device_status(int* bits, int* detail, int clear) {
+  FSIM_REQUIRE(bits, FSIM_EINVAL, "device_status: null output");
+  int rc = fsim::ensure_init();
+  if (rc) return rc;
+  FSIM_CUDA(cudaDeviceSynchronize());
+  int w[4];
+  FSIM_CUDA(cudaMemcpy(w, fsim::ctx().status, sizeof(w), cudaMemcpyDeviceToHost));
+  *bits = w[0];
+  if (detail)
+    for (int i = 0; i < 3; i++) detail[i] = w[1 + i];
+  if (clear) FSIM_CUDA(cudaMemset(fsim::ctx().status, 0, sizeof(w)));
   return FSIM_OK;
 }
 
@@ -204,6 +223,12 @@ int fsim_fft_plan_2d(int w, int h, int64_t* plan) {
   // nothing to build: the line FFTs use the resident twiddle tables; the handle carries
   // the shape for the vector that is transformed with it
   *plan = ((int64_t)w << 32) | (int64_t)(uint32_t)h;
+  return FSIM_OK;
+}
+
+int fsim_debug_b2_staging(int on, int* prev) {
+  const int p = fsim::g_b2_staging.exchange(on ? 1 : 0);
+  if (prev) *prev = p;
   return FSIM_OK;
 }
 

@@ -15,6 +15,7 @@ struct Ctx {
   bool own_stream = false;
   double* red = nullptr;       // device reduction outputs
   double* red_host = nullptr;  // pinned mirror
+  int* status = nullptr;       // device status word: bits set by kernels whose bounded waits expired
 };
 
 Ctx& ctx();

@@ -189,18 +189,16 @@ __global__ void __launch_bounds__(WfCfg<N>::G* WfCfg<N>::T) k_wf_out(const JobDe
 // frequency lies beyond the cutoff: OtfProvider.otfToVector (S/OtfProvider.java:331-373, no
 // attenuation), WienerFilter.getWidefieldDenominator (S/WienerFilter.java:129-139, from
 // addWienerDenominator at band 0, java:46-79) and OtfProvider.maskOtf(0, 0) (java:538-559).
-// Radii in double as MTool.fhypot; coordinates x~ = x < N/2 ? x : x - N, y~ = y < N/2 ? -y : N - y.
+// Table positions as otf_pos_ff (the reference's double-precision radius, MTool.fhypot, at
+// the boundaries of its tests); coordinates x~ = x < N/2 ? x : x - N, y~ = y < N/2 ? -y : N - y.
 __global__ void k_build_wff(float* __restrict__ f, int N, const OtfTable* __restrict__ otf, float wp) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   if (x >= N) return;
-  const OtfTable& ot = *otf;
-  const double xh = x < N / 2 ? x : x - N, yh = y < N / 2 ? -y : N - y;
-  const double cycl = d_hypot_java(xh, yh) * ot.vec_cpm;
+  float2 o;
   float v = 0.f;
-  if (!(cycl > ot.cutoff)) {
-    const float o = otf_val(ot, cycl, false);
-    const float a2 = __fmul_rn(o, o);
-    v = __fmul_rn(o, __frcp_rn(__fadd_rn(__fadd_rn(a2, a2), wp)));
+  if (otf_at_fast(*otf, 0, freq_x(x, N), freq_y(y, N), FShift{0.f, 0.f, 0.f, 0.f}, 0, 0, false, &o)) {
+    const float a2 = __fmul_rn(o.x, o.x);
+    v = __fmul_rn(o.x, __frcp_rn(__fadd_rn(__fadd_rn(a2, a2), wp)));
   }
   f[(size_t)y * N + x] = v;
 }

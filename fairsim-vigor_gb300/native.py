@@ -244,6 +244,8 @@ _SIGS = {
     "fsim_plan_workspace_bytes": (C.c_size_t, [VP]),
     "fsim_plan_filter_bytes": (C.c_size_t, [VP]),
     "fsim_plan_info": (I32, [VP, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
+    "fsim_plan_filter_table": (I32, [VP, VP, C.c_size_t, C.POINTER(I32)]),
+    "fsim_device_status": (I32, [C.POINTER(I32), VP, I32]),
     "fsim_plan_set_clip_scale": (I32, [VP, I32]),
     "fsim_recon_batch": (I32, [VP, I32, VP, C.c_size_t, VP]),
     "fsim_recon_batch_host": (I32, [VP, I32, I32]),
@@ -263,6 +265,7 @@ _SIGS = {
     "fsim_serve_submit": (I32, [VP, I32, VP, C.c_size_t, C.POINTER(C.c_uint64)]),
     "fsim_serve_cancel": (I32, [VP, C.c_uint64]),
     "fsim_debug_fail_alloc": (I32, [I32]),
+    "fsim_debug_b2_staging": (I32, [I32, C.POINTER(I32)]),
     "fsim_serve_wait": (I32, [VP, C.c_uint64, VP, I32, C.POINTER(F64)]),
     "fsim_serve_stats_get": (I32, [VP, VP]),
     "fsim_serve_params": (I32, [VP, I32, VP]),

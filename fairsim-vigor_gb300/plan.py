@@ -60,6 +60,17 @@ class ReconPlan:
     def filter_bytes(self) -> int:
         return int(N.lib().fsim_plan_filter_bytes(self._h))
 
+    def filter_table(self) -> np.ndarray:
+        """The resident Wiener x apodization table: 2w rows of w + 1 columns (offline, the
+        Hermitian half) or 2w (live), in the reference's vector layout."""
+        W = 2 * self.sp.imgSize
+        nc = W if self.path == N.PATH_LIVE else W // 2 + 1
+        out = np.zeros((W, nc), np.float32)
+        got = C.c_int()
+        N.check(N.lib().fsim_plan_filter_table(self._h, out.ctypes.data_as(C.c_void_p), out.size, C.byref(got)))
+        assert got.value == nc
+        return out
+
     def raw_dtype(self):
         return np.uint16 if self.input_type == N.INPUT_U16 else np.float32
 

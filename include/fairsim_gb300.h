@@ -200,6 +200,22 @@ int fsim_plan_destroy(fsim_plan* plan);
 size_t fsim_plan_workspace_bytes(const fsim_plan* plan);      /* per dataset */
 size_t fsim_plan_filter_bytes(const fsim_plan* plan);         /* resident filters */
 int fsim_plan_info(const fsim_plan* plan, int* w, int* path, int* input_type);
+/* The plan's resident Wiener x apodization table, 1/(sum |OTF|^2 + wiener^2) * apo
+ * (WienerFilter.getDenominator times OtfProvider.writeApoVector, S/SimAlgorithm.java:506-518;
+ * the live path's setupFilters, LM/ReconstructionRunner.java:773-828), copied to host memory
+ * as rows Y = 0..2w-1 of columns X = 0..ncols-1 in the reference's vector layout:
+ * ncols = w + 1 for offline plans (the Hermitian half their column pass reads), 2w for live
+ * plans. n_floats must hold 2w * ncols values; *ncols receives ncols. Synchronises the device. */
+/* Bits set on the device since the last clear by kernels that detected a failure instead of
+ * hanging or faulting (FSIM_STATUS_*; 0 when none): read after the work has finished.
+ * detail (nullable, 3 ints) receives a description of the first event (kernel-specific:
+ * pass B2 records (block x) | (stage << 12) | (stages << 18) | (depth << 24), then the two
+ * 32-bit halves of the barrier word it waited on). Synchronises the device; clear != 0
+ * resets the words. */
+#define FSIM_STATUS_BULK_WAIT 1    /* pass B2: a staged bulk copy was not seen complete in time */
+#define FSIM_STATUS_STAGE_LAYOUT 2 /* pass B2: a stage would span more than two column quads */
+int fsim_device_status(int* bits, int* detail, int clear);
+int fsim_plan_filter_table(const fsim_plan* plan, float* host_out, size_t n_floats, int* ncols);
 /* Output scaling of an offline plan's reconstruction, SimParam.CLIPSCALE
  * (SimParam.java:61-62, applied by SimUtils.spatial / clipAndScale, SimUtils.java:146-153,
  * 244-264): 0 NONE (the default here), 1 CLIP (negative values set to 0), 2 BOTH (scaled to
@@ -296,6 +312,11 @@ int fsim_corr_grid_noalloc(const void* b0, const void* b1, int n, const double* 
  * The nth next device allocation made by the library (nth >= 1) fails as out of memory;
  * 0 disarms. Lets tests drive every FSIM_EOOM path without exhausting a shared GPU. */
 int fsim_debug_fail_alloc(int nth);
+/* Pass B2 of the fused offline path stages its inputs into shared memory with bulk copies
+ * where they fit (on = 1, the default) or reads them with plain loads (on = 0); both give the
+ * same bits. *prev (nullable) receives the previous setting. Lets tests and benchmarks compare
+ * the two. */
+int fsim_debug_b2_staging(int on, int* prev);
 
 /* ---- served form: continuous batching over channels (replaces ReconstructionRunner) --- */
 typedef struct fsim_server fsim_server;

@@ -5,6 +5,8 @@ the C ABI) against the oracle's restatement of the reference:
   * live path = ReconstructionThread.run (org/fairsim/livemode/ReconstructionRunner.java:434-542).
 Tolerance: relative L2 <= 1e-4 against the reference's float semantics (the parity bound),
 and the error against the FP64 oracle is checked to stay below 1e-5."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -75,6 +77,71 @@ def test_offline_fused_clip_scale_vs_oracle(fs, oracle, torch_cuda, clip):
     assert np.array_equal(d_out[0].cpu().numpy(), got)
     assert np.array_equal(d_out[1].cpu().numpy(), plain.reconstruct_host(raw))
     assert rel_l2(d_out[1].cpu().numpy(), oracle.recon_raw(sp, raw, fade=10)) < 1e-4
+
+
+@pytest.mark.parametrize("n", [256, 384, 512, 1024])
+def test_b2_bulk_staging_matches_plain_loads(fs, torch_cuda, n):
+    """Pass B2 staged through shared memory by bulk copies (cp.async.bulk into an
+    mbarrier-tracked ring, where two stages fit) gives the same bits as the variant with plain
+    loads, alone and in a batch with another wavelength's window size, and no bounded wait
+    expires (device status word)."""
+    torch = torch_cuda
+    N_ = fs.native
+    raw, truth, sp = make(fs, n, seed=51 + n)
+    raw2, truth2, sp2 = make(fs, n, seed=52 + n, em_wavelength=600.0)
+    plans = [fs.plan.ReconPlan(p, path=N_.PATH_OFFLINE, input_type=N_.INPUT_F32, fade_px=10) for p in (sp, sp2)]
+    st, prev = C.c_int(), C.c_int()
+    detail = (C.c_int * 3)()
+    N_.check(N_.lib().fsim_device_status(C.byref(st), None, 1))
+
+    def run():
+        d_raw = [torch.from_numpy(r).cuda() for r in (raw, raw2)]
+        d_out = [torch.empty((2 * n, 2 * n), dtype=torch.float32, device="cuda") for _ in range(2)]
+        ws = torch.empty(fs.plan.batch_workspace_bytes(plans), dtype=torch.uint8, device="cuda")
+        fs.plan.recon_batch([(p, r.data_ptr(), o.data_ptr()) for p, r, o in zip(plans, d_raw, d_out)],
+                            ws.data_ptr(), ws.numel())
+        torch.cuda.synchronize()
+        return [plans[0].reconstruct_host(raw)] + [o.cpu().numpy() for o in d_out]
+
+    N_.check(N_.lib().fsim_debug_b2_staging(1, C.byref(prev)))
+    try:
+        staged = run()
+        N_.check(N_.lib().fsim_debug_b2_staging(0, None))
+        plain = run()
+    finally:
+        N_.check(N_.lib().fsim_debug_b2_staging(prev.value, None))
+    N_.check(N_.lib().fsim_device_status(C.byref(st), detail, 1))
+    assert st.value == 0, (st.value, [hex(d & 0xffffffff) for d in detail])
+    for a, b in zip(staged, plain):
+        assert np.array_equal(a, b)
+    assert np.array_equal(staged[0], staged[1])
+
+
+@pytest.mark.parametrize("n,kind,att", [(256, "est", False), (512, "est", True), (1024, "est", False),
+                                        (384, "est", True), (256, "measured", True), (256, "live", True),
+                                        (512, "live", False)])
+def test_plan_filter_table_vs_oracle(fs, oracle, n, kind, att):
+    """The plans' resident Wiener x apodization tables (table positions in float-float, the
+    apodization from its octant table) against the oracle's double-precision
+    getDenominator times writeApoVector: within 1e-7 relative L2, every element within a few
+    float ulps, and nearly all of them bit-equal."""
+    from test_gpu_vector_api import measured_otf
+    raw, truth, sp = make(fs, n, seed=31 + n)
+    if kind == "measured":
+        sp.setOtf(measured_otf(fs, samples=300))
+    sp.otf().setAttenuation(0.97, 1.1)
+    sp.otf().switchAttenuation(att)
+    live = kind == "live"
+    plan = fs.plan.ReconPlan(sp, path=fs.native.PATH_LIVE if live else fs.native.PATH_OFFLINE,
+                             input_type=fs.native.INPUT_U16 if live else fs.native.INPUT_F32, fade_px=10)
+    got = plan.filter_table()
+    bend, cut = (1.0, 2.0) if live else (sp.apoBend, sp.apoCutOff)
+    exp = (oracle.wiener_denominator(sp) * oracle.apo_vector(sp, 2 * n, 2 * n, bend, cut)).astype(np.float32)
+    exp = exp[:, :got.shape[1]]
+    assert rel_l2(got, exp) < 1e-7
+    rel = np.abs(got.astype(np.float64) - exp) / np.maximum(np.abs(exp), 1e-30)
+    assert rel.max() < 5e-7
+    assert np.count_nonzero(got != exp) <= 1e-3 * got.size
 
 
 # (with attenuation on, the table must reach the cutoff: the reference indexes beyond its
