@@ -172,11 +172,13 @@ def run_reference(args):
     return 0
 
 
-# DRAM bytes (read + write) per dataset of each pass at 512^2 3x3, from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum) of this program's passes on a 16-dataset
-# batch (raw 151 MB, larger than L2); per-launch traffic = this x the batch size. None where
-# the pass has not been captured in its current form.
-TRAFFIC_PER_DATASET = {"k_pass_a<512>": 15.98e6, "k_pass_g+k_pass_b1<512>": 11.16e6, "k_pass_b2<512>": None,
+# DRAM bytes (read + write) per dataset of each pass at 512^2 3x3, from single-kernel ncu
+# captures (dram__bytes_read.sum + dram__bytes_write.sum; `ncu --set full -k regex:<pass>
+# -s 2 -c 1` of `bench.py --batch 16 --steps 3 --warmup 3 --no-extras`, raw 151 MB, larger than
+# L2); per-launch traffic = this x the batch size. G+B1 counts B1 (G moves 0.04 MB). Pass C is
+# left out: at batch 16 its input, the Hermitian halves pass B2 has just written (67 MB), is
+# still in L2, so the capture does not show its DRAM traffic at batch 64.
+TRAFFIC_PER_DATASET = {"k_pass_a<512>": 16.02e6, "k_pass_g+k_pass_b1<512>": 11.21e6, "k_pass_b2<512>": 14.20e6,
                        "k_pass_c<512>": None}
 PASS_NAMES = ["k_pass_a<512>", "k_pass_g+k_pass_b1<512>", "k_pass_b2<512>", "k_pass_c<512>"]
 
@@ -369,6 +371,9 @@ def main():
         extras["plain_gpu_rl_both"] = plain_gpu_leg(fs, datasets[0], k=3, style=3)
         extras["speedup_batched_vs_plain"] = value / extras["plain_gpu"]["value"]
         extras["speedup_e2e_vs_plain"] = e2e_value / extras["plain_gpu"]["value"]
+        extras["fused_batch1"] = fused_batch1_leg(fs, datasets[0])
+        extras["speedup_batched_vs_fused_batch1"] = value / extras["fused_batch1"]["value"]
+        extras["speedup_e2e_vs_fused_batch1"] = e2e_value / extras["fused_batch1"]["value"]
         extras["serve"] = serve_leg(fs, seconds=3.0)
         extras["serve_saturated"] = serve_capacity_leg(fs)
         extras["serve_saturated"]["speedup_vs_plain"] = (extras["serve_saturated"]["recon_per_s"]
@@ -490,6 +495,22 @@ def plain_gpu_leg(fs, dataset, k=5, style=0):
     return {"value": k / (time.perf_counter() - t0), "unit": "recon/s", "filter_style": style,
             "note": "op-by-op device vector path (fsim_vec_* + fsim_run_reconstruction), one dataset at a time, "
                     "host buffers"}
+
+
+def fused_batch1_leg(fs, dataset, k=200):
+    """One dataset at a time through the fused plan from host buffers (fsim_recon_host: the raw
+    stack uploaded, the passes, the image downloaded, one C call per dataset): the
+    one-at-a-time GPU form without per-op calls, beside the op-by-op plain GPU form."""
+    N_ = fs.native
+    raw, sp = dataset
+    plan = fs.plan.ReconPlan(sp, path=N_.PATH_OFFLINE, input_type=N_.INPUT_F32, fade_px=10)
+    for _ in range(3):
+        plan.reconstruct_host(raw)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        plan.reconstruct_host(raw)
+    return {"value": k / (time.perf_counter() - t0), "unit": "recon/s",
+            "note": "fused plan, one dataset per call from pageable host memory (fsim_recon_host), %d calls" % k}
 
 
 def mixed_leg(fs, torch, stream, timed, n_datasets=64, steps=5, seed=77):

@@ -47,8 +47,7 @@ __global__ void __launch_bounds__(LinePlan<L>::G* LinePlan<L>::T, LinePlan<L>::M
 }
 
 template <int L, bool INV>
-__global__ void __launch_bounds__(LinePlan<L>::C* LinePlan<L>::T, LinePlan<L>::MINB_C)
-    k_fft_cols(float2* __restrict__ data, int ncols, size_t item_stride, float scale) {
+__device__ __forceinline__ void fft_cols_body(float2* __restrict__ data, int ncols, size_t item_stride, float scale) {
   using P = LinePlan<L>;
   constexpr int T = P::T, E = P::E, C = P::C;
   extern __shared__ float2 s[];
@@ -63,6 +62,18 @@ __global__ void __launch_bounds__(LinePlan<L>::C* LinePlan<L>::T, LinePlan<L>::M
 #pragma unroll
     for (int i = 0; i < E; i++) base[(size_t)(t + i * T) * ncols + x] = cscale(v[i], scale);
   }
+}
+// 8 elements per thread: 64 registers for 32 resident warps per SM
+template <int L, bool INV>
+__global__ void __launch_bounds__(LinePlan<L>::C* LinePlan<L>::T, LinePlan<L>::MINB_C)
+    k_fft_cols(float2* __restrict__ data, int ncols, size_t item_stride, float scale) {
+  fft_cols_body<L, INV>(data, ncols, item_stride, scale);
+}
+// longer plans: the compiler's own register choice (a bound of 512 threads raised it from
+// 96 to 121 registers at 1024 and slowed 16 x 1024^2 from 0.126 to 0.139 ms)
+template <int L, bool INV>
+__global__ void k_fft_cols_wide(float2* __restrict__ data, int ncols, size_t item_stride, float scale) {
+  fft_cols_body<L, INV>(data, ncols, item_stride, scale);
 }
 
 template <int L, bool INV>
@@ -81,16 +92,23 @@ static int launch_rows(float2* d, int nrows, int batch, size_t stride, float sca
 }
 
 template <int L, bool INV>
+constexpr auto cols_kernel() {
+  if constexpr (LinePlan<L>::E <= 8) return k_fft_cols<L, INV>;
+  else return k_fft_cols_wide<L, INV>;
+}
+
+template <int L, bool INV>
 static int launch_cols(float2* d, int ncols, int batch, size_t stride, float scale, cudaStream_t st) {
   using P = LinePlan<L>;
   size_t smem = sizeof(float2) * (size_t)smem_line_elems(L, P::C);
+  auto kern = cols_kernel<L, INV>();
   static bool attr = false;
   if (!attr) {
-    FSIM_CUDA(cudaFuncSetAttribute(k_fft_cols<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FSIM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
   dim3 grid(div_up(ncols, P::C), batch);
-  k_fft_cols<L, INV><<<grid, P::C * P::T, smem, st>>>(d, ncols, stride, scale);
+  kern<<<grid, P::C * P::T, smem, st>>>(d, ncols, stride, scale);
   FSIM_CHECK_LAUNCH();
   return FSIM_OK;
 }
