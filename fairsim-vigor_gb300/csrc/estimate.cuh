@@ -10,6 +10,8 @@
 namespace fsim {
 
 // Device scratch of one estimation (allocated stream-ordered; reused across calls).
+struct FitState;  // fitPeak's iteration state on the device (estimate.cu)
+constexpr int EST_PEAK_BLOCKS = 512;  // blocks of locatePeak's partial argmax
 struct EstScratch {
   int n = 0;
   float2 *b0 = nullptr, *b1 = nullptr, *tx = nullptr, *ty = nullptr;
@@ -17,6 +19,8 @@ struct EstScratch {
   double* kbuf = nullptr;
   float* pmag = nullptr;
   int* pidx = nullptr;
+  double* red = nullptr;  // reduction scratch (RED_SLOTS doubles): norms left on the device
+  FitState* fit = nullptr;
   int alloc(int N, cudaStream_t st);
   void free(cudaStream_t st);
 };
@@ -25,8 +29,10 @@ struct EstScratch {
 int common_region_device(float2* b0, float2* b1, int w, int h, const OtfTable* t, double kx, double ky, double dist,
                          double wl, bool divide, cudaStream_t st, int bn0 = 0, int bn1 = 1);
 int locate_peak_device(const float2* v, int w, int h, double kmin, EstScratch& s, cudaStream_t st, double out4[4]);
+// scal: the normaliser, or taken as 1 / *n2 when n2 (device) is not null
 int corr_grid_device(const float2* b0, const float2* b1, int N, const double* kxs, int nx, const double* kys, int ny,
-                     double scal, EstScratch& s, cudaStream_t st, std::vector<std::complex<double>>& out);
+                     double scal, EstScratch& s, cudaStream_t st, std::vector<std::complex<double>>& out,
+                     const double* n2 = nullptr);
 int fit_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
                     double search, EstScratch& s, cudaStream_t st, double out4[4], double* grid_out, int bn0 = 0,
                     int bn1 = 1);

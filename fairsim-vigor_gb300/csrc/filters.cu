@@ -266,8 +266,37 @@ int apo_device(float* out, int cplx, int W, int H, double vec_cpm, double cutoff
   return FSIM_OK;
 }
 
+// Unshifted on a square grid the attenuation depends on (|x~|, |y~|) only, symmetrically:
+// evaluated in double once per octant point 0 <= j <= i <= n/2 (the same expression as
+// k_att_vector, so the same bits) and spread over the grid.
+__global__ void k_att_octant(float* __restrict__ q, int h2, double vec_cpm, double str, double fwhm) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (j > i) return;
+  const double rad = d_hypot_java((double)i, (double)j);
+  const double dist = __dmul_rn(rad, vec_cpm);
+  const double s = fwhm / 2.355;
+  const double g = exp(-__dmul_rn(dist, dist) / __dmul_rn(2.0, __dmul_rn(s, s)));
+  q[(size_t)i * (h2 + 1) + j] = (float)__dsub_rn(1.0, __dmul_rn(str, g));
+}
+__global__ void k_att_expand(float* __restrict__ v, int n, const float* __restrict__ q) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= n) return;
+  const int ax = abs(freq_x(x, n)), ay = abs(freq_y(y, n));
+  v[(size_t)y * n + x] = __ldg(q + (size_t)max(ax, ay) * (n / 2 + 1) + min(ax, ay));
+}
+
 int att_device(float* out, int w, int h, double vec_cpm, double str, double fwhm, double kx, double ky, cudaStream_t st) {
   dim3 g(div_up(w, 128), h);
+  if (w == h && w % 2 == 0 && kx == 0 && ky == 0) {
+    const int h2 = w / 2;
+    float* q = nullptr;
+    FSIM_CUDA(fsim::dev_alloc_async(&q, sizeof(float) * (size_t)(h2 + 1) * (h2 + 1), st));
+    k_att_octant<<<dim3(div_up(h2 + 1, 128), h2 + 1), 128, 0, st>>>(q, h2, vec_cpm, str, fwhm);
+    k_att_expand<<<g, 128, 0, st>>>(out, w, q);
+    FSIM_CHECK_LAUNCH();
+    FSIM_CUDA(cudaFreeAsync(q, st));
+    return FSIM_OK;
+  }
   k_att_vector<<<g, 128, 0, st>>>(out, w, h, vec_cpm, str, fwhm, kx, ky);
   FSIM_CHECK_LAUNCH();
   return FSIM_OK;

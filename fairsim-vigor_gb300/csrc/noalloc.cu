@@ -93,7 +93,7 @@ extern "C" int fsim_corr_grid_noalloc(const void* b0, const void* b1, int n, con
   for (int i = 0; i < nx; i++) k[i] = kx[i];
   for (int i = 0; i < ny; i++) k[NA_MAX_K + i] = -ky[i];
   FSIM_CUDA(cudaMemcpyAsync(kv, k, sizeof(k), cudaMemcpyHostToDevice, st));
-  fsim::launch_corr_grid((const float2*)b0, (const float2*)b1, n, kv, nx, ny, scal, tx, ty, Q, corr, st);
+  fsim::launch_corr_grid((const float2*)b0, (const float2*)b1, n, kv, nx, ny, scal, nullptr, tx, ty, Q, corr, st);
   FSIM_CHECK_LAUNCH();
   FSIM_CUDA(cudaMemcpyAsync(out, corr, sizeof(double2) * nx * ny, cudaMemcpyDeviceToHost, st));
   FSIM_CUDA(cudaStreamSynchronize(st));

@@ -124,7 +124,7 @@ __device__ __forceinline__ bool otf_at_c(const OtfTable& t, int band, double xh,
 struct FShift {  // a shift as float hi + lo (hi = (float)k, lo = (float)(k - hi))
   float xh, xl, yh, yl;
 };
-inline FShift fshift_host(double kx, double ky) {
+__host__ __device__ inline FShift fshift_host(double kx, double ky) {
   FShift s;
   s.xh = (float)kx;
   s.xl = (float)(kx - (double)s.xh);

@@ -163,14 +163,14 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     damp_row<EN, T>(J, row, t, x);
     line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
 #pragma unroll
-    for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
+    for (int i = 0; i < EN; i++) bh[t + i * T] = x[i];
     __syncthreads();
     const int Xs = J.win[0];
     for (int xl = t; xl < J.nWin; xl += T) {
       int X = Xs + xl;
       if (X >= W) X -= W;
       const int m = paste_src<N>(X);
-      J.I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = m >= 0 ? bh[sidx(m)] : make_float2(0.f, 0.f);
+      J.I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = m >= 0 ? bh[m] : make_float2(0.f, 0.f);
     }
     if (y == 0 && t == 0) *J.clip_max = 0.f;  // CLIPSCALE.BOTH: pass C takes the maximum from 0
     return;
@@ -198,6 +198,11 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     }
     damp_row<EN, T>(J, row, t, z);
   };
+  // Row values outside the transforms (the stashed mixed row, transform outputs, window
+  // read-out) use the unpadded index: 16 consecutive float2 of a half-warp then fall into
+  // distinct bank pairs from any starting element, where the padded layout of the transforms'
+  // exchanges splits a run that crosses a 16-element boundary (2-way conflicts on the window
+  // read-out).
   // Components: band 0, then per band b the pair neg = 2b-1, pos = 2b. The separation
   // coefficients of a pair are complex conjugates, so z_pos = conj(z_neg): the pos
   // component's row transform follows from the neg one's (below). A line stays in
@@ -220,7 +225,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     // the mixed row waits in bz (each thread its own elements) for the even-sample product
     // below, instead of in 16 registers across the three transforms of the odd samples
 #pragma unroll
-    for (int i = 0; i < EN; i++) bz[sidx(t + i * T)] = x[i];
+    for (int i = 0; i < EN; i++) bz[t + i * T] = x[i];
     line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);  // Z = FFT_N(z)
     if (t == (N / 2) % T) {
       const float2 zn = x[(N / 2) / T];
@@ -236,14 +241,14 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     for (int i = 0; i < EN; i++) x[i] = cmul(x[i], __ldg(ro + t + i * T));
     line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
 #pragma unroll
-    for (int i = 0; i < EN; i++) bh[sidx(t + i * T)] = x[i];
+    for (int i = 0; i < EN; i++) bh[t + i * T] = x[i];
     // even samples times the even-sample ramp, FFT: E
 #pragma unroll
-    for (int i = 0; i < EN; i++) x[i] = cmul(bz[sidx(t + i * T)], __ldg(re + t + i * T));
+    for (int i = 0; i < EN; i++) x[i] = cmul(bz[t + i * T], __ldg(re + t + i * T));
     __syncthreads();  // every thread has its elements back before the transform reuses bz
     line_fft_reg<N, T, 1, false>(x, bz, 0, t, twN);
 #pragma unroll
-    for (int i = 0; i < EN; i++) bz[sidx(t + i * T)] = x[i];
+    for (int i = 0; i < EN; i++) bz[t + i * T] = x[i];
     __syncthreads();
     // neg window of the shifted spectrum: E[X mod N] + exp(-2 pi i X/W) O[X mod N]
     const int Xs = J.win[2 * (a * nC + cn)];
@@ -252,7 +257,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
       int X = Xs + xl;
       if (X >= W) X -= W;
       const int m = X < N ? X : X - N;
-      I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(bz[sidx(m)], cmul(twW[X], bh[sidx(m)]));
+      I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(bz[m], cmul(twW[X], bh[m]));
     }
   }
 }

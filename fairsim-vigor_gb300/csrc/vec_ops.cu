@@ -243,6 +243,20 @@ int norm2_device(const float2* v, size_t n, double* out, cudaStream_t st) {
   return reduce_device(0, reinterpret_cast<const float*>(v), nullptr, 2 * n, 1, st, out, nullptr);
 }
 
+// The same reduction (same blocks, same order, so the same bits) into the caller's RED_SLOTS
+// doubles of scratch, left on the device at *result = scratch + RED_SLOTS - 2 (no sync).
+int norm2_device_async(const float2* v, size_t n, double* scratch, const double** result, cudaStream_t st) {
+  const int threads = 256;
+  const size_t nf = 2 * n;
+  int blocks = grid_for(nf, threads);
+  if (blocks > (RED_SLOTS - 8) / 2) blocks = (RED_SLOTS - 8) / 2;
+  k_reduce_partial<0><<<blocks, threads, 0, st>>>(reinterpret_cast<const float*>(v), nullptr, nf, 1, scratch);
+  k_reduce_final<<<1, 256, 0, st>>>(scratch, blocks, scratch + RED_SLOTS - 2);
+  FSIM_CHECK_LAUNCH();
+  *result = scratch + RED_SLOTS - 2;
+  return FSIM_OK;
+}
+
 int times_real_device(float2* y, const float* x, size_t n, cudaStream_t st) {
   k_times_cr<<<grid_for(n, 256), 256, 0, st>>>(y, x, n);
   FSIM_CHECK_LAUNCH();
