@@ -112,7 +112,8 @@ __device__ __forceinline__ bool otf_at_c(const OtfTable& t, int band, double xh,
 // ---- table positions in float-float arithmetic -----------------------------------------------
 // The reference evaluates cycl = hypot(xh - kx, yh - ky) * vec_cpm and pos = cycl /
 // cycles_per_sample in double and then branches on cycl >= cutoff and floor(pos). GB300 runs
-// FP64 at a small fraction of its FP32 rate, so the plan builders evaluate the same
+// FP64 at a small fraction of its FP32 rate, so the plan builders and the fit's common region
+// evaluate the same
 // quantities as unevaluated sums of two floats (hi + lo, ~44 significant bits; error-free
 // sum and FMA product steps, Dekker / Knuth): the absolute error of pos stays below 1e-9
 // samples for |kx|, |ky| <= 4096 pixels, so every test the reference makes comes out the
