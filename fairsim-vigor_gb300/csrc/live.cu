@@ -66,8 +66,7 @@ __global__ void __launch_bounds__(LCfg<N>::GA* LCfg<N>::TN) k_live_a(const JobDe
   const int g = threadIdx.x / T, t = threadIdx.x % T;
   const int y = blockIdx.x * G + g;
   __shared__ float2 sm[G * smem_line_elems(N, 1)];
-  __shared__ float2 tw[stw_len(N, E)];
-  stage_stage_twiddles<N, E>(tw, threadIdx.x, G * T);
+  const float2* tw = g_stw + stw_offset(N, E);  // stage twiddles through L1
   float2* s = sm + g * smem_line_elems(N, 1);
   const size_t frame = (size_t)N * N, row = (size_t)y * N;
   const float* rawf = (const float*)J.raw;
@@ -104,7 +103,6 @@ __global__ void __launch_bounds__(LCfg<N>::GA* LCfg<N>::TN) k_live_a(const JobDe
 #pragma unroll
     for (int i = 0; i < E; i++) J.widefield[row + t + i * T] = __fmul_rn(wf[i], sc);
   }
-  __syncthreads();  // the twiddle table is staged
   for (int a = 0; a < nA; a++)
     for (int c = 0; c < nC; c++) {
       const float2* coef = J.coef + (a * nC + c) * nP;
@@ -139,10 +137,8 @@ __global__ void __launch_bounds__(LCfg<N>::CBL* LCfg<N>::TN, live_min_blocks(LCf
   const int lt = threadIdx.x, lane = lt % C, t = lt / C;
   const int x = blockIdx.x * C + lane;
   __shared__ float2 s[smem_line_elems(N, C)];
-  __shared__ float2 tw[stw_len(N, E)];
-  stage_stage_twiddles<N, E>(tw, lt, C * T);
+  const float2* tw = g_stw + stw_offset(N, E);  // stage twiddles through L1
   const size_t frame = (size_t)N * N;
-  __syncthreads();  // the twiddle table is staged
   for (int a = 0; a < J.nA; a++)
     for (int c = 0; c < J.nC; c++) {
       float2* X = J.I + (size_t)(a * J.nC + c) * frame;
@@ -175,13 +171,16 @@ __global__ void __launch_bounds__(LCfg<N>::TW, live_min_blocks(LCfg<N>::TW)) k_l
   constexpr int W = P::W, TW = P::TW, EW = P::EW, EN = N / TW;
   const JobDesc& J = jobs[blockIdx.y];
   const int Y = blockIdx.x, t = threadIdx.x;
+  // Stage twiddles are read through L1 (g_stw), as in the offline passes: per-block copies in
+  // shared memory held the pass to 16 warps per SM. Row values outside the transforms (the
+  // paste read-out, the sum) use the unpadded index: a half-warp's 16 consecutive float2 then
+  // fall into distinct bank pairs from any starting element.
   __shared__ float2 acc[smem_line_elems(W, 1)];
   __shared__ float2 s[smem_line_elems(N, 1)];
-  __shared__ float2 twN[stw_len(N, EN)], twW[stw_len(W, EW)];
-  stage_stage_twiddles<N, EN>(twN, t, TW);
-  stage_stage_twiddles<W, EW>(twW, t, TW);
+  const float2* twN = g_stw + stw_offset(N, EN);
+  const float2* twW = g_stw + stw_offset(W, EW);
 #pragma unroll
-  for (int i = 0; i < EW; i++) acc[sidx(t + i * TW)] = make_float2(0.f, 0.f);
+  for (int i = 0; i < EW; i++) acc[t + i * TW] = make_float2(0.f, 0.f);
   const size_t frame = (size_t)N * N;
   for (int a = 0; a < J.nA; a++)
     for (int c = 0; c < J.nC; c++) {
@@ -192,7 +191,7 @@ __global__ void __launch_bounds__(LCfg<N>::TW, live_min_blocks(LCfg<N>::TW)) k_l
       float2 v[EN];  // element t + i*TW of the row, in registers through the transforms
 #pragma unroll
       for (int i = 0; i < EN; i++) v[i] = X[t + i * TW];
-      __syncthreads();  // the twiddle tables are staged; the previous paste has read s
+      __syncthreads();  // the previous paste has read s
       if (c > 0) {
         line_fft_reg<N, TW, 1, true>(v, s, 0, t, twN);
         const float2* rx = J.ramps + (size_t)(a * J.nC + c) * 2 * N;
@@ -201,7 +200,7 @@ __global__ void __launch_bounds__(LCfg<N>::TW, live_min_blocks(LCfg<N>::TW)) k_l
         line_fft_reg<N, TW, 1, false>(v, s, 0, t, twN);
       }
 #pragma unroll
-      for (int i = 0; i < EN; i++) s[sidx(t + i * TW)] = v[i];
+      for (int i = 0; i < EN; i++) s[t + i * TW] = v[i];
       __syncthreads();
       // pasteFreq at (xInt, yInt) and fullResult.add
 #pragma unroll
@@ -209,8 +208,8 @@ __global__ void __launch_bounds__(LCfg<N>::TW, live_min_blocks(LCfg<N>::TW)) k_l
         const int Xo = t + i * TW;
         const int xs = paste_source(Xo, xInt, N, W);
         if (xs >= 0) {
-          float2& o = acc[sidx(Xo)];
-          const float2 v = s[sidx(xs)];
+          float2& o = acc[Xo];
+          const float2 v = s[xs];
           o = make_float2(__fadd_rn(o.x, v.x), __fadd_rn(o.y, v.y));
         }
       }
@@ -222,7 +221,7 @@ __global__ void __launch_bounds__(LCfg<N>::TW, live_min_blocks(LCfg<N>::TW)) k_l
   for (int i = 0; i < EW; i++) {
     const int k = t + i * TW;
     const float f = __ldg(&wa[k]);
-    const float2 o = acc[sidx(k)];
+    const float2 o = acc[k];
     u[i] = make_float2(o.x * f, o.y * f);
   }
   __syncthreads();  // acc is read: it becomes the transform's scratch
@@ -241,12 +240,10 @@ __global__ void __launch_bounds__(LCfg<N>::CD* LCfg<N>::TW) k_live_d(const JobDe
   const int lt = threadIdx.x, lane = lt % C, t = lt / C;
   const int X = blockIdx.x * C + lane;
   extern __shared__ float2 s[];
-  __shared__ float2 tw[stw_len(W, EW)];
-  stage_stage_twiddles<W, EW>(tw, lt, C * TW);
+  const float2* tw = g_stw + stw_offset(W, EW);  // stage twiddles through L1
   float2 v[EW];  // element t + i*TW of the column, in registers through the transform
 #pragma unroll
   for (int i = 0; i < EW; i++) v[i] = J.O[(size_t)(t + i * TW) * W + X];
-  __syncthreads();  // the twiddle table is staged
   line_fft_reg<W, TW, C, true>(v, s, lane, t, tw);
   const float scale = 1.f / ((float)W * (float)W);
 #pragma unroll
