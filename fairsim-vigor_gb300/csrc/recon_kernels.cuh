@@ -433,39 +433,46 @@ __device__ __forceinline__ float2 b2_cmul(float2 a, float2 b) {
 __device__ __forceinline__ float2 b2_cadd(float2 a, float2 b) {
   return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
 }
-// Band 0: (T0(X,Y) + conj T0(-X,-Y)) / 2 with one symmetric mask (global loads).
+// Band 0: (T0(X,Y) + conj T0(-X,-Y)) / 2 with one symmetric mask. tv / mk / mkc point at the
+// thread's column of the window's column quad (row stride 4), tm at its mirrored column (-X;
+// mirror_in false when -X lies outside the window), from global or shared memory (SM).
+template <int N, int T2, int EN, bool CM, bool SM>
+__device__ __forceinline__ void b2_band0_px(float2 (&acc)[EN], int t, int Ys, int nWin, const float2* tv,
+                                            const float2* tm, bool mirror_in, const float* mk, const float2* mkc) {
+  constexpr int W = 2 * N;
+  auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
+#pragma unroll
+  for (int i = 0; i < EN; i++) {
+    const int Y = t + i * T2;
+    const int yl = wrap(Y - Ys), ylm = wrap(wrap(-Y) - Ys);
+    if (yl < nWin) {
+      const float2 u = b2_ld<SM>(tv + (size_t)yl * 4);
+      const float2 um = (mirror_in && ylm < nWin) ? b2_ld<SM>(tm + (size_t)ylm * 4) : make_float2(0.f, 0.f);
+      if constexpr (CM) {
+        const float2 m = b2_ld<SM>(mkc + (size_t)yl * 4);
+        const float2 p = b2_cmul(m, u), q = b2_cmul(m, um);
+        acc[i].x = __fmaf_rn(0.5f, __fadd_rn(p.x, q.x), acc[i].x);
+        acc[i].y = __fmaf_rn(0.5f, __fsub_rn(p.y, q.y), acc[i].y);
+      } else {
+        const float f = __fmul_rn(0.5f, b2_ld<SM>(mk + (size_t)yl * 4));
+        acc[i].x = __fmaf_rn(f, __fadd_rn(u.x, um.x), acc[i].x);
+        acc[i].y = __fmaf_rn(f, __fsub_rn(u.y, um.y), acc[i].y);
+      }
+    }
+  }
+}
 template <int N, int T2, int EN, bool CM>
 __device__ __forceinline__ void b2_band0(const JobDesc& J, float2 (&acc)[EN], int t, int X, int Xm) {
   constexpr int W = 2 * N;
   const int nWin = J.nWin;
   auto wrap = [](int v) { return v < 0 ? v + W : (v >= W ? v - W : v); };
   auto qoff = [&](int xl) { return ((size_t)(xl >> 2) * nWin) * 4 + (xl & 3); };
-  const int xl = wrap(X - J.win[0]), xlm = wrap(Xm - J.win[0]), Ys = J.win[1];
+  const int xl = wrap(X - J.win[0]), xlm = wrap(Xm - J.win[0]);
   if (xl >= nWin) return;
-  const float* mk = J.masks + qoff(xl);
-  const float2* mkc = reinterpret_cast<const float2*>(J.masks) + qoff(xl);
-  const float2* tv = J.Tw + qoff(xl);
-  const float2* tm = J.Tw + qoff(xlm);
   const bool mirror_in = xlm < nWin;  // (X,Y) in the support puts -X in the window
-#pragma unroll
-  for (int i = 0; i < EN; i++) {
-    const int Y = t + i * T2;
-    const int yl = wrap(Y - Ys), ylm = wrap(wrap(-Y) - Ys);
-    if (yl < nWin) {
-      const float2 u = tv[(size_t)yl * 4];
-      const float2 um = (mirror_in && ylm < nWin) ? tm[(size_t)ylm * 4] : make_float2(0.f, 0.f);
-      if constexpr (CM) {
-        const float2 m = __ldg(mkc + (size_t)yl * 4);
-        const float2 p = b2_cmul(m, u), q = b2_cmul(m, um);
-        acc[i].x = __fmaf_rn(0.5f, __fadd_rn(p.x, q.x), acc[i].x);
-        acc[i].y = __fmaf_rn(0.5f, __fsub_rn(p.y, q.y), acc[i].y);
-      } else {
-        const float f = __fmul_rn(0.5f, __ldg(mk + (size_t)yl * 4));
-        acc[i].x = __fmaf_rn(f, __fadd_rn(u.x, um.x), acc[i].x);
-        acc[i].y = __fmaf_rn(f, __fsub_rn(u.y, um.y), acc[i].y);
-      }
-    }
-  }
+  b2_band0_px<N, T2, EN, CM, false>(acc, t, J.win[1], nWin, J.Tw + qoff(xl), J.Tw + (mirror_in ? qoff(xlm) : 0),
+                                    mirror_in, J.masks + qoff(xl),
+                                    reinterpret_cast<const float2*>(J.masks) + qoff(xl));
 }
 // One component of a band pair. neg (POS false): mask_neg(X,Y) (A + conj(n2)/2), A = the neg
 // transform at (X, Y) = tv[yl*4], n2 from G[nWin-1-yl]; pos (POS true): mask_pos(X,Y)
@@ -615,15 +622,23 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
 // tracked by an mbarrier; the block reads the stage from shared memory. A pos component reads
 // the mirrored neg column quad, which is aligned with the window's quads; the neg window is
 // the mirror image of the aligned pos window, so the block's four columns fall into one or
-// two of its quads, adjacent in the quad layout and copied together. Band 0 is read from
-// global memory while the first stages are in flight. The FFT buffers of the epilogue alias
-// the ring. Slot layout (bytes, lw = the launch's largest window): quads [0, 64 lw), masks
-// [64 lw, (64 + 32 ME) lw), G [.., + 8 lw), Qy [.., + 8 N).
+// two of its quads, adjacent in the quad layout and copied together. Band 0 is the first
+// stage (its window column quad, the one or two quads of the mirrored columns, its mask
+// quad). The FFT buffers of the epilogue alias the ring. Slot layout (bytes, lw = the launch's
+// largest window): pair stages quads [0, 64 lw), masks [64 lw, (64 + 32 ME) lw),
+// G [.., + 8 lw), Qy [.., + 8 N); the band-0 stage mirrored quads [0, 64 lw), direct quad
+// [64 lw, 96 lw), mask [96 lw, (96 + 16 ME) lw).
 constexpr int B2S_MAX_DEPTH = 4;
-constexpr int B2S_MAX_STAGES = 2 * FSIM_MAX_DIRS * (FSIM_MAX_BANDS - 1);
+constexpr int B2S_MAX_STAGES = 1 + 2 * FSIM_MAX_DIRS * (FSIM_MAX_BANDS - 1);
 constexpr int B2S_WAIT_LIMIT = 1 << 20;  // polls of about 100 ns: a copy seen incomplete for ~0.1 s
 __host__ __device__ constexpr size_t b2s_slot_bytes(int lw, int n, bool cm) {
-  return ((size_t)(64 + 32 * (cm ? 2 : 1) + 8) * lw + (size_t)8 * n + 127) / 128 * 128;
+  // pair stage: quads 64 lw, masks 32 ME lw, G 8 lw, Qy 8 n; band-0 stage: mirrored quads
+  // 64 lw, the direct quad 32 lw, its mask 16 ME lw
+  return ((((size_t)(64 + 32 * (cm ? 2 : 1) + 8) * lw + (size_t)8 * n) > (size_t)(96 + 16 * (cm ? 2 : 1)) * lw
+               ? ((size_t)(64 + 32 * (cm ? 2 : 1) + 8) * lw + (size_t)8 * n)
+               : (size_t)(96 + 16 * (cm ? 2 : 1)) * lw) +
+          127) /
+         128 * 128;
 }
 template <int N, int ENV, int CBV, bool CM>
 __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
@@ -639,7 +654,9 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   const int X = blockIdx.x * CB + lane;
   __shared__ JobDesc J;
   __shared__ alignas(8) uint64_t full[B2S_MAX_DEPTH];
-  // per stage: (a * nPair + b - 1, pos | quads << 1, first Tw quad, first mask quad)
+  // per stage: (a * nPair + b - 1, kind | quads << 2, first Tw quad, first mask quad); kind 0
+  // a pair's neg component, 1 its pos component, 2 band 0 (then: -, kind | mirrored quads << 2,
+  // the direct quad, the first mirrored quad)
   __shared__ int4 stg[B2S_MAX_STAGES];
   __shared__ int nstg, expired;
   extern __shared__ __align__(128) unsigned char b2s_ring[];
@@ -653,6 +670,22 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   if (lt == 0) {
     const int X0 = blockIdx.x * CB;
     int n = 0;
+    {  // band 0: its window is quad-aligned; the mirrored columns fall into one or two quads
+      const int xl0 = wrap(X0 - J.win[0]);
+      if (xl0 < nWin) {
+        int mlo = 1 << 30, mhi = -1;
+        for (int l = 0; l < CB; l++) {
+          const int xlm = wrap(wrap(-(X0 + l)) - J.win[0]);
+          if (xlm < nWin) {
+            mlo = min(mlo, xlm >> 2);
+            mhi = max(mhi, xlm >> 2);
+          }
+        }
+        if (mhi < 0) stg[n++] = make_int4(-1, 2, xl0 >> 2, 0);
+        else if (mhi - mlo <= 1) stg[n++] = make_int4(-1, 2 | ((mhi - mlo + 1) << 2), xl0 >> 2, mlo);
+        else if (J.status) atomicOr(J.status, FSIM_STATUS_STAGE_LAYOUT);
+      }
+    }
     for (int a = 0; a < J.nA; a++)
       for (int b = 1; b <= nPair; b++) {
         const int ab = a * nPair + (b - 1);
@@ -666,10 +699,10 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
         }
         // the columns are consecutive inside the window (it is narrower than the grid), so
         // their quads are one or two adjacent ones
-        if (qhi >= 0 && qhi - qlo <= 1) stg[n++] = make_int4(ab, (qhi - qlo + 1) << 1, qlo, qlo);
+        if (qhi >= 0 && qhi - qlo <= 1) stg[n++] = make_int4(ab, (qhi - qlo + 1) << 2, qlo, qlo);
         else if (qhi >= 0 && J.status) atomicOr(J.status, FSIM_STATUS_STAGE_LAYOUT);
         const int xp0 = wrap(X0 - J.win[2 * (a * nC + 2 * b)]);  // the pos window is quad-aligned
-        if (xp0 < nWin) stg[n++] = make_int4(ab, 1 | (1 << 1), (nWin - 1 - xp0) >> 2, xp0 >> 2);
+        if (xp0 < nWin) stg[n++] = make_int4(ab, 1 | (1 << 2), (nWin - 1 - xp0) >> 2, xp0 >> 2);
       }
     nstg = n;
     expired = 0;
@@ -679,10 +712,21 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   __syncthreads();
   const int ns = nstg;
   const size_t oq = 0, om = (size_t)64 * lw, og = om + (size_t)32 * ME * lw, oy = og + (size_t)8 * lw;
+  const size_t od0 = (size_t)64 * lw, ok0 = (size_t)96 * lw;  // band-0 stage: direct quad, mask
   auto issue = [&](int s) {  // thread 0: stage s into slot s % depth
     const int4 e = stg[s];
     unsigned char* slot = b2s_ring + (size_t)(s % depth) * slot_bytes;
-    const int ab = e.x, a = ab / nPair, b = ab % nPair + 1, pos = e.y & 1, nq = e.y >> 1;
+    if ((e.y & 3) == 2) {
+      const int nqm = e.y >> 2;
+      const uint32_t bd = 32u * nWin, bk = 16u * ME * nWin, bmq = 32u * nqm * nWin;
+      uint64_t* bar = &full[s % depth];
+      mbar_arrive_expect(bar, bd + bk + bmq);
+      bulk_copy_g2s(slot + od0, J.Tw + (size_t)e.z * nWin * 4, bd, bar);
+      bulk_copy_g2s(slot + ok0, J.masks + (size_t)e.z * nWin * 4 * ME, bk, bar);
+      if (nqm) bulk_copy_g2s(slot, J.Tw + (size_t)e.w * nWin * 4, bmq, bar);
+      return;
+    }
+    const int ab = e.x, a = ab / nPair, b = ab % nPair + 1, pos = e.y & 1, nq = e.y >> 2;
     const int comp = pos ? 2 * b : 2 * b - 1;
     const float2* src_q = J.Tw + ((size_t)(1 + ab) * nWin * nWin + (size_t)e.z * nWin * 4);
     const float* src_m = J.masks + ((size_t)(a * nC + comp) * nWin * nWin + (size_t)e.w * nWin * 4) * ME;
@@ -703,7 +747,6 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
   float2 acc[EN];
 #pragma unroll
   for (int i = 0; i < EN; i++) acc[i] = make_float2(0.f, 0.f);
-  b2_band0<N, T2, EN, CM>(J, acc, t, X, Xm);
   for (int s = 0; s < ns; s++) {
     uint64_t* bar = &full[s % depth];
     const uint32_t par = (uint32_t)(s / depth) & 1u;
@@ -718,13 +761,29 @@ __global__ void __launch_bounds__(2 * Cfg<N, ENV, CBV>::CB* Cfg<N, ENV, CBV>::T,
     }
     const int4 e = stg[s];
     const unsigned char* slot = b2s_ring + (size_t)(s % depth) * slot_bytes;
+    if ((e.y & 3) == 2) {  // band 0 from the staged direct and mirrored column quads
+      const int xl = wrap(X - J.win[0]), xlm = wrap(Xm - J.win[0]);
+      const bool mirror_in = xlm < nWin;
+      const float2* tv = reinterpret_cast<const float2*>(slot + od0) + (xl & 3);
+      const float2* tm = reinterpret_cast<const float2*>(slot) +
+                         (mirror_in ? (size_t)((xlm >> 2) - e.w) * nWin * 4 + (xlm & 3) : 0);
+      const float* mk = reinterpret_cast<const float*>(slot + ok0) + (xl & 3) * ME;
+      b2_band0_px<N, T2, EN, CM, true>(acc, t, J.win[1], nWin, tv, tm, mirror_in, mk,
+                                       reinterpret_cast<const float2*>(mk));
+      __syncthreads();  // every thread is done with the slot
+      if (lt == 0 && s + depth < ns) {
+        fence_proxy_async();
+        issue(s + depth);
+      }
+      continue;
+    }
     const int ab = e.x, a = ab / nPair, b = ab % nPair + 1;
     const float2* Qx = J.nyq + (size_t)(ab * 2) * N;
     const float2* sq = reinterpret_cast<const float2*>(slot + oq);
     const float* smk = reinterpret_cast<const float*>(slot + om);
     const float2* sg = reinterpret_cast<const float2*>(slot + og);
     const float2* sy = reinterpret_cast<const float2*>(slot + oy);
-    if (!(e.y & 1)) {
+    if ((e.y & 3) == 0) {
       const int xn = wrap(X - J.win[2 * (a * nC + 2 * b - 1)]);
       if (xn < nWin) {
         const size_t qo = (size_t)((xn >> 2) - e.z) * nWin * 4 + (xn & 3);
