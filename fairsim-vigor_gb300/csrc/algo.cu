@@ -127,16 +127,34 @@ int estimate_core(fsim_sim_param* p, const float2* const* spec, int fit_band, do
     TRY(times_cplx_device(c1, c0, n, true, st));
     TRY(fft2d_device(c1, N, N, false, st));
     const double minDist = fit_exclude * ht.cutoff / vec_cpm;
-    double peak[4];
-    TRY(locate_peak_device(c1, N, N, minDist, s, st, peak));
-    double fit[4];
+    // locatePeak -> fitPeak -> getPeak on the device (no host round trips); the results of
+    // direction a: fit (kx, ky, phase, magnitude) at r[0..3], p1 at r[4..5], p2 at r[6..7]
+    double* r = s.results + 8 * a;
+    TRY(locate_peak_to_fit(c1, N, N, minDist, s, st));
     const int fb = live ? hb : ((fit_band == 1) ? lb : hb);
-    TRY(fit_peak_device(sep, sep + fb * n, N, otf.d, -peak[0], -peak[1], 0.05, 2.5, s, st, fit, nullptr, 0,
-                        live ? 1 : fit_band));
-    std::complex<double> p1, p2;
+    TRY(fit_peak_iterate(sep, sep + fb * n, N, otf.d, 0.05, s, st, r, 0, live ? 1 : fit_band));
     if (live) {
-      const int nBand = nB - 1;
-      TRY(get_peak_device(sep, sep + lb * n, N, otf.d, fit[0] / nBand, fit[1] / nBand, 0.05, s, st, &p1));
+      const int nBand = nB - 1;  // fit / nBand (nBand 1 or 2: exact)
+      TRY(get_peak_at_fit(sep, sep + lb * n, N, otf.d, 0.05, s, st, r, 1.0 / nBand, r + 4));
+    } else if (lb != hb) {
+      // the host doubles the fit for fit band 1: p1 at fit' / 2, p2 at fit'
+      const double f2 = (fit_band == 1) ? 2.0 : 1.0;
+      TRY(get_peak_at_fit(sep, sep + lb * n, N, otf.d, 0.05, s, st, r, f2 / 2, r + 4));
+      TRY(get_peak_at_fit(sep, sep + hb * n, N, otf.d, 0.05, s, st, r, f2, r + 6, 0, 2));
+    } else {
+      TRY(get_peak_at_fit(sep, sep + 1 * n, N, otf.d, 0.05, s, st, r, 1.0, r + 4));
+    }
+  }
+  // one read of every direction's results
+  double res[8 * FSIM_MAX_DIRS];
+  FSIM_CUDA(cudaMemcpyAsync(res, s.results, sizeof(double) * 8 * p->nr_dirs, cudaMemcpyDeviceToHost, st));
+  FSIM_CUDA(cudaStreamSynchronize(st));
+  for (int a = 0; a < p->nr_dirs; a++) {
+    const double* r = res + 8 * a;
+    double fit[4] = {r[0], r[1], r[2], r[3]};
+    const std::complex<double> p1(r[4], r[5]), p2(r[6], r[7]);
+    const int lb = 1, hb = (nB == 3) ? 3 : 1;
+    if (live) {
       p->px[a] = -fit[0] / (nB - 1);
       p->py[a] = -fit[1] / (nB - 1);
       p->pha_off[a] = std::atan2(p1.imag(), p1.real());
@@ -146,15 +164,12 @@ int estimate_core(fsim_sim_param* p, const float2* const* spec, int fit_band, do
         fit[0] *= 2;
         fit[1] *= 2;
       }
-      TRY(get_peak_device(sep, sep + lb * n, N, otf.d, fit[0] / 2, fit[1] / 2, 0.05, s, st, &p1));
-      TRY(get_peak_device(sep, sep + hb * n, N, otf.d, fit[0], fit[1], 0.05, s, st, &p2, 0, 2));
       p->px[a] = -fit[0] / (nB - 1);
       p->py[a] = -fit[1] / (nB - 1);
       p->pha_off[a] = std::atan2(p1.imag(), p1.real());
       p->modulation[a][1] = std::hypot(p1.real(), p1.imag());
       p->modulation[a][2] = std::hypot(p2.real(), p2.imag());
     } else {
-      TRY(get_peak_device(sep, sep + 1 * n, N, otf.d, fit[0], fit[1], 0.05, s, st, &p1));
       p->px[a] = -fit[0] / (nB - 1);
       p->py[a] = -fit[1] / (nB - 1);
       p->pha_off[a] = std::atan2(p1.imag(), p1.real());

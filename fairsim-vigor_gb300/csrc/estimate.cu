@@ -352,6 +352,7 @@ int EstScratch::alloc(int N, cudaStream_t st) {
   if (e == cudaSuccess) e = fsim::dev_alloc_async(&pidx, sizeof(int) * EST_PEAK_BLOCKS, st);
   if (e == cudaSuccess) e = fsim::dev_alloc_async(&red, sizeof(double) * RED_SLOTS, st);
   if (e == cudaSuccess) e = fsim::dev_alloc_async(&fit, sizeof(FitState), st);
+  if (e == cudaSuccess) e = fsim::dev_alloc_async(&results, sizeof(double) * 8 * FSIM_MAX_DIRS, st);
   if (e != cudaSuccess) {
     free(st);
     set_error("estimation scratch for %d x %d: %s", N, N, cudaGetErrorString(e));
@@ -361,7 +362,7 @@ int EstScratch::alloc(int N, cudaStream_t st) {
   return FSIM_OK;
 }
 void EstScratch::free(cudaStream_t st) {
-  void* ps[] = {b0, tx, ty, Q, corr, kbuf, pmag, pidx, red, fit};  // b1 lies inside b0's allocation
+  void* ps[] = {b0, tx, ty, Q, corr, kbuf, pmag, pidx, red, fit, results};  // b1 lies inside b0's allocation
   for (void* p : ps)
     if (p) cudaFreeAsync(p, st);
   b0 = b1 = nullptr;
@@ -372,6 +373,7 @@ void EstScratch::free(cudaStream_t st) {
   pidx = nullptr;
   red = nullptr;
   fit = nullptr;
+  results = nullptr;
   n = 0;
 }
 
@@ -449,6 +451,119 @@ int get_peak_device(const float2* band0, const float2* band1, int N, const OtfTa
   rc = corr_grid_device(s.b0, s.b1, N, &kx, 1, &ky, 1, 0., s, st, c, n2);
   if (rc) return rc;
   *out = c[0];
+  return FSIM_OK;
+}
+
+// ---- the parameter fit's steps chained on the device ------------------------------------------
+// locatePeak's final reduction: the partial maxima in a fixed tree order (the comparison, the
+// larger magnitude and then the smaller index, is a total order, so any order gives the
+// reference's first maximum), the position converted as Correlation.locatePeak does
+// (Correlation.java:159-164) and stored as fitPeak's start (-x, -y), search width 2.5.
+__global__ void __launch_bounds__(EST_PEAK_BLOCKS) k_peak_final(const float* __restrict__ pmag,
+                                                                const int* __restrict__ pidx, int w, int h,
+                                                                FitState* f) {
+  __shared__ float sm[EST_PEAK_BLOCKS];
+  __shared__ int si[EST_PEAK_BLOCKS];
+  const int i = threadIdx.x;
+  sm[i] = pmag[i];
+  si[i] = pidx[i];
+  __syncthreads();
+  for (int o = EST_PEAK_BLOCKS / 2; o > 0; o >>= 1) {
+    if (i < o && (sm[i + o] > sm[i] || (sm[i + o] == sm[i] && si[i + o] < si[i]))) {
+      sm[i] = sm[i + o];
+      si[i] = si[i + o];
+    }
+    __syncthreads();
+  }
+  if (i != 0) return;
+  double xPos = -0., yPos = -1;
+  if (si[0] != 0x7fffffff && sm[0] >= 0) {
+    xPos = si[0] % w;
+    yPos = si[0] / w;
+  }
+  if (xPos > w / 2) xPos = xPos - w;
+  if (yPos > h / 2) yPos = h - yPos;
+  else yPos *= -1;
+  f->kx = -xPos;
+  f->ky = -yPos;
+  f->search = 2.5;
+  f->res_phase = 0;
+  f->res_mag = 0;
+}
+__global__ void k_fit_store(const FitState* __restrict__ f, double* res) {
+  res[0] = f->kx;
+  res[1] = f->ky;
+  res[2] = f->res_phase;
+  res[3] = f->res_mag;
+}
+// getPeak at the fitted shift times a power of two (exact, as the host's divisions)
+__global__ void k_gp_init(FitState* f, const double* __restrict__ res, double scale) {
+  f->kx = res[0] * scale;
+  f->ky = res[1] * scale;
+  f->search = 0;  // the grid's first point is the shift itself
+}
+__global__ void k_gp_store(const double2* __restrict__ corr, double* out2) {
+  out2[0] = corr[0].x;
+  out2[1] = corr[0].y;
+}
+
+int locate_peak_to_fit(const float2* v, int w, int h, double kmin, EstScratch& s, cudaStream_t st) {
+  const long long r2max = (long long)(w / 2) * (w / 2) + (long long)(h / 2) * (h / 2);
+  long long lo = -1, hi = r2max;  // the last r^2 with sqrt((double)r^2) <= kmin
+  while (lo < hi) {
+    const long long m = hi - (hi - lo) / 2;
+    if (std::sqrt((double)m) > kmin) hi = m - 1;
+    else lo = m;
+  }
+  k_peak_partial<<<EST_PEAK_BLOCKS, 256, 0, st>>>(v, w, h, lo, s.pmag, s.pidx);
+  k_peak_final<<<1, EST_PEAK_BLOCKS, 0, st>>>(s.pmag, s.pidx, w, h, s.fit);
+  FSIM_CHECK_LAUNCH();
+  return FSIM_OK;
+}
+
+int fit_peak_iterate(const float2* band0, const float2* band1, int N, const OtfTable* t, double wl, EstScratch& s,
+                     cudaStream_t st, double* res, int bn0, int bn1) {
+  const size_t img = (size_t)N * N * sizeof(float2);
+  FitState* f = s.fit;
+  const float wlf = weight_limit_float(wl);
+  for (int iter = 0; iter < 3; iter++) {
+    k_fit_setup<<<1, 1, 0, st>>>(f, 0.15, N, N);
+    FSIM_CUDA(cudaMemcpyAsync(s.b0, band0, img, cudaMemcpyDeviceToDevice, st));
+    FSIM_CUDA(cudaMemcpyAsync(s.b1, band1, img, cudaMemcpyDeviceToDevice, st));
+    k_common_region_fit<<<dim3(div_up(N, 128), N), 128, 0, st>>>(s.b0, s.b1, N, N, t, f, 0.15, wlf, bn0, bn1);
+    FSIM_CHECK_LAUNCH();
+    int rc = fft2d_device(s.b0, N, N, true, st, 2);  // b0 and b1 (adjacent)
+    if (rc) return rc;
+    const double* n2 = nullptr;
+    rc = norm2_device_async(s.b0, (size_t)N * N, s.red, &n2, st);
+    if (rc) return rc;
+    launch_corr_grid(s.b0, s.b1, N, f->kv, 10, 10, 0., n2, s.tx, s.ty, s.Q, s.corr, st);
+    k_fit_scan<<<1, 128, 0, st>>>(f, s.corr, iter, 0);
+    FSIM_CHECK_LAUNCH();
+  }
+  if (res) k_fit_store<<<1, 1, 0, st>>>(f, res);
+  FSIM_CHECK_LAUNCH();
+  return FSIM_OK;
+}
+
+int get_peak_at_fit(const float2* band0, const float2* band1, int N, const OtfTable* t, double wl, EstScratch& s,
+                    cudaStream_t st, const double* res, double scale, double* out2, int bn0, int bn1) {
+  const size_t img = (size_t)N * N * sizeof(float2);
+  FitState* f = s.fit;
+  k_gp_init<<<1, 1, 0, st>>>(f, res, scale);
+  k_fit_setup<<<1, 1, 0, st>>>(f, 0.15, N, N);
+  FSIM_CUDA(cudaMemcpyAsync(s.b0, band0, img, cudaMemcpyDeviceToDevice, st));
+  FSIM_CUDA(cudaMemcpyAsync(s.b1, band1, img, cudaMemcpyDeviceToDevice, st));
+  k_common_region_fit<<<dim3(div_up(N, 128), N), 128, 0, st>>>(s.b0, s.b1, N, N, t, f, 0.15,
+                                                                weight_limit_float(wl), bn0, bn1);
+  FSIM_CHECK_LAUNCH();
+  int rc = fft2d_device(s.b0, N, N, true, st, 2);
+  if (rc) return rc;
+  const double* n2 = nullptr;
+  if ((rc = norm2_device_async(s.b0, (size_t)N * N, s.red, &n2, st))) return rc;
+  launch_corr_grid(s.b0, s.b1, N, f->kv, 1, 1, 0., n2, s.tx, s.ty, s.Q, s.corr, st);
+  k_gp_store<<<1, 1, 0, st>>>(s.corr, out2);
+  FSIM_CHECK_LAUNCH();
   return FSIM_OK;
 }
 

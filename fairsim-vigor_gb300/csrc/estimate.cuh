@@ -21,6 +21,7 @@ struct EstScratch {
   int* pidx = nullptr;
   double* red = nullptr;  // reduction scratch (RED_SLOTS doubles): norms left on the device
   FitState* fit = nullptr;
+  double* results = nullptr;  // per direction: fitPeak's kx, ky, phase, magnitude; getPeak's p1, p2
   int alloc(int N, cudaStream_t st);
   void free(cudaStream_t st);
 };
@@ -38,6 +39,14 @@ int fit_peak_device(const float2* band0, const float2* band1, int N, const OtfTa
                     int bn1 = 1);
 int get_peak_device(const float2* band0, const float2* band1, int N, const OtfTable* t, double kx, double ky, double wl,
                     EstScratch& s, cudaStream_t st, std::complex<double>* out, int bn0 = 0, int bn1 = 1);
+// The same three steps without host round trips, chained through the device fit state:
+// locatePeak leaves fitPeak's start (-peak) in it, fitPeak's result is stored at res[0..3],
+// getPeak at (res[0], res[1]) * scale writes its correlation to out2 (two doubles).
+int locate_peak_to_fit(const float2* v, int w, int h, double kmin, EstScratch& s, cudaStream_t st);
+int fit_peak_iterate(const float2* band0, const float2* band1, int N, const OtfTable* t, double wl, EstScratch& s,
+                     cudaStream_t st, double* res, int bn0 = 0, int bn1 = 1);
+int get_peak_at_fit(const float2* band0, const float2* band1, int N, const OtfTable* t, double wl, EstScratch& s,
+                    cudaStream_t st, const double* res, double scale, double* out2, int bn0 = 0, int bn1 = 1);
 
 // SimAlgorithm.estimateParameters (live=false) or ParameterRefitThread.doRefit (live=true)
 // on device spectra spec[a*nP + p] (N x N complex); updates p's shifts/phases/modulations.
