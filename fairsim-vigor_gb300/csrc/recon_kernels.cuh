@@ -66,11 +66,9 @@ __device__ __forceinline__ int paste_src(int X) {
 }
 
 // ---- pass A: rows ----------------------------------------------------------------------------
-// 64-thread blocks at up to 8 elements per thread: ask for 20 resident blocks (51
-// registers) so that registers, not only shared memory, allow 40 warps per SM.
-// Register budgets (the compiler otherwise keeps 90-230 registers per thread in the longer
-// radix plans, which caps occupancy at a few warps per scheduler): 48 per thread for the
-// 64-thread row blocks of 8 elements, 64 for longer rows at 8 elements, 96 at 12 elements.
+// Register budgets (registers per thread; the compiler otherwise keeps 90-230 registers per
+// thread in the longer radix plans, which caps occupancy at a few warps per scheduler):
+// 64 per thread at up to 8 elements per thread (32 warps per SM), 96 at 12 elements.
 template <int T, int EN>
 __host__ __device__ constexpr int pass_a_min_blocks() {
   return EN <= 8 ? (65536 / (T * FSIM_PA_REGS) > 0 ? 65536 / (T * FSIM_PA_REGS) : 1)
@@ -123,29 +121,77 @@ __device__ __forceinline__ void damp_row(const JobDesc& J, size_t row, int t, fl
   }
 }
 
+// Rows per pass-A block: the rows of a block share the job descriptor and the separation
+// coefficients, and write their windows together, so that each quad of the quad layout
+// (4 columns x RB rows) is one contiguous run of RB * 32 bytes instead of one 32-byte piece
+// per row and quad (global store wavefronts 1.21 M -> 0.55 M per 16 datasets of 512^2 3x3 at
+// four rows). Up to 128 threads per block: the rows meet at the block's barriers (the
+// transforms' exchanges included), and at 256 threads those waits cost more than the store
+// wavefronts save (pass A 0.568 ms per 64 datasets at two rows of 64 threads, 0.572 at one,
+// 0.599 at four; 0.582 at four with one named barrier per row, which also holds the block to
+// four per SM). The row buffers are RS float2 apart, RS = 4 (mod 16) for RB >= 4 and
+// 8 (mod 16) for RB = 2, so that a half-warp of the read-out (RB >= 4: four rows x four
+// columns; RB = 2: two rows x two quads) reads 16 distinct bank pairs.
+__host__ __device__ constexpr int pass_a_row_stride(int N, int RB) {
+  const int s = smem_line_elems(N, 1), m = RB >= 4 ? 4 : 8;
+  return s + ((m - s % 16) % 16 + 16) % 16;
+}
+__host__ __device__ constexpr int pass_a_rows(int N, int T) {
+  int rb = 1;
+  while (2 * rb * T <= 128 && N % (2 * rb) == 0 && 2 * (2 * rb) * pass_a_row_stride(N, 2 * rb) * 8 <= 44 * 1024)
+    rb *= 2;
+  return rb;
+}
 template <int N, int ENV>
-__global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>::T, Cfg<N, ENV>::EN>())
+struct PassA {
+  static constexpr int T = Cfg<N, ENV>::T;
+  static constexpr int RB = pass_a_rows(N, T);
+  static constexpr int RS = pass_a_row_stride(N, RB);
+  static constexpr int NT = RB * T;  // threads per block
+};
+
+template <int N, int ENV>
+__global__ void __launch_bounds__(PassA<N, ENV>::NT, pass_a_min_blocks<PassA<N, ENV>::NT, Cfg<N, ENV>::EN>())
     k_pass_a(const JobDesc* __restrict__ jobs) {
   using P = Cfg<N, ENV>;
-  constexpr int W = P::W, T = P::T, EN = P::EN;
-  const int y = blockIdx.x, a = blockIdx.y, t = threadIdx.x;
+  using PA = PassA<N, ENV>;
+  constexpr int W = P::W, T = P::T, EN = P::EN, RB = PA::RB, RS = PA::RS, NT = PA::NT;
+  const int tid = threadIdx.x, g = tid / T, t = tid % T;
+  const int y0 = blockIdx.x * RB, y = y0 + g, a = blockIdx.y;
   __shared__ JobDesc J;
-  __shared__ float2 bz[smem_line_elems(N, 1)], bh[smem_line_elems(N, 1)];
+  __shared__ float2 sbz[RB * RS], sbh[RB * RS];
   __shared__ float2 coef[FSIM_MAX_DIRS * FSIM_MAX_PHASES];
+  float2* bz = sbz + g * RS;  // this row group's buffers
+  float2* bh = sbh + g * RS;
   const float2* twN = g_stw + stw_offset(N, EN);  // stage table, read through L1
   const float2* twW = g_tw + tw_offset(W);
-  load_job(&J, jobs + blockIdx.z, t, T);
+  const JobDesc* jg = jobs + blockIdx.z;
+  load_job(&J, jg, tid, NT);
+  // the counts and the separation coefficients straight from the descriptor in global
+  // memory, so that one barrier covers both shared-memory copies
+  const int nA = jg->nA, nP = jg->nP, nC = jg->nC, nPair = (nC - 1) / 2;
+  if (a > nA || (a < nA && nPair == 0)) return;  // uniform per block; one band: band 0 only
+  if (a == nA) {
+    for (int i = tid; i < nA * nP; i += NT) coef[i] = jg->coef[((i / nP) * nC) * nP + i % nP];
+  } else {
+    for (int i = tid; i < nC * nP; i += NT) coef[i] = jg->coef[a * nC * nP + i];
+  }
   __syncthreads();
-  if (a > J.nA) return;  // uniform per block
-  const int nA = J.nA, nP = J.nP, nC = J.nC, nPair = (nC - 1) / 2;
   const size_t frame = (size_t)N * N, row = (size_t)y * N;
+  // Window read-out of the block's RB rows: element idx = (quad q, row r, column j) with
+  // (r, j) fastest, stored at ((q * N + y0) * 4 + 4 r + j) of the quad layout.
+  auto window_pos = [&](int idx, int& q, int& r, int& xl) {
+    q = idx / (4 * RB);
+    const int rem = idx - q * 4 * RB;
+    r = rem >> 2;
+    xl = 4 * q + (rem & 3);
+    return ((size_t)q * N + y0) * 4 + rem;
+  };
   if (a == nA) {
     // Band 0 is summed over the angles before the column pass, and its band separation
-    // and row FFT are linear: one block per row mixes the band-0 rows of every angle and
+    // and row FFT are linear: one row group per row mixes the band-0 rows of every angle and
     // transforms the sum once into slot 0 (band 0 has no shift: one window for all angles).
     const int nF = nA * nP;
-    for (int i = t; i < nF; i += T) coef[i] = J.coef[((i / nP) * nC) * nP + i % nP];
-    __syncthreads();
     float2 x[EN];
 #pragma unroll
     for (int i = 0; i < EN; i++) x[i] = make_float2(0.f, 0.f);
@@ -164,20 +210,19 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     line_fft_reg<N, T, 1, false>(x, bh, 0, t, twN);
 #pragma unroll
     for (int i = 0; i < EN; i++) bh[t + i * T] = x[i];
-    __syncthreads();
+    __syncthreads();  // the read-out reads every row group's buffer
     const int Xs = J.win[0];
-    for (int xl = t; xl < J.nWin; xl += T) {
+    for (int idx = tid; idx < J.nWin * RB; idx += NT) {
+      int q, r, xl;
+      const size_t o = window_pos(idx, q, r, xl);
       int X = Xs + xl;
       if (X >= W) X -= W;
       const int m = paste_src<N>(X);
-      J.I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = m >= 0 ? bh[m] : make_float2(0.f, 0.f);
+      J.I[o] = m >= 0 ? sbh[r * RS + m] : make_float2(0.f, 0.f);
     }
-    if (y == 0 && t == 0) *J.clip_max = 0.f;  // CLIPSCALE.BOTH: pass C takes the maximum from 0
+    if (y0 == 0 && tid == 0) *J.clip_max = 0.f;  // CLIPSCALE.BOTH: pass C takes the maximum from 0
     return;
   }
-  if (nPair == 0) return;  // one band: the band-0 block above is the whole row pass
-  for (int i = t; i < nC * nP; i += T) coef[i] = J.coef[a * nC * nP + i];
-  __syncthreads();
   // band separation in real space of component cm for this thread's elements t + i*T: the
   // phases outer, so that every element's load of a phase row is in flight at once (pass A
   // 0.61 ms per 64 datasets of 512^2 3x3, 0.94 ms with the elements outer and one load in
@@ -221,7 +266,7 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
   for (int b = 1; b <= nPair; b++) {
     const int cn = 2 * b - 1;
     mix(cn, x);
-    __syncthreads();  // the previous window reads of bh and bz are done
+    if (b > 1) __syncthreads();  // the previous pair's read-out of every row group's buffers is done
     // the mixed row waits in bz (each thread its own elements) for the even-sample product
     // below, instead of in 16 registers across the three transforms of the odd samples
 #pragma unroll
@@ -249,15 +294,17 @@ __global__ void __launch_bounds__(Cfg<N, ENV>::T, pass_a_min_blocks<Cfg<N, ENV>:
     line_fft_reg<N, T, 1, false>(x, bz, 0, t, twN);
 #pragma unroll
     for (int i = 0; i < EN; i++) bz[t + i * T] = x[i];
-    __syncthreads();
+    __syncthreads();  // the read-out reads every row group's buffers
     // neg window of the shifted spectrum: E[X mod N] + exp(-2 pi i X/W) O[X mod N]
     const int Xs = J.win[2 * (a * nC + cn)];
     float2* I = J.I + (size_t)(1 + a * nPair + (b - 1)) * J.nWin * N;  // slot of (a, b)
-    for (int xl = t; xl < J.nWin; xl += T) {
+    for (int idx = tid; idx < J.nWin * RB; idx += NT) {
+      int q, r, xl;
+      const size_t o = window_pos(idx, q, r, xl);
       int X = Xs + xl;
       if (X >= W) X -= W;
       const int m = X < N ? X : X - N;
-      I[((size_t)(xl >> 2) * N + y) * 4 + (xl & 3)] = cadd(bz[m], cmul(twW[X], bh[m]));
+      I[o] = cadd(sbz[r * RS + m], cmul(twW[X], sbh[r * RS + m]));
     }
   }
 }
@@ -837,8 +884,9 @@ __global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::T) k_pass_c(const JobDesc*
   const int g = threadIdx.x / T, t = threadIdx.x % T;
   const int y = blockIdx.x * G + g;
   __shared__ float2 sm[G * smem_line_elems(N, 1)];
-  __shared__ float2 tw[stw_len(N, EN)];
-  stage_stage_twiddles<N, EN>(tw, threadIdx.x, G * T);
+  // stage twiddles through L1 (a per-block shared copy of the 511-entry table cost a 4 KB
+  // copy and a barrier per pair of rows)
+  const float2* tw = g_stw + stw_offset(N, EN);
   float2* s = sm + g * smem_line_elems(N, 1);
   const float2* twW = g_tw + tw_offset(W);
   const float2* row = J.O + (size_t)y * N;
@@ -852,7 +900,6 @@ __global__ void __launch_bounds__(Cfg<N>::GC* Cfg<N>::T) k_pass_c(const JobDesc*
     const float2 e = cadd(h, hm), d = cmul(csub(h, hm), cconjf(twW[k]));
     x[i] = make_float2(e.x - d.y, e.y + d.x);  // e + i d
   }
-  __syncthreads();  // the twiddle table is staged
   line_fft_reg<N, T, 1, true>(x, s, 0, t, tw);
   const float scale = 1.f / ((float)W * (float)W);
   const int clip = J.clip;
@@ -894,9 +941,10 @@ static __global__ void k_scale_clip(const JobDesc* __restrict__ jobs, int W) {
 // A, G, B1, B2, C in order on one stream.
 template <int N, int ENA>
 static void launch_a(const JobDesc* d_jobs, int njobs, int maxA, int maxPair, cudaStream_t st) {
-  using PA = Cfg<N, ENA>;
-  // blockIdx.y: the angles' band pairs, then (y == nA) the band-0 row of all angles
-  k_pass_a<N, ENA><<<dim3(N, maxA + 1, njobs), PA::T, 0, st>>>(d_jobs);
+  using PAR = PassA<N, ENA>;
+  // blockIdx.x: RB rows; blockIdx.y: the angles' band pairs, then (y == nA) the band-0 rows
+  // of all angles
+  k_pass_a<N, ENA><<<dim3(N / PAR::RB, maxA + 1, njobs), PAR::NT, 0, st>>>(d_jobs);
 }
 
 template <int N, int ENA>
