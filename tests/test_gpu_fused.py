@@ -651,6 +651,30 @@ def test_recon_batch_host_widefield(fs, torch_cuda):
             assert np.array_equal(f.numpy(), single[2])
 
 
+@pytest.mark.parametrize("layout", ["one_array", "separate"])
+def test_recon_batch_host_merged_copies(fs, torch_cuda, layout):
+    """Stacks whose host buffers are one page-locked array move as one copy per chunk and
+    direction; buffers in separate allocations (adjacent or not) are copied one by one. Both
+    give the same bits as each stack reconstructed alone."""
+    torch = torch_cuda
+    n, B = 256, 6
+    raw0, truth, sp = make(fs, n, seed=150)
+    p = fs.plan.ReconPlan(sp, path=fs.native.PATH_OFFLINE, input_type=fs.native.INPUT_F32, fade_px=10)
+    g = np.random.default_rng(150)
+    raws = [np.ascontiguousarray(raw0 * np.float32(1 + 0.1 * i) + g.random(raw0.shape, np.float32)) for i in range(B)]
+    singles = [p.reconstruct_host(r) for r in raws]
+    if layout == "one_array":
+        h_raw_all = torch.from_numpy(np.stack(raws)).pin_memory()
+        h_out_all = torch.empty((B, 2 * n, 2 * n), dtype=torch.float32).pin_memory()
+        h_raw, h_out = list(h_raw_all), list(h_out_all)
+    else:
+        h_raw = [torch.from_numpy(r).pin_memory() for r in raws]
+        h_out = [torch.empty((2 * n, 2 * n), dtype=torch.float32).pin_memory() for _ in range(B)]
+    fs.plan.recon_batch_host([(p, r.data_ptr(), o.data_ptr()) for r, o in zip(h_raw, h_out)], chunk=3)
+    for o, s in zip(h_out, singles):
+        assert np.array_equal(o.numpy(), s)
+
+
 def test_plan_from_saved_config(fs, oracle, tmp_path):
     """A parameter set written as the reference's XML (SimParam.saveConfig,
     OtfProvider.saveConfig), read back and used for a plan: the reconstruction matches the
