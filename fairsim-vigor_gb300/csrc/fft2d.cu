@@ -6,6 +6,9 @@
 // Each pass reads and writes the array once (16 bytes per complex element per pass).
 // Twiddles come from the per-stage tables (one to three loads per butterfly, the other
 // powers by products), read through L1; lines enter and leave the transform in registers.
+#include <algorithm>
+#include <cstdint>
+
 #include "common.cuh"
 #include "fft_line.cuh"
 #include "runtime.cuh"
@@ -93,6 +96,74 @@ static int launch_rows(float2* d, int nrows, int batch, size_t stride, float sca
   return FSIM_OK;
 }
 
+// Column pass with the next tile's loads in flight during this tile's transform: a
+// persistent block (two per SM) walks tiles of C columns x L rows; while it transforms one,
+// cp.async (16-byte copies, no registers held) fills the other of two shared-memory tile
+// buffers. The plain column pass keeps only the loads of its own 8 elements per thread in
+// flight and waits on them (long-scoreboard stalls, 45% of DRAM peak at 64 x 512^2).
+// Requires C | ncols and 16-byte aligned rows (the launcher checks); used for 512-point
+// columns (8 columns x 512 rows per tile, two 32 KB tile buffers per block).
+template <int L>
+struct ColPipe {
+  static constexpr int C = LinePlan<L>::C, T = LinePlan<L>::T, NT = C * T;
+  static constexpr int TILE = L * C;                           // float2 per tile buffer
+  static constexpr int CHUNKS = TILE / 2;                      // 16-byte copies per tile
+  static constexpr int PER_THREAD = CHUNKS / NT;               // copies per thread
+  static constexpr size_t SMEM = sizeof(float2) * (2 * TILE + smem_line_elems(L, C));
+  static_assert(CHUNKS % NT == 0 && (C * 8) % 16 == 0, "tile copies");
+};
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+template <int L, bool INV>
+__global__ void __launch_bounds__(ColPipe<L>::NT, 2)
+    k_fft_cols_pipe(float2* __restrict__ data, int ncols, int batch, size_t item_stride, float scale) {
+  using P = ColPipe<L>;
+  constexpr int T = P::T, C = P::C, NT = P::NT, E = L / T;
+  extern __shared__ float4 smem4[];
+  float2* buf = reinterpret_cast<float2*>(smem4);  // [2][L][C]
+  float2* s = buf + 2 * P::TILE;                  // exchanges of the transform
+  const int lt = threadIdx.x, c = lt % C, t = lt / C;
+  const int tiles_per_item = ncols / C, ntiles = tiles_per_item * batch;
+  // copy k of a tile: row k / (C/2), 16-byte piece k % (C/2) of the row's C columns
+  auto issue = [&](int tile, float2* dst) {
+    const float2* base = data + (size_t)(tile / tiles_per_item) * item_stride + (size_t)(tile % tiles_per_item) * C;
+#pragma unroll
+    for (int j = 0; j < P::PER_THREAD; j++) {
+      const int k = lt + j * NT, r = k / (C / 2), q = k % (C / 2);
+      cp_async16(dst + r * C + 2 * q, base + (size_t)r * ncols + 2 * q);
+    }
+  };
+  int tile = blockIdx.x, cur = 0;
+  if (tile < ntiles) issue(tile, buf);
+  cp_async_commit();
+  for (; tile < ntiles; tile += gridDim.x, cur ^= 1) {
+    const int next = tile + gridDim.x;
+    if (next < ntiles) issue(next, buf + (cur ^ 1) * P::TILE);
+    cp_async_commit();
+    cp_async_wait<1>();  // this tile's copies (all but the group just committed) have landed
+    __syncthreads();
+    const float2* tb = buf + cur * P::TILE;
+    float2 v[E];  // element t + i*T of column c of the tile
+#pragma unroll
+    for (int i = 0; i < E; i++) v[i] = tb[(t + i * T) * C + c];
+    // the transform's barriers also order these reads before the tile buffer is refilled
+    // (two tiles later)
+    line_fft_reg<L, T, C, INV>(v, s, c, t, g_stw + stw_offset(L, E));
+    float2* out = data + (size_t)(tile / tiles_per_item) * item_stride + (size_t)(tile % tiles_per_item) * C + c;
+#pragma unroll
+    for (int i = 0; i < E; i++) out[(size_t)(t + i * T) * ncols] = cscale(v[i], scale);
+  }
+  cp_async_wait<0>();
+}
+
 template <int L, bool INV>
 constexpr auto cols_kernel() {
   if constexpr (LinePlan<L>::E <= 8) return k_fft_cols<L, INV>;
@@ -102,6 +173,25 @@ constexpr auto cols_kernel() {
 template <int L, bool INV>
 static int launch_cols(float2* d, int ncols, int batch, size_t stride, float scale, cudaStream_t st) {
   using P = LinePlan<L>;
+  if constexpr (L == 512) {
+    // the pipelined pass where its 16-byte copies are aligned and a batch has at least
+    // as many tiles as two blocks per SM
+    using Q = ColPipe<L>;
+    const long long tiles = (long long)(ncols / Q::C) * batch;
+    if (ncols % Q::C == 0 && ((uintptr_t)d % 16) == 0 && (stride * sizeof(float2)) % 16 == 0 &&
+        ((size_t)ncols * sizeof(float2)) % 16 == 0 && tiles >= 2LL * ctx().num_sms) {
+      static bool attr = false;
+      if (!attr) {
+        FSIM_CUDA(cudaFuncSetAttribute(k_fft_cols_pipe<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)Q::SMEM));
+        attr = true;
+      }
+      const int grid = (int)std::min<long long>(tiles, 2LL * ctx().num_sms);
+      k_fft_cols_pipe<L, INV><<<grid, Q::NT, Q::SMEM, st>>>(d, ncols, batch, stride, scale);
+      FSIM_CHECK_LAUNCH();
+      return FSIM_OK;
+    }
+  }
   size_t smem = sizeof(float2) * (size_t)smem_line_elems(L, P::C);
   auto kern = cols_kernel<L, INV>();
   static bool attr = false;

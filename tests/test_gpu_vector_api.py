@@ -270,7 +270,9 @@ def test_accel_natives_set_get_reshape_plan_buffers(fs, V):
     fs.native.check(lib.fsim_profiler(0))
 
 
-@pytest.mark.parametrize("w,h,batch", [(64, 64, 3), (384, 384, 2), (512, 256, 4)])
+# (512, 512, 6) and (256, 512, 12): the 512-point column pass with cp.async-pipelined tiles
+# (at least two tiles per SM); the others the plain column pass
+@pytest.mark.parametrize("w,h,batch", [(64, 64, 3), (384, 384, 2), (512, 256, 4), (512, 512, 6), (256, 512, 12)])
 def test_fft2d_batch_on_device_buffers(fs, V, w, h, batch):
     import ctypes as C
 
