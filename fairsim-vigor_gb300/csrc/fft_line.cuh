@@ -8,8 +8,11 @@
 //
 // Radices 16, 8, 4, 2 (and one radix-3 stage for 3*2^k lengths) are picked at compile
 // time so that R divides both the remaining length and E, giving 3 stages for 512..4096
-// with E = 16. Twiddles come from an accurate table exp(-2*pi*i*m/L) computed in double on
-// the host (tw_all), not from fast-math intrinsics.
+// with E = 16. Twiddles come from per-stage tables (g_stw: one to three entries per
+// butterfly, the other powers by products) computed in double on the host, not from
+// fast-math intrinsics; the plain table g_tw (exp(-2 pi i m/L)) serves the callers' shift
+// and window factors. Lines either stay in shared memory (line_fft_st) or enter and leave
+// the transform in registers (line_fft_reg, the register-chained form below).
 //
 // Forward = exp(-2 pi i jk/L) (unscaled); inverse = exp(+2 pi i jk/L) (unscaled; callers
 // apply 1/(w*h) where fairSIM's complexInverse(scale=true) does).
@@ -240,41 +243,32 @@ __device__ __forceinline__ void dft(float2* v) {
 __host__ __device__ constexpr int pick_radix(int rem, int E) { return pick_radix_fwd(rem, E); }
 
 // ---- one Stockham stage ---------------------------------------------------------
-template <int L, int T, int C, int R, int NS, bool INV, int TS, int M = 1>
+// C interleaved lines in shared memory (padded layout sidx), stage tables [r-1][k] of this
+// stage (tw points at the stage's first entry).
+template <int L, int T, int C, int R, int NS, bool INV>
 __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2* tw) {
-  // TS > 0: plain table exp(-2 pi i m/(L*TS)) read at stride TS; TS == 0: stage table
-  // [r-1][k] of this stage (tw points at the stage's first entry).
-  // M > 1: the thread transforms M adjacent lines c*M .. c*M+M-1 of C*M interleaved lines,
-  // with one set of twiddles for all of them.
-  constexpr int E = L / T, NB = E / R, LR = L / R, CL = C * M;
+  constexpr int E = L / T, NB = E / R, LR = L / R;
   // The twiddle loads depend only on the thread's index: issue them first, so that their
   // latency overlaps the shared-memory reads and the barrier.
-  constexpr int NT = NS > 1 ? (TS > 0 ? R - 1 : (R == 16 ? 3 : (R >= 8 || R == 3 ? 2 : 1))) : 1;
+  constexpr int NT = NS > 1 ? (R == 16 ? 3 : (R >= 8 || R == 3 ? 2 : 1)) : 1;
   float2 tl[NB][NT];
   if constexpr (NS > 1) {
 #pragma unroll
     for (int b = 0; b < NB; b++) {
       const int k = (t + b * T) % NS;
-      if constexpr (TS > 0) {
-#pragma unroll
-        for (int r = 1; r < R; r++) tl[b][r - 1] = tw[r * k * (L / (NS * R)) * TS];
-      } else {
-        // stage table [r-1][k]: W^k, W^2k (radix 3), W^4k (radix 8/16), W^8k (radix 16)
-        tl[b][0] = tw[k];
-        if constexpr (R == 3) tl[b][1] = tw[NS + k];
-        if constexpr (R >= 8) tl[b][1] = tw[3 * NS + k];
-        if constexpr (R == 16) tl[b][2] = tw[7 * NS + k];
-      }
+      // stage table [r-1][k]: W^k, W^2k (radix 3), W^4k (radix 8/16), W^8k (radix 16)
+      tl[b][0] = tw[k];
+      if constexpr (R == 3) tl[b][1] = tw[NS + k];
+      if constexpr (R >= 8) tl[b][1] = tw[3 * NS + k];
+      if constexpr (R == 16) tl[b][2] = tw[7 * NS + k];
     }
   }
-  float2 v[NB][M][R];
+  float2 v[NB][R];
 #pragma unroll
   for (int b = 0; b < NB; b++) {
     const int j = t + b * T;
 #pragma unroll
-    for (int l = 0; l < M; l++)
-#pragma unroll
-      for (int r = 0; r < R; r++) v[b][l][r] = s[sidx((j + r * LR) * CL + c * M + l)];
+    for (int r = 0; r < R; r++) v[b][r] = s[sidx((j + r * LR) * C + c)];
   }
   __syncthreads();
 #pragma unroll
@@ -282,46 +276,37 @@ __device__ __forceinline__ void fft_stage(float2* s, int c, int t, const float2*
     const int j = t + b * T;
     const int k = j % NS;
     if constexpr (NS > 1) {
+      // the remaining powers by products (at most three roundings beyond the table's)
       float2 w[R];
-      if constexpr (TS > 0) {
+      w[1] = tl[b][0];
+      if constexpr (R == 3) w[2] = tl[b][1];
+      if constexpr (R == 4) {
+        w[2] = cmul(w[1], w[1]);
+        w[3] = cmul(w[2], w[1]);
+      }
+      if constexpr (R >= 8) {
+        w[4] = tl[b][1];
+        w[2] = cmul(w[1], w[1]);
+        w[3] = cmul(w[2], w[1]);
 #pragma unroll
-        for (int r = 1; r < R; r++) w[r] = tl[b][r - 1];
-      } else {
-        // the remaining powers by products (at most three roundings beyond the table's)
-        w[1] = tl[b][0];
-        if constexpr (R == 3) w[2] = tl[b][1];
-        if constexpr (R == 4) {
-          w[2] = cmul(w[1], w[1]);
-          w[3] = cmul(w[2], w[1]);
-        }
-        if constexpr (R >= 8) {
-          w[4] = tl[b][1];
-          w[2] = cmul(w[1], w[1]);
-          w[3] = cmul(w[2], w[1]);
+        for (int r = 5; r < 8; r++) w[r] = cmul(w[4], w[r - 4]);
+      }
+      if constexpr (R == 16) {
+        w[8] = tl[b][2];
 #pragma unroll
-          for (int r = 5; r < 8; r++) w[r] = cmul(w[4], w[r - 4]);
-        }
-        if constexpr (R == 16) {
-          w[8] = tl[b][2];
-#pragma unroll
-          for (int r = 9; r < 16; r++) w[r] = cmul(w[8], w[r - 8]);
-        }
+        for (int r = 9; r < 16; r++) w[r] = cmul(w[8], w[r - 8]);
       }
 #pragma unroll
       for (int r = 1; r < R; r++) {
         float2 ww = w[r];
         if (INV) ww.y = -ww.y;
-#pragma unroll
-        for (int l = 0; l < M; l++) v[b][l][r] = cmul(v[b][l][r], ww);
+        v[b][r] = cmul(v[b][r], ww);
       }
     }
     const int base = (j / NS) * NS * R + k;
+    dft<R, INV>(v[b]);
 #pragma unroll
-    for (int l = 0; l < M; l++) {
-      dft<R, INV>(v[b][l]);
-#pragma unroll
-      for (int r = 0; r < R; r++) s[sidx((base + r * NS) * CL + c * M + l)] = v[b][l][r];
-    }
+    for (int r = 0; r < R; r++) s[sidx((base + r * NS) * C + c)] = v[b][r];
   }
   __syncthreads();
 }
@@ -419,63 +404,24 @@ __device__ __forceinline__ void line_fft_reg(float2 (&x)[L / T], float2* s, int 
   fft_stages_reg<L, T, C, INV, 1>(x, s, c, t, stw);
 }
 
-template <int L, int T, int C, bool INV, int NS, int TS, int M = 1>
+template <int L, int T, int C, bool INV, int NS>
 __device__ __forceinline__ void fft_stages(float2* s, int c, int t, const float2* tw) {
   if constexpr (NS < L) {
     constexpr int R = pick_radix(L / NS, L / T);
     static_assert((L / NS) % R == 0 && (L / T) % R == 0, "bad radix plan");
-    fft_stage<L, T, C, R, NS, INV, TS, M>(s, c, t, tw);
+    fft_stage<L, T, C, R, NS, INV>(s, c, t, tw);
     // stage tables: the next stage's entries follow this stage's (R-1)*NS entries
-    fft_stages<L, T, C, INV, NS * R, TS, M>(s, c, t, TS > 0 ? tw : tw + (R - 1) * NS);
+    fft_stages<L, T, C, INV, NS * R>(s, c, t, tw + (R - 1) * NS);
   }
 }
 
-// Transform C interleaved lines of length L in place in shared memory `s`.
+// Transform C interleaved lines of length L in place in shared memory `s` (element k of
+// line c at s[sidx(k*C + c)]) with per-stage twiddle tables (g_stw layout, read through L1).
 // Called by exactly C*T threads (the whole block): it contains __syncthreads.
-// Twiddles come from the accurate global table by default, or from a copy of the
-// length-LT table in shared memory (tw_smem, LT a multiple of L) when the caller staged one.
 template <int L, int T, int C, bool INV>
-__device__ __forceinline__ void line_fft(float2* s, int lt) {
-  static_assert(supported_len(L), "unsupported FFT length");
-  static_assert(plan_ok(L, T), "L/T must be divisible by every radix");
-  fft_stages<L, T, C, INV, 1, 1>(s, lt % C, lt / C, g_tw + tw_offset(L));
-}
-template <int L, int T, int C, bool INV, int LT>
-__device__ __forceinline__ void line_fft_tw(float2* s, int lt, const float2* tw_smem) {
-  static_assert(supported_len(L) && LT % L == 0, "unsupported FFT length / table");
-  static_assert(plan_ok(L, T), "L/T must be divisible by every radix");
-  fft_stages<L, T, C, INV, 1, LT / L>(s, lt % C, lt / C, tw_smem);
-}
-// Line FFT with per-stage twiddle tables (g_stw layout) staged in shared memory by
-// stage_stage_twiddles<L, L/T>.
-template <int L, int T, int C, bool INV>
-__device__ __forceinline__ void line_fft_st(float2* s, int lt, const float2* stw_smem) {
+__device__ __forceinline__ void line_fft_st(float2* s, int lt, const float2* stw) {
   static_assert(supported_len(L) && plan_ok(L, T) && stw_ok(L, L / T), "no stage table for this plan");
-  fft_stages<L, T, C, INV, 1, 0>(s, lt % C, lt / C, stw_smem);
-}
-// C*M interleaved lines by C*T threads, M adjacent lines per thread (stage tables).
-template <int L, int T, int C, int M, bool INV>
-__device__ __forceinline__ void line_fft_st_m(float2* s, int lt, const float2* stw) {
-  static_assert(supported_len(L) && plan_ok(L, T) && stw_ok(L, L / T), "no stage table for this plan");
-  fft_stages<L, T, C, INV, 1, 0, M>(s, lt % C, lt / C, stw);
-}
-// One line `c` of CL interleaved lines, by T threads (lane t).
-template <int L, int T, int CL, bool INV>
-__device__ __forceinline__ void line_fft_st_one(float2* s, int c, int t, const float2* stw) {
-  static_assert(supported_len(L) && plan_ok(L, T) && stw_ok(L, L / T), "no stage table for this plan");
-  fft_stages<L, T, CL, INV, 1, 0>(s, c, t, stw);
-}
-template <int L, int E>
-__device__ __forceinline__ void stage_stage_twiddles(float2* dst, int tid, int nthreads) {
-  static_assert(stw_ok(L, E), "no stage table for this plan");
-  const float2* g = g_stw + stw_offset(L, E);
-  for (int i = tid; i < stw_len(L, E); i += nthreads) dst[i] = g[i];
-}
-// Stage the exp(-2 pi i m / LT) table into shared memory (all threads of the block).
-template <int LT>
-__device__ __forceinline__ void stage_twiddles(float2* tw_smem, int tid, int nthreads) {
-  const float2* g = g_tw + tw_offset(LT);
-  for (int i = tid; i < LT; i += nthreads) tw_smem[i] = g[i];
+  fft_stages<L, T, C, INV, 1>(s, lt % C, lt / C, stw);
 }
 
 }  // namespace fsim
