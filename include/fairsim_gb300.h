@@ -249,8 +249,10 @@ int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t w
  * passes and downloads of successive chunks of `chunk` jobs
  * overlap on three library-owned streams (chunk 0 = about 40 MiB of raw frames); returns
  * when every output is in host memory.
- * Page-locked host buffers are copied by DMA; pageable ones copy synchronously. One call
- * runs at a time per process (others wait). */
+ * Page-locked host buffers are copied by DMA; pageable ones copy synchronously. Jobs whose
+ * host buffers follow one another in one allocation (one array of stacks, one of images)
+ * move as one copy per chunk and direction. One call runs at a time per process (others
+ * wait). */
 typedef struct fsim_host_job {
   const fsim_plan* plan;
   const void* raw_host;  /* nr_dirs*nr_phases frames, w*w each, f32 or u16 */
