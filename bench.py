@@ -178,7 +178,7 @@ def run_reference(args):
 # L2); per-launch traffic = this x the batch size. G+B1 counts B1 (G moves 0.04 MB). Pass C is
 # left out: at batch 16 its input, the Hermitian halves pass B2 has just written (67 MB), is
 # still in L2, so the capture does not show its DRAM traffic at batch 64.
-TRAFFIC_PER_DATASET = {"k_pass_a<512>": 16.02e6, "k_pass_g+k_pass_b1<512>": 11.21e6, "k_pass_b2<512>": 14.20e6,
+TRAFFIC_PER_DATASET = {"k_pass_a<512>": 15.99e6, "k_pass_g+k_pass_b1<512>": 11.21e6, "k_pass_b2<512>": 14.20e6,
                        "k_pass_c<512>": None}
 PASS_NAMES = ["k_pass_a<512>", "k_pass_g+k_pass_b1<512>", "k_pass_b2<512>", "k_pass_c<512>"]
 

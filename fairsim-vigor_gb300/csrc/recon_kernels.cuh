@@ -148,6 +148,8 @@ struct PassA {
   static constexpr int RB = pass_a_rows(N, T);
   static constexpr int RS = pass_a_row_stride(N, RB);
   static constexpr int NT = RB * T;  // threads per block
+  static_assert(RS >= smem_line_elems(N, 1) && (RB == 1 || RS % 16 == (RB >= 4 ? 4 : 8)),
+                "row buffers: a transform's scratch, read-out half-warps on distinct bank pairs");
 };
 
 template <int N, int ENV>
