@@ -145,12 +145,12 @@ extern "C" int fsim_recon_batch_host(const fsim_host_job* jobs, int n_jobs, int 
   int rc = ensure_init();
   if (rc) return rc;
   if (chunk <= 0) {
-    // about 40 MiB of raw frames per chunk (four 512^2 3x3 stacks): the host link, not
+    // about 60 MiB of raw frames per chunk (six 512^2 3x3 f32 stacks): the host link, not
     // the passes, bounds a host-buffer batch, and short chunks keep both copy directions
-    // busy from the start (measured on GB300, 64 stacks: chunks of 2 14.3k/s, 4 17.1k/s,
-    // 8 16.3k/s, 16 14.9k/s)
+    // busy from the start (measured on GB300, 64 stacks from one array, merged copies:
+    // chunks of 3 18.1k/s, 4 18.0k/s, 6 18.3k/s, 8 17.6k/s, 12 17.5k/s, 16 16.4k/s)
     const size_t rb = raw_bytes(reinterpret_cast<const Plan*>(jobs[0].plan));
-    chunk = (int)std::max<size_t>(1, ((size_t)40 << 20) / std::max<size_t>(rb, 1));
+    chunk = (int)std::max<size_t>(1, ((size_t)60 << 20) / std::max<size_t>(rb, 1));
   }
   chunk = std::min(chunk, n_jobs);
   std::lock_guard<std::mutex> lock(g_pipe.mu);

@@ -247,7 +247,7 @@ int fsim_recon_batch(const fsim_job* jobs, int n_jobs, void* workspace, size_t w
 /* Host-buffer batch (replaces the per-op Java-array copies of the accel vectors,
  * AccelVectorReal.java:218-247 / AccelVectorCplx.java:296-331, for whole stacks): uploads,
  * passes and downloads of successive chunks of `chunk` jobs
- * overlap on three library-owned streams (chunk 0 = about 40 MiB of raw frames); returns
+ * overlap on three library-owned streams (chunk 0 = about 60 MiB of raw frames); returns
  * when every output is in host memory.
  * Page-locked host buffers are copied by DMA; pageable ones copy synchronously. Jobs whose
  * host buffers follow one another in one allocation (one array of stacks, one of images)
